@@ -1,0 +1,35 @@
+"""Input types of the eigensubstitution path.
+
+They mirror subby's own NamedTuples so that code written against
+``subby.jax`` passes the same objects here:
+
+* ``Tree`` — subby/formats.py:15-17 (re-exported by subby/jax/types.py:5):
+  ``parentIndex`` (R,) int32 in preorder (``parentIndex[0] == -1``,
+  ``parentIndex[n] < n``), ``distanceToParent`` (R,) float64.
+* ``DiagModel`` — subby/jax/types.py:8-11: ``eigenvalues`` (A,),
+  ``eigenvectors`` (A, A) with ``v[a, k]`` = component a of eigenvector k of
+  the symmetrised rate matrix, ``pi`` (A,).
+* ``RateModel`` — subby/jax/types.py:21-23: ``subRate`` (A, A), ``rootProb``
+  (A,); diagonalised on the host on entry (subby/jax/__init__.py:44-50).
+"""
+from __future__ import annotations
+
+from typing import NamedTuple
+
+import numpy as np
+
+
+class Tree(NamedTuple):
+    parentIndex: np.ndarray
+    distanceToParent: np.ndarray
+
+
+class DiagModel(NamedTuple):
+    eigenvalues: np.ndarray
+    eigenvectors: np.ndarray
+    pi: np.ndarray
+
+
+class RateModel(NamedTuple):
+    subRate: np.ndarray
+    rootProb: np.ndarray

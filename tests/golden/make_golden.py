@@ -1,0 +1,144 @@
+"""Generate the golden fixtures under tests/golden/ from the REFERENCE oracle.
+
+Run in a container where ihh/subby is mounted (default /root/reference):
+
+    python tests/golden/make_golden.py [--reference /root/reference]
+
+It imports the reference's own CPU oracle (``subby.oracle``, numpy + scipy)
+and runs it on
+
+* the inputs of the reference's golden files ``tests/golden/*.json``
+  (5node_jc4, 7node_hky85_4, 7node_jc4_mixed_gaps, 7node_jc4_all_gaps,
+  7node_jc64), and
+* seeded synthetic cases of this repository (plain_small column subsets,
+  legacy -1 gaps, F81 with non-uniform pi, zero-length branches, random
+  reversible A=16 / A=20 models with near-degenerate eigenvalue pairs),
+
+and writes one ``.npz`` per case holding the inputs, the reference oracle's
+outputs (logLike, unmasked and Steiner-masked Counts, F81 fast-path Counts
+where the model is F81/JC, RootProb, branch mask) and, for the small A=4
+cases, its intermediates.  The fixtures travel with the repository; the
+reference itself is never read by the GPU tests.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.abspath(os.path.join(HERE, "..", "..")))
+
+
+def _ref(path):
+    sys.path.insert(0, path)
+    import subby.oracle as oracle          # noqa: E402  (reference)
+    from subby.formats import Tree         # noqa: E402  (reference)
+    return oracle, Tree
+
+
+def run_case(oracle, RTree, name, alignment, parent, dist, model, f81_ok,
+             intermediates=False, masked=True):
+    alignment = np.asarray(alignment, dtype=np.int32)
+    parent = np.asarray(parent, dtype=np.int32)
+    dist = np.asarray(dist, dtype=np.float64)
+    m = {k: np.asarray(model[k], dtype=np.float64) for k in ('eigenvalues', 'eigenvectors', 'pi')}
+    tree = RTree(parentIndex=parent, distanceToParent=dist)
+    A = len(m['pi'])
+    out = dict(alignment=alignment, parentIndex=parent, distanceToParent=dist,
+               eigenvalues=m['eigenvalues'], eigenvectors=m['eigenvectors'], pi=m['pi'],
+               A=np.int64(A))
+    out['logLike'] = oracle.LogLike(alignment, tree, m)
+    out['counts'] = oracle.Counts(alignment, tree, m, branch_mask=None)
+    if masked:
+        out['counts_masked'] = oracle.Counts(alignment, tree, m, branch_mask="auto")
+    if f81_ok:
+        out['counts_f81'] = oracle.Counts(alignment, tree, m, f81_fast=True, branch_mask=None)
+        if masked:
+            out['counts_f81_masked'] = oracle.Counts(alignment, tree, m, f81_fast=True,
+                                                     branch_mask="auto")
+    out['root_prob'] = oracle.RootProb(alignment, tree, m)
+    out['branch_mask'] = oracle.compute_branch_mask(alignment, parent, A)
+    if intermediates:
+        M = oracle.compute_sub_matrices(m, dist)
+        U, lnU, lnL = oracle.upward_pass(alignment, tree, M, m['pi'])
+        D, lnD = oracle.downward_pass(U, lnU, tree, M, m['pi'], alignment)
+        J = oracle.compute_J(m['eigenvalues'], dist)
+        Ut, Dt = oracle.eigenbasis_project(U, D, m)
+        Ce = oracle.accumulate_C(Dt, Ut, J, lnU, lnD, lnL, parent)
+        out.update(sub_matrices=M, U=U, logNormU=lnU, D=D, logNormD=lnD, J=J,
+                   U_tilde=Ut, D_tilde=Dt, C_eigen=Ce)
+    path = os.path.join(HERE, f"{name}.npz")
+    np.savez(path, **out)
+    print(f"  {name}: R={len(parent)} C={alignment.shape[1]} A={A} -> {os.path.basename(path)}")
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--reference", default="/root/reference")
+    args = ap.parse_args()
+    oracle, RTree = _ref(args.reference)
+    from subby_gb300 import synth, models
+
+    gdir = os.path.join(args.reference, "tests", "golden")
+    for fname, f81_ok, inter in [("5node_jc4", True, True), ("7node_hky85_4", False, True),
+                                 ("7node_jc4_mixed_gaps", True, True),
+                                 ("7node_jc4_all_gaps", True, True), ("7node_jc64", True, False)]:
+        with open(os.path.join(gdir, fname + ".json")) as f:
+            inp = json.load(f)['inputs']
+        run_case(oracle, RTree, "ref_" + fname, inp['alignment'], inp['parentIndex'],
+                 inp['distanceToParent'], inp['model'], f81_ok, intermediates=inter,
+                 masked=(fname != "7node_jc64"))
+
+    # plain_small column subset (R=31, A=4 HKY85, 5% unobserved split A/A+1)
+    w = synth.plain_small(seed=1, C=1024)
+    sel = np.random.default_rng(11).choice(1024, size=96, replace=False)
+    aln = w['alignment'][:, np.sort(sel)]
+    mm = w['model']._asdict()
+    run_case(oracle, RTree, "plain_small_sub96", aln, w['tree'].parentIndex,
+             w['tree'].distanceToParent, mm, False)
+
+    # legacy -1 gaps, observed internal tokens, an all-gap and an all-unobserved column
+    rng = np.random.default_rng(12)
+    tr = synth.random_tree(16, 0.1, rng)
+    R = len(tr.parentIndex)
+    aln = rng.integers(-1, 6, size=(R, 40)).astype(np.int32)
+    aln[:, 0] = -1
+    aln[:, 1] = 4
+    aln[:, 2] = 5
+    run_case(oracle, RTree, "legacy_gaps_hky", aln, tr.parentIndex, tr.distanceToParent,
+             models.hky85_diag(3.0, [0.1, 0.4, 0.3, 0.2])._asdict(), False)
+
+    # F81 non-uniform pi: fast path and general path on the same input
+    rng = np.random.default_rng(13)
+    tr = synth.random_tree(24, 0.2, rng)
+    m = models.f81_model(rng.dirichlet(np.ones(4)))
+    aln = synth.simulated_alignment(tr, m, 64, 0.1, rng)
+    run_case(oracle, RTree, "f81_4", aln, tr.parentIndex, tr.distanceToParent, m._asdict(), True)
+
+    # zero-length branches
+    rng = np.random.default_rng(14)
+    tr = synth.random_tree(10, 0.1, rng)
+    d = tr.distanceToParent.copy()
+    d[3] = 0.0
+    d[len(d) - 1] = 0.0
+    m = models.hky85_diag(2.0, [0.25, 0.25, 0.3, 0.2])
+    aln = synth.simulated_alignment(tr, m, 32, 0.1, rng)
+    run_case(oracle, RTree, "zero_branch_hky", aln, tr.parentIndex, d, m._asdict(), False)
+
+    # random reversible A=16 and A=20 with near-degenerate eigenvalue pairs
+    for A, L, C, seed in [(16, 8, 8, 15), (20, 6, 5, 16)]:
+        rng = np.random.default_rng(seed)
+        base, _, _ = models.random_reversible(A, rng, 1.0, 1.0)
+        m, _ = models.force_near_degenerate(base, rng, target_fraction=0.08, cluster=3)
+        tr = synth.random_tree(L, 0.1, rng)
+        aln = synth.simulated_alignment(tr, base, C, 0.1, rng)
+        run_case(oracle, RTree, f"reversible_{A}", aln, tr.parentIndex, tr.distanceToParent,
+                 m._asdict(), False)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,86 @@
+"""Pins the FP64 oracle (oracle/oracle.py) to the reference.
+
+* against fixtures made by running the reference's own oracle
+  (tests/golden/make_golden.py), including every intermediate for the small
+  cases, and
+* against the reference's golden JSON files directly when the reference tree
+  is mounted (skipped otherwise).
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+import oracle
+from tests import _golden
+
+CASES = _golden.names()
+
+
+def _tree(g):
+    return oracle.Tree(g['parentIndex'], g['distanceToParent'])
+
+
+def _model(g):
+    return {'eigenvalues': g['eigenvalues'], 'eigenvectors': g['eigenvectors'], 'pi': g['pi']}
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_outputs_match_reference_oracle(name):
+    g = _golden.load(name)
+    aln, tree, model = g['alignment'], _tree(g), _model(g)
+    np.testing.assert_allclose(oracle.LogLike(aln, tree, model), g['logLike'], rtol=1e-12, atol=1e-12)
+    np.testing.assert_allclose(oracle.Counts(aln, tree, model, branch_mask=None), g['counts'],
+                               rtol=1e-9, atol=1e-11)
+    if 'counts_masked' in g:
+        np.testing.assert_allclose(oracle.Counts(aln, tree, model), g['counts_masked'],
+                                   rtol=1e-9, atol=1e-11)
+    if 'counts_f81' in g:
+        np.testing.assert_allclose(oracle.Counts(aln, tree, model, f81_fast=True, branch_mask=None),
+                                   g['counts_f81'], rtol=1e-9, atol=1e-11)
+    if 'counts_f81_masked' in g:
+        np.testing.assert_allclose(oracle.Counts(aln, tree, model, f81_fast=True),
+                                   g['counts_f81_masked'], rtol=1e-9, atol=1e-11)
+    np.testing.assert_allclose(oracle.RootProb(aln, tree, model), g['root_prob'], rtol=1e-12, atol=1e-12)
+    np.testing.assert_array_equal(
+        oracle.compute_branch_mask(aln, g['parentIndex'], int(g['A'])), g['branch_mask'])
+
+
+@pytest.mark.parametrize("name", [n for n in CASES if 'U' in _golden.load(n)])
+def test_intermediates_match_reference_oracle(name):
+    g = _golden.load(name)
+    p = oracle.pipeline(g['alignment'], _tree(g), _model(g))
+    for k in ('sub_matrices', 'U', 'logNormU', 'D', 'logNormD', 'J', 'U_tilde', 'D_tilde', 'C_eigen'):
+        np.testing.assert_allclose(p[k], g[k], rtol=1e-11, atol=1e-12, err_msg=k)
+
+
+REF_GOLDEN = "/root/reference/tests/golden"
+
+
+@pytest.mark.skipif(not os.path.isdir(REF_GOLDEN), reason="reference tree not mounted")
+@pytest.mark.parametrize("fname", ["5node_jc4", "7node_hky85_4", "7node_jc4_mixed_gaps",
+                                   "7node_jc4_all_gaps", "7node_jc64"])
+def test_reference_golden_json(fname):
+    with open(os.path.join(REF_GOLDEN, fname + ".json")) as f:
+        gj = json.load(f)
+    inp = gj['inputs']
+    aln = np.asarray(inp['alignment'], dtype=np.int32)
+    tree = oracle.Tree(inp['parentIndex'], inp['distanceToParent'])
+    model = {k: np.asarray(v) for k, v in inp['model'].items()}
+    p = oracle.pipeline(aln, tree, model)
+    out = gj['outputs']
+    np.testing.assert_allclose(p['logLike'], out['logLike'], rtol=1e-12, atol=1e-12)
+    np.testing.assert_allclose(p['counts'], out['counts'], rtol=1e-9, atol=1e-12)
+    np.testing.assert_allclose(oracle.RootProb(aln, tree, model), out['root_prob'], rtol=1e-12, atol=1e-12)
+    np.testing.assert_array_equal(oracle.compute_branch_mask(aln, tree.parentIndex, inp['A']),
+                                  np.asarray(out['branch_mask']))
+    inter = gj['intermediates']
+    for k in ('sub_matrices', 'U', 'logNormU', 'D', 'logNormD', 'J', 'U_tilde', 'D_tilde', 'C_eigen'):
+        np.testing.assert_allclose(p[k], np.asarray(inter[k]), rtol=1e-10, atol=1e-12, err_msg=k)
+
+
+def test_validate_binary_tree_rejects():
+    with pytest.raises(ValueError):
+        oracle.validate_binary_tree([-1, 0, 0, 0])
+    oracle.validate_binary_tree([-1, 0, 0, 1, 1])

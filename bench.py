@@ -1,0 +1,351 @@
+"""Benchmark of the eigensubstitution hot path: Counts columns/s on one GB300.
+
+Workload (default): A=4 HKY85 (kappa=2, pi ~ Dir(1^4)), random binary tree
+with 128 leaves (R=255), branch lengths Exp(mean 0.05), C=2^20 columns
+simulated down the tree with 10% gaps.  One step = one Counts call (general
+eigensubstitution path, Steiner branch mask "auto" = the subby default) over
+all 2^20 columns.  The 1.07 GB token matrix is larger than L2 (129 MB), so
+no flush is needed between steps.  The F81 fast path is timed on the same
+tokens and tree with the F81 model and reported beside it.
+
+Output: one JSON line (rank 0).  ``value`` is device throughput with inputs
+resident in HBM; ``e2e`` is the same metric through the public API with host
+(pinned) buffers, copies included; ``roofline`` is the Counts kernel against
+the measured HBM copy bandwidth; ``cpu_baseline`` is the FP64 oracle port on
+the host cores on a bounded sample.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Under torchrun (N > 1) every rank processes its own 2^20 columns (weak
+scaling, no data-path collective); the step time is the max over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import multiprocessing as mp
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "Counts columns/s (A=4 HKY85, R=255, C=2^20, FP32, general eigensub path)"
+UNIT = "columns/s"
+
+
+def _peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), float(d["bf16_tflops"]), "measured"
+    return 6800.0, 1900.0, "fallback"
+
+
+def _traffic_per_column(kernel):
+    """DRAM bytes per column of `kernel` from the committed ncu summary, or None."""
+    p = os.path.join(ROOT, "profiles", "traffic.json")
+    if not os.path.exists(p):
+        return None
+    with open(p) as f:
+        d = json.load(f)
+    v = d.get(kernel)
+    return None if v is None else float(v["bytes_per_column"])
+
+
+class ClockSampler:
+    """nvidia-smi clocks/throttle sampling during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.idx = gpu_index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.idx}", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:  # noqa: BLE001
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:  # noqa: BLE001
+                self.proc.kill()
+            self.f.close()
+
+    def summary(self):
+        if not self.path or not os.path.exists(self.path):
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        with open(self.path) as f:
+            for line in f:
+                parts = [x.strip() for x in line.split(",")]
+                if len(parts) < 9:
+                    continue
+                try:
+                    sm.append(float(parts[1]))
+                    smax.append(float(parts[2]))
+                except ValueError:
+                    continue
+                for n, v in zip(names, parts[5:9]):
+                    if v.lower() == "active":
+                        reasons.add(n)
+        os.unlink(self.path)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------
+# CPU baseline: the FP64 oracle port over column shards (spawned workers)
+# ---------------------------------------------------------------------------
+
+def _oracle_counts_shard(args):
+    aln, parent, dist, ev, V, pi = args
+    import oracle
+    t = oracle.Tree(parent, dist)
+    oracle.Counts(aln, t, {'eigenvalues': ev, 'eigenvectors': V, 'pi': pi})
+    return aln.shape[1]
+
+
+def cpu_oracle_throughput(aln, tree, model, target_s=12.0, pool=None, cores=None):
+    """Columns/s of the oracle on a bounded sample sized to ~target_s of work."""
+    cores = cores or (os.cpu_count() or 1)
+    ev, V, pi = (np.asarray(x, dtype=np.float64) for x in (model.eigenvalues, model.eigenvectors, model.pi))
+    parent, dist = np.asarray(tree.parentIndex), np.asarray(tree.distanceToParent)
+    # calibrate on one shard in-process
+    cal = 1024
+    t0 = time.perf_counter()
+    _oracle_counts_shard((aln[:, :cal], parent, dist, ev, V, pi))
+    per_col = (time.perf_counter() - t0) / cal
+    shard = 2048
+    n_shards = max(cores, int(target_s * cores / max(per_col * shard, 1e-9)))
+    n_shards = min(n_shards, max(1, aln.shape[1] // shard))
+    sample = n_shards * shard
+    work = [(np.ascontiguousarray(aln[:, i * shard:(i + 1) * shard]), parent, dist, ev, V, pi)
+            for i in range(n_shards)]
+    t0 = time.perf_counter()
+    if pool is not None and cores > 1:
+        done = sum(pool.map(_oracle_counts_shard, work))
+    else:
+        done = sum(map(_oracle_counts_shard, work))
+    dt = time.perf_counter() - t0
+    return done / dt, cores, f"{sample} of {aln.shape[1]} columns ({n_shards} shards of {shard}), {dt:.1f} s"
+
+
+# ---------------------------------------------------------------------------
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--columns", type=int, default=1 << 20)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+
+    from subby_gb300 import synth
+
+    if args.impl == "reference":
+        if rank != 0:
+            return 0
+        return reference_arm(args, world)
+
+    # spawn pool for the CPU baseline before any GPU work
+    pool = None
+    cores = os.cpu_count() or 1
+    if rank == 0 and not args.no_cpu_baseline and cores > 1:
+        pool = mp.get_context("spawn").Pool(cores)
+
+    import torch
+    import subby_gb300 as sg
+    from subby_gb300 import _lib
+
+    torch.cuda.set_device(local_rank)
+    dist_on = world > 1
+    if dist_on:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local_rank))
+
+    C = args.columns
+    w = synth.plain_large(seed=2 + rank, C=C)
+    wf = synth.plain_large(seed=2 + rank, C=C, f81=True)
+    aln, tree, model = w['alignment'], w['tree'], w['model']
+    R, A = aln.shape[0], 4
+    plan = sg.Plan(tree, model)
+    plan_f81 = sg.Plan(wf['tree'], wf['model'])
+    d_aln = torch.as_tensor(aln).cuda()
+    d_aln_f = torch.as_tensor(wf['alignment']).cuda()
+    out = {'counts': torch.empty((A, A, C), dtype=torch.float32, device="cuda")}
+    out_f = {'counts': torch.empty((A, A, C), dtype=torch.float32, device="cuda")}
+    stream = torch.cuda.current_stream()
+
+    def step():
+        plan.run(d_aln, loglike=False, counts=True, branch_mask="auto", out=out)
+
+    def step_f81():
+        plan_f81.run(d_aln_f, loglike=False, counts=True, f81=True, branch_mask="auto", out=out_f)
+
+    def barrier():
+        if dist_on:
+            torch.distributed.barrier()
+
+    def timed(fn, K):
+        for _ in range(args.warmup):
+            fn()
+        torch.cuda.synchronize()
+        barrier()
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(K):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        barrier()
+        ms = e0.elapsed_time(e1) / K
+        if dist_on:
+            t = torch.tensor([ms], device="cuda")
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            ms = float(t.item())
+        return ms
+
+    # general path: headline value (clocks sampled during this region)
+    with ClockSampler(local_rank) as clk:
+        ms = timed(step, args.steps)
+    clocks = clk.summary()
+    launches_per_step = _lib.last_launch_count()
+    ms_f81 = timed(step_f81, args.steps)
+
+    # e2e through the public API with pinned host buffers (copies in the timed region)
+    h_aln = torch.empty((R, C), dtype=torch.int32, pin_memory=True)
+    h_aln.numpy()[:] = aln
+    h_out = torch.empty((A, A, C), dtype=torch.float32, pin_memory=True)
+    hbuf = {'counts': h_out.numpy()}
+    for _ in range(2):
+        plan.run(h_aln.numpy(), loglike=False, counts=True, branch_mask="auto", out=hbuf)
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(max(3, args.steps // 4)):
+        plan.run(h_aln.numpy(), loglike=False, counts=True, branch_mask="auto", out=hbuf)
+    e2e_ms = (time.perf_counter() - t0) * 1000 / max(3, args.steps // 4)
+    if dist_on:
+        t = torch.tensor([e2e_ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_ms = float(t.item())
+
+    # correctness spot check of this run against the oracle (64 columns)
+    import oracle
+    md = {'eigenvalues': np.asarray(model.eigenvalues), 'eigenvectors': np.asarray(model.eigenvectors),
+          'pi': np.asarray(model.pi)}
+    ref = oracle.Counts(aln[:, :64], oracle.Tree(tree.parentIndex, tree.distanceToParent), md)
+    got = out['counts'][:, :, :64].cpu().numpy()
+    from tests._tol import colwise_err
+    err = colwise_err(got, ref)
+
+    if rank != 0:
+        if dist_on:
+            torch.distributed.destroy_process_group()
+        return 0
+
+    hbm, _, peak_kind = _peaks()
+    b_col = 4 * R + 4 * A * A           # int32 tokens in, FP32 counts out
+    achieved = b_col * C / (ms / 1000) / 1e9
+    tr = _traffic_per_column("counts_eigen_a4")
+    cpu = None
+    if not args.no_cpu_baseline:
+        v, ncores, sample = cpu_oracle_throughput(aln, tree, model, pool=pool, cores=cores)
+        cpu = {"value": v, "unit": UNIT, "cores": ncores, "kind": "port",
+               "sample": "FP64 numpy oracle restatement, Counts (mask auto) on " + sample}
+    if pool is not None:
+        pool.close()
+    n = world
+    line = {
+        "metric": METRIC, "value": n * C / (ms / 1000), "unit": UNIT, "n_gpus": n,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "fp32", "data": "synthetic (seeded simulation)",
+        "config": {"workload": "plain_large: A=4 HKY85 kappa=2, R=255 (128 leaves), C=2^20 per GPU, "
+                               "10% gaps, branch_mask=auto", "columns_per_gpu": C, "R": R, "A": A,
+                   "l2": "inputs (1.07 GB tokens) larger than L2, no flush",
+                   "parallelism": f"column shards x{n}" if n > 1 else "single GPU"},
+        "f81_fast_path": {"value": n * C / (ms_f81 / 1000), "unit": UNIT, "ms_per_step": ms_f81},
+        "e2e": {"value": n * C / (e2e_ms / 1000), "unit": UNIT, "ms_per_step": e2e_ms,
+                "h2d_bytes_per_step": R * C * 4, "d2h_bytes_per_step": A * A * C * 4},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                     "frac": achieved / hbm, "peak_kind": peak_kind,
+                     "traffic": None if tr is None else tr * C,
+                     "algorithmic_bytes_per_column": b_col},
+        "cpu_baseline": cpu,
+        "clocks": clocks,
+        "gpu_launches": launches_per_step * args.steps,
+        "max_colwise_err_vs_oracle_64cols": err,
+    }
+    print(json.dumps(line))
+    if dist_on:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+def reference_arm(args, world):
+    """The reference's CPU algorithm (FP64 oracle port: the reference itself is
+    Python and does not travel) on the host cores, same workload and metric."""
+    from subby_gb300 import synth
+    C = args.columns
+    w = synth.plain_large(seed=2, C=C)
+    cores = os.cpu_count() or 1
+    pool = mp.get_context("spawn").Pool(cores) if cores > 1 else None
+    vals = []
+    sample = ""
+    for i in range(args.warmup + args.steps):
+        v, ncores, sample = cpu_oracle_throughput(w['alignment'], w['tree'], w['model'],
+                                                  target_s=4.0, pool=pool, cores=cores)
+        if i >= args.warmup:
+            vals.append(v)
+    if pool is not None:
+        pool.close()
+    v = float(statistics.median(vals))
+    line = {
+        "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": C / v * 1000, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "fp64", "data": "synthetic (seeded simulation)",
+        "config": {"workload": "plain_large: A=4 HKY85 kappa=2, R=255 (128 leaves), C=2^20, "
+                               "10% gaps, branch_mask=auto", "columns_per_gpu": C},
+        "impl": "reference",
+        "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": "per step: " + sample},
+        "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

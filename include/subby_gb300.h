@@ -1,0 +1,149 @@
+/*
+ * subby_gb300 — C ABI of the GB300 (sm_103a) eigensubstitution backend.
+ *
+ * One call computes, for every alignment column independently, the
+ * Felsenstein inside pass, the outside pass and the eigenbasis J(t) count
+ * accumulation of ihh/subby, on one GPU.  Inputs are the reference's
+ * (alignment, parentIndex, distanceToParent, eigenvalues, eigenvectors, pi)
+ * as flat arrays; outputs use the reference layouts (column last):
+ *
+ *   logLike   (C,)        float32     subby/jax/__init__.py:207-291
+ *   counts    (A, A, C)   float32     subby/jax/__init__.py:338-447
+ *             diagonal = dwell times, off-diagonal = substitution counts
+ *   rootProb  (A, C)      float32     subby/jax/__init__.py:543-650
+ *
+ * The flat-array argument convention (R = len(parentIndex), C = columns,
+ * A = len(pi), eigenvectors row-major v[a*A + k]) is that of the reference's
+ * Rust/WASM exports subby/wasm/src/lib.rs:622-760, which every entry point
+ * below mirrors; the reference's Python API the host shim reproduces is
+ * subby/jax/__init__.py.
+ *
+ * Conventions
+ *  - alignment is (R, C) int32 row-major; tokens 0..A-1 observed, A
+ *    ungapped-unobserved, A+1 gapped, -1 legacy gap; any other value is
+ *    treated as unobserved (subby/oracle/oracle.py:69-96).
+ *  - parentIndex[0] < 0, 0 <= parentIndex[n] < n, every node has 0 or 2
+ *    children (subby/oracle/oracle.py:52-62); violations return
+ *    SUBBY_ERR_TREE.
+ *  - Tree and model arrays are always host pointers (FP64 preparation stays
+ *    on the host, as in the reference).
+ *  - alignment, mask and output pointers are host pointers unless
+ *    SUBBY_DEVICE_PTRS is set in `flags`, in which case they are device
+ *    pointers on the current device.  With host pointers the call copies in
+ *    and out on `stream` and returns after the results are in host memory;
+ *    with device pointers it only enqueues work on `stream` (NULL = legacy
+ *    default stream).
+ *  - Every function returns 0 (SUBBY_OK) or a negative SUBBY_ERR_* code;
+ *    subby_strerror() names it and subby_last_error() gives details of the
+ *    most recent failure on the calling thread.
+ */
+#ifndef SUBBY_GB300_H
+#define SUBBY_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SUBBY_OK               0
+#define SUBBY_ERR_ARG         -1   /* null pointer / bad size / bad enum      */
+#define SUBBY_ERR_TREE        -2   /* parentIndex is not a binary preorder tree */
+#define SUBBY_ERR_UNSUPPORTED -3   /* alphabet size or tree too large          */
+#define SUBBY_ERR_CUDA        -4   /* CUDA runtime failure                     */
+#define SUBBY_ERR_NOMEM       -5   /* device or pinned allocation failed       */
+#define SUBBY_ERR_TIMEOUT     -6   /* a bounded device wait gave up            */
+
+/* flags */
+#define SUBBY_DEVICE_PTRS   1      /* alignment/mask/outputs are device pointers */
+#define SUBBY_BT_FP32       2      /* back-transform in FP32 (default: FP64 for A <= 8) */
+#define SUBBY_BT_FP64       4      /* force FP64 back-transform for any A          */
+
+/* mask_mode */
+#define SUBBY_MASK_NONE   0        /* every branch n >= 1 counts                 */
+#define SUBBY_MASK_AUTO   1        /* Steiner tree of ungapped leaves (default)  */
+#define SUBBY_MASK_GIVEN  2        /* (R, C) uint8 mask supplied by the caller   */
+
+/* Counts variants */
+#define SUBBY_COUNTS_EIGEN 0       /* general eigensubstitution path            */
+#define SUBBY_COUNTS_F81   1       /* O(A^2) F81/JC closed form (f81_fast_flag) */
+
+typedef struct subby_plan subby_plan;
+
+/* Library version string. */
+const char *subby_version(void);
+/* Human-readable name of a status code. */
+const char *subby_strerror(int status);
+/* Details of the last failure on the calling thread ("" if none). */
+const char *subby_last_error(void);
+
+/*
+ * Prepare a (tree, model) pair once: validates the tree, builds the
+ * postorder schedule, computes M(t) in FP64 on the host and J(t) on the GPU
+ * (FP64 only for near-degenerate eigenvalue pairs), and keeps every table
+ * resident on the current device.  Replaces the per-call model preparation
+ * of subby/jax/__init__.py:285-289 / 431-435 (compute_sub_matrices,
+ * subby/jax/diagonalize.py:141-172; compute_J, subby/jax/eigensub.py:7-50).
+ */
+int subby_plan_create(const int32_t *parent_index, const double *distances,
+                      const double *eigenvalues, const double *eigenvectors,
+                      const double *pi, int R, int A, subby_plan **out);
+int subby_plan_destroy(subby_plan *plan);
+/* Bytes of device memory the plan currently holds (tables + workspace). */
+size_t subby_plan_device_bytes(const subby_plan *plan);
+
+/*
+ * Run the hot path of a prepared plan on a (R, C) alignment.
+ *   logLike : (C,) or NULL
+ *   counts  : (A, A, C) or NULL (NULL skips the outside pass)
+ *   rootProb: (A, C) or NULL
+ *   counts_kind: SUBBY_COUNTS_EIGEN or SUBBY_COUNTS_F81
+ *   mask_mode / mask: as above (mask ignored unless SUBBY_MASK_GIVEN)
+ * Replaces subby.jax LogLike (subby/jax/__init__.py:207), Counts (:338) and
+ * RootProb (:543) for a single reversible DiagModel.
+ */
+int subby_plan_run(subby_plan *plan, const int32_t *alignment, int C,
+                   float *logLike, float *counts, float *rootProb,
+                   int counts_kind, int mask_mode, const uint8_t *mask,
+                   int flags, void *stream);
+
+/*
+ * Gradient of sum_c g_c * logLike_c (g NULL = all ones) with respect to the
+ * branch lengths (dldt, (R,), root entry 0) and to the symmetrised rate
+ * matrix S (dldS, (A, A), FP64, = sum_c g_c V C_c V^T with the unmasked
+ * eigenbasis counts C_c).  The distance part is the Fisher-identity rule of
+ * subby/jax/vjp.py:62-133; the rate part has no reference counterpart beyond
+ * jax.grad and is checked against finite differences.  logLike (C,) may be
+ * NULL.  Always synchronous.
+ */
+int subby_plan_grad(subby_plan *plan, const int32_t *alignment, int C,
+                    const float *g, float *logLike, double *dldt, double *dldS,
+                    int flags, void *stream);
+
+/* One-shot conveniences (plan create + run + destroy), mirroring the
+ * reference Rust/WASM exports wasm_log_like / wasm_counts / wasm_root_prob
+ * (subby/wasm/src/lib.rs:628-734) with explicit output buffers. */
+int subby_loglike(const int32_t *alignment, const int32_t *parent_index,
+                  const double *distances, const double *eigenvalues,
+                  const double *eigenvectors, const double *pi,
+                  int R, int C, int A, float *logLike, int flags, void *stream);
+int subby_counts(const int32_t *alignment, const int32_t *parent_index,
+                 const double *distances, const double *eigenvalues,
+                 const double *eigenvectors, const double *pi,
+                 int R, int C, int A, int counts_kind, int mask_mode,
+                 const uint8_t *mask, float *counts, int flags, void *stream);
+int subby_rootprob(const int32_t *alignment, const int32_t *parent_index,
+                   const double *distances, const double *eigenvalues,
+                   const double *eigenvectors, const double *pi,
+                   int R, int C, int A, float *rootProb, int flags, void *stream);
+
+/* Number of kernel launches the most recent subby_plan_run /
+ * subby_plan_grad on this thread enqueued (for launch accounting). */
+int subby_last_launch_count(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SUBBY_GB300_H */

@@ -1,1 +1,20 @@
-"""GB300-native backend for subby's eigensubstitution hot path (placeholder init)."""
+"""subby_gb300 — GB300-native (sm_103a) backend for subby's eigensubstitution
+hot path: Felsenstein inside pass, outside pass, eigenbasis J(t) count
+accumulation (general and F81/JC fast path), per-column LogLike, Counts and
+root posteriors.  Drop-in for the single-model entry points of ``subby.jax``.
+"""
+from .types import Tree, DiagModel, RateModel
+from .models import (hky85_diag, jukes_cantor_model, f81_model, diagonalize_rate_matrix,
+                     reversible_rate_matrix, random_reversible)
+from .api import LogLike, Counts, RootProb, LogLikeCustomGrad, Plan, get_plan, clear_plan_cache
+from . import _lib
+
+__all__ = ["Tree", "DiagModel", "RateModel", "hky85_diag", "jukes_cantor_model", "f81_model",
+           "diagonalize_rate_matrix", "reversible_rate_matrix", "random_reversible", "LogLike",
+           "Counts", "RootProb", "LogLikeCustomGrad", "Plan", "get_plan", "clear_plan_cache"]
+
+__version__ = "0.1.0"
+
+
+def library_path() -> str:
+    return _lib.library_path()

@@ -1,0 +1,106 @@
+"""ctypes binding of ``libsubby_gb300.so`` (the C ABI of include/subby_gb300.h).
+
+There is no CPU fallback: if the library is missing or cannot be loaded,
+every entry point raises ``RuntimeError``.
+"""
+from __future__ import annotations
+
+import ctypes as ct
+import os
+import threading
+
+from . import _build
+
+OK = 0
+ERR_ARG, ERR_TREE, ERR_UNSUPPORTED, ERR_CUDA, ERR_NOMEM, ERR_TIMEOUT = -1, -2, -3, -4, -5, -6
+DEVICE_PTRS, BT_FP32, BT_FP64 = 1, 2, 4
+MASK_NONE, MASK_AUTO, MASK_GIVEN = 0, 1, 2
+COUNTS_EIGEN, COUNTS_F81 = 0, 1
+
+# Exported symbols, as declared in include/subby_gb300.h.
+EXPORTS = (
+    "subby_version", "subby_strerror", "subby_last_error", "subby_plan_create",
+    "subby_plan_destroy", "subby_plan_device_bytes", "subby_plan_run", "subby_plan_grad",
+    "subby_loglike", "subby_counts", "subby_rootprob", "subby_last_launch_count",
+)
+
+_lock = threading.Lock()
+_lib = None
+
+_p = ct.c_void_p
+_i32p = ct.POINTER(ct.c_int32)
+_f64p = ct.POINTER(ct.c_double)
+
+
+class SubbyError(RuntimeError):
+    def __init__(self, code: int, where: str):
+        lib = _lib
+        name = lib.subby_strerror(code).decode() if lib else str(code)
+        detail = lib.subby_last_error().decode() if lib else ""
+        super().__init__(f"{where}: {name} ({code}){': ' + detail if detail else ''}")
+        self.code = code
+
+
+class TreeError(SubbyError, ValueError):
+    pass
+
+
+def _declare(lib):
+    lib.subby_version.restype = ct.c_char_p
+    lib.subby_strerror.restype = ct.c_char_p
+    lib.subby_strerror.argtypes = [ct.c_int]
+    lib.subby_last_error.restype = ct.c_char_p
+    lib.subby_last_launch_count.restype = ct.c_int
+    lib.subby_plan_create.restype = ct.c_int
+    lib.subby_plan_create.argtypes = [_p, _p, _p, _p, _p, ct.c_int, ct.c_int, ct.POINTER(ct.c_void_p)]
+    lib.subby_plan_destroy.restype = ct.c_int
+    lib.subby_plan_destroy.argtypes = [_p]
+    lib.subby_plan_device_bytes.restype = ct.c_size_t
+    lib.subby_plan_device_bytes.argtypes = [_p]
+    lib.subby_plan_run.restype = ct.c_int
+    lib.subby_plan_run.argtypes = [_p, _p, ct.c_int, _p, _p, _p, ct.c_int, ct.c_int, _p, ct.c_int, _p]
+    lib.subby_plan_grad.restype = ct.c_int
+    lib.subby_plan_grad.argtypes = [_p, _p, ct.c_int, _p, _p, _p, _p, ct.c_int, _p]
+    for name in ("subby_loglike", "subby_rootprob"):
+        f = getattr(lib, name)
+        f.restype = ct.c_int
+        f.argtypes = [_p, _p, _p, _p, _p, _p, ct.c_int, ct.c_int, ct.c_int, _p, ct.c_int, _p]
+    lib.subby_counts.restype = ct.c_int
+    lib.subby_counts.argtypes = [_p, _p, _p, _p, _p, _p, ct.c_int, ct.c_int, ct.c_int, ct.c_int,
+                                 ct.c_int, _p, _p, ct.c_int, _p]
+    return lib
+
+
+def library_path() -> str:
+    return _build.LIB_PATH
+
+
+def load(build_if_missing: bool = True):
+    """Load (building first if needed) the CUDA library; raise if impossible."""
+    global _lib
+    with _lock:
+        if _lib is not None:
+            return _lib
+        path = _build.LIB_PATH
+        if not os.path.exists(path) or build_if_missing:
+            try:
+                path = _build.build()
+            except Exception as e:  # noqa: BLE001
+                if not os.path.exists(path):
+                    raise RuntimeError(f"subby_gb300: CUDA library unavailable ({e})") from e
+        try:
+            _lib = _declare(ct.CDLL(path))
+        except OSError as e:
+            raise RuntimeError(f"subby_gb300: cannot load {path}: {e}") from e
+        return _lib
+
+
+def check(code: int, where: str):
+    if code != OK:
+        if code == ERR_TREE:
+            raise TreeError(code, where)
+        raise SubbyError(code, where)
+
+
+def last_launch_count() -> int:
+    return int(load().subby_last_launch_count())

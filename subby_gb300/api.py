@@ -1,0 +1,307 @@
+"""Drop-in replacement for the single-model entry points of ``subby.jax``.
+
+``LogLike``, ``Counts``, ``RootProb`` and ``LogLikeCustomGrad`` take the same
+arguments as subby/jax/__init__.py:207, :338, :543 and :294 and return the
+same shapes (column last).  They run on the GPU through the C ABI of
+``libsubby_gb300.so``; there is no CPU fallback.
+
+Inputs may be numpy arrays (results come back as numpy float32, copies in
+and out are part of the call) or CUDA ``torch`` tensors (results stay on the
+device as torch tensors, work is enqueued on the current torch stream).
+
+Not supported (raise ``NotImplementedError``): per-column model lists and
+model grids (subby/jax/__init__.py:53-205), irreversible complex models
+(``IrrevDiagModel``), and ``*H`` batch dimensions.
+"""
+from __future__ import annotations
+
+import ctypes as ct
+import hashlib
+import threading
+from collections import OrderedDict
+
+import numpy as np
+
+from . import _lib
+from .models import ensure_diag
+from .types import Tree
+
+_PLAN_CACHE_SIZE = 32
+
+
+def _is_torch(x) -> bool:
+    try:
+        import torch
+    except ImportError:  # pragma: no cover
+        return False
+    return isinstance(x, torch.Tensor)
+
+
+def _np(x, dtype):
+    if _is_torch(x):
+        x = x.detach().cpu().numpy()
+    return np.ascontiguousarray(np.asarray(x), dtype=dtype)
+
+
+def _ptr(a: np.ndarray):
+    return a.ctypes.data_as(ct.c_void_p)
+
+
+class Plan:
+    """A (tree, model) pair prepared once and kept resident on the GPU.
+
+    Creating a plan validates the tree (binary, preorder), builds the node
+    schedule, computes M(t) in FP64 on the host and J(t) on the GPU.  The
+    plan can then run any number of alignments with that tree and model.
+    """
+
+    def __init__(self, tree, model, device=None):
+        lib = _lib.load()
+        m = ensure_diag(model)
+        self.parentIndex = _np(tree.parentIndex, np.int32)
+        self.distances = _np(tree.distanceToParent, np.float64)
+        self.eigenvalues = _np(m.eigenvalues, np.float64)
+        self.eigenvectors = _np(m.eigenvectors, np.float64)
+        self.pi = _np(m.pi, np.float64)
+        if np.iscomplexobj(m.eigenvalues) or np.iscomplexobj(m.eigenvectors):
+            raise NotImplementedError("irreversible (complex) models are not supported")
+        self.R = int(self.parentIndex.shape[0])
+        self.A = int(self.pi.shape[0])
+        if self.distances.shape != (self.R,):
+            raise ValueError("distanceToParent must have shape (R,)")
+        if self.eigenvalues.shape != (self.A,) or self.eigenvectors.shape != (self.A, self.A):
+            raise ValueError("model arrays must have shapes (A,), (A, A), (A,)")
+        self.device = device
+        self._handle = ct.c_void_p()
+        self._lock = threading.Lock()
+        with _device_ctx(device):
+            _lib.check(lib.subby_plan_create(
+                _ptr(self.parentIndex), _ptr(self.distances), _ptr(self.eigenvalues),
+                _ptr(self.eigenvectors), _ptr(self.pi), self.R, self.A, ct.byref(self._handle)),
+                "subby_plan_create")
+
+    # ------------------------------------------------------------------ run
+    def run(self, alignment, loglike=True, counts=False, rootprob=False, f81=False,
+            branch_mask="auto", bt64=None, out=None):
+        """Run the hot path; returns a dict with the requested outputs.
+
+        ``branch_mask``: "auto" (Steiner mask, the reference default for
+        Counts), None (unmasked) or an (R, C) bool array.  ``bt64``: None =
+        FP64 back-transform for A <= 8 and FP32 above; True/False forces it.
+        ``out``: optional dict of preallocated output buffers (same keys).
+        """
+        lib = _lib.load()
+        kind = _lib.COUNTS_F81 if f81 else _lib.COUNTS_EIGEN
+        flags = 0
+        if bt64 is True:
+            flags |= _lib.BT_FP64
+        elif bt64 is False:
+            flags |= _lib.BT_FP32
+        if isinstance(branch_mask, str):
+            if branch_mask != "auto":
+                raise ValueError('branch_mask must be "auto", None or an (R, C) array')
+            mask_mode, mask = _lib.MASK_AUTO, None
+        elif branch_mask is None:
+            mask_mode, mask = _lib.MASK_NONE, None
+        else:
+            mask_mode, mask = _lib.MASK_GIVEN, branch_mask
+        if not counts:
+            mask_mode, mask = _lib.MASK_NONE, None
+        A = self.A
+        if _is_torch(alignment) and alignment.is_cuda:
+            import torch
+            aln = alignment
+            if aln.dtype != torch.int32:
+                aln = aln.to(torch.int32)
+            aln = aln.contiguous()
+            if aln.dim() != 2 or aln.shape[0] != self.R:
+                raise ValueError(f"alignment must have shape (R={self.R}, C)")
+            C = int(aln.shape[1])
+            dev = aln.device
+            res = {}
+            out = out or {}
+            if loglike:
+                res['logLike'] = out.get('logLike', torch.empty(C, dtype=torch.float32, device=dev))
+            if counts:
+                res['counts'] = out.get('counts', torch.empty((A, A, C), dtype=torch.float32, device=dev))
+            if rootprob:
+                res['rootProb'] = out.get('rootProb', torch.empty((A, C), dtype=torch.float32, device=dev))
+            dmask = None
+            if mask_mode == _lib.MASK_GIVEN:
+                dmask = torch.as_tensor(np.asarray(mask) if not _is_torch(mask) else mask)
+                dmask = dmask.to(device=dev, dtype=torch.uint8).contiguous()
+                if tuple(dmask.shape) != (self.R, C):
+                    raise ValueError("branch_mask must have shape (R, C)")
+            stream = torch.cuda.current_stream(dev).cuda_stream
+
+            def dp(t):
+                return ct.c_void_p(t.data_ptr()) if t is not None else None
+            with self._lock, _device_ctx(dev):
+                _lib.check(lib.subby_plan_run(
+                    self._handle, dp(aln), C, dp(res.get('logLike')), dp(res.get('counts')),
+                    dp(res.get('rootProb')), kind, mask_mode, dp(dmask),
+                    flags | _lib.DEVICE_PTRS, ct.c_void_p(stream)), "subby_plan_run")
+            return res
+        aln = _np(alignment, np.int32)
+        if aln.ndim != 2 or aln.shape[0] != self.R:
+            raise ValueError(f"alignment must have shape (R={self.R}, C)")
+        C = int(aln.shape[1])
+        out = out or {}
+        res = {}
+        if loglike:
+            res['logLike'] = out.get('logLike', np.empty(C, dtype=np.float32))
+        if counts:
+            res['counts'] = out.get('counts', np.empty((A, A, C), dtype=np.float32))
+        if rootprob:
+            res['rootProb'] = out.get('rootProb', np.empty((A, C), dtype=np.float32))
+        hmask = None
+        if mask_mode == _lib.MASK_GIVEN:
+            hmask = _np(mask, np.uint8)
+            if hmask.shape != (self.R, C):
+                raise ValueError("branch_mask must have shape (R, C)")
+
+        def hp(a):
+            return _ptr(a) if a is not None else None
+        with self._lock, _device_ctx(self.device):
+            _lib.check(lib.subby_plan_run(
+                self._handle, _ptr(aln), C, hp(res.get('logLike')), hp(res.get('counts')),
+                hp(res.get('rootProb')), kind, mask_mode, hp(hmask), flags, None),
+                "subby_plan_run")
+        return res
+
+    def grad(self, alignment, g=None, want_loglike=True):
+        """(logLike (C,), d(sum g logL)/dt (R,), d(sum g logL)/dS~ (A, A) FP64)."""
+        lib = _lib.load()
+        aln = _np(alignment, np.int32)
+        if aln.ndim != 2 or aln.shape[0] != self.R:
+            raise ValueError(f"alignment must have shape (R={self.R}, C)")
+        C = int(aln.shape[1])
+        gg = None if g is None else _np(g, np.float32)
+        ll = np.empty(C, dtype=np.float32) if want_loglike else None
+        dldt = np.zeros(self.R, dtype=np.float64)
+        dldS = np.zeros((self.A, self.A), dtype=np.float64)
+        with self._lock, _device_ctx(self.device):
+            _lib.check(lib.subby_plan_grad(
+                self._handle, _ptr(aln), C, _ptr(gg) if gg is not None else None,
+                _ptr(ll) if ll is not None else None, _ptr(dldt), _ptr(dldS), 0, None),
+                "subby_plan_grad")
+        return ll, dldt, dldS
+
+    def device_bytes(self) -> int:
+        return int(_lib.load().subby_plan_device_bytes(self._handle))
+
+    def close(self):
+        if getattr(self, "_handle", None) and self._handle.value:
+            _lib.load().subby_plan_destroy(self._handle)
+            self._handle = ct.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:  # noqa: BLE001
+            pass
+
+
+class _device_ctx:
+    def __init__(self, dev):
+        self.dev = dev
+        self.ctx = None
+
+    def __enter__(self):
+        if self.dev is not None:
+            import torch
+            self.ctx = torch.cuda.device(self.dev)
+            self.ctx.__enter__()
+
+    def __exit__(self, *a):
+        if self.ctx is not None:
+            self.ctx.__exit__(*a)
+
+
+# ---------------------------------------------------------------------------
+# plan cache and the subby.jax-compatible functions
+# ---------------------------------------------------------------------------
+
+_cache: "OrderedDict[str, Plan]" = OrderedDict()
+_cache_lock = threading.Lock()
+
+
+def _key(tree, model, device):
+    h = hashlib.sha1()
+    for a in (tree.parentIndex, tree.distanceToParent, model.eigenvalues, model.eigenvectors, model.pi):
+        arr = np.ascontiguousarray(_np(a, np.float64))
+        h.update(arr.tobytes())
+        h.update(str(arr.shape).encode())
+    h.update(str(device).encode())
+    return h.hexdigest()
+
+
+def get_plan(tree, model, device=None) -> Plan:
+    """Cached Plan for (tree, model)."""
+    _reject_batched(model)
+    m = ensure_diag(model)
+    k = _key(tree, m, device)
+    with _cache_lock:
+        p = _cache.get(k)
+        if p is not None:
+            _cache.move_to_end(k)
+            return p
+    p = Plan(tree, m, device)
+    with _cache_lock:
+        _cache[k] = p
+        while len(_cache) > _PLAN_CACHE_SIZE:
+            _cache.popitem(last=False)[1].close()
+    return p
+
+
+def clear_plan_cache():
+    with _cache_lock:
+        while _cache:
+            _cache.popitem()[1].close()
+
+
+def _reject_batched(model):
+    if isinstance(model, (list, tuple)) and not hasattr(model, '_fields'):
+        raise NotImplementedError("per-column model lists and model grids are not supported")
+
+
+def _device_of(x):
+    if _is_torch(x) and x.is_cuda:
+        return x.device
+    return None
+
+
+def LogLike(alignment, tree: Tree, model, maxChunkSize: int = 128):
+    """Per-column log-likelihoods (C,); subby/jax/__init__.py:207."""
+    del maxChunkSize  # columns are tiled on the device
+    return get_plan(tree, model, _device_of(alignment)).run(alignment, loglike=True)['logLike']
+
+
+def Counts(alignment, tree: Tree, model, maxChunkSize: int = 128, f81_fast_flag: bool = False,
+           branch_mask="auto"):
+    """(A, A, C) dwell times (diagonal) and substitution counts; subby/jax/__init__.py:338."""
+    del maxChunkSize
+    return get_plan(tree, model, _device_of(alignment)).run(
+        alignment, loglike=False, counts=True, f81=f81_fast_flag, branch_mask=branch_mask)['counts']
+
+
+def RootProb(alignment, tree: Tree, model, maxChunkSize: int = 128):
+    """(A, C) posterior root distribution; subby/jax/__init__.py:543."""
+    del maxChunkSize
+    return get_plan(tree, model, _device_of(alignment)).run(
+        alignment, loglike=False, rootprob=True)['rootProb']
+
+
+def LogLikeCustomGrad(alignment, tree: Tree, model, maxChunkSize: int = 128, method: str = 'eigen'):
+    """LogLike whose gradient w.r.t. ``tree.distanceToParent`` comes from the
+    hand-written adjoint kernel (subby/jax/__init__.py:294, vjp.py:35-136).
+
+    ``tree.distanceToParent`` may be a torch tensor with ``requires_grad``;
+    the result is then a torch tensor connected to it.  Only ``method='eigen'``
+    exists here (the Padé variant of the reference computes the same value).
+    """
+    del maxChunkSize
+    if method not in ('eigen', 'pade'):
+        raise ValueError("method must be 'eigen' or 'pade'")
+    from .autograd import loglike_with_grad
+    return loglike_with_grad(alignment, tree, model)

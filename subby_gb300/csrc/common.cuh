@@ -1,0 +1,96 @@
+// Shared definitions of the subby_gb300 kernels and host plan.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace subby {
+
+// Step of the node schedule: one internal node p with children l < r.
+// Steps are stored in postorder (children before parents); the outside pass
+// walks them backwards (preorder).
+//   step.x = p, step.y = l, step.z = r, step.w = flags (bit0 l is leaf,
+//   bit1 r is leaf, bit2 p is the root)
+//   slot.x = scratch slot of p (-1 root), slot.y = of l, slot.z = of r
+//            (-1 for leaves: leaves are recomputed from their token)
+enum : int { kLeafL = 1, kLeafR = 2, kRoot = 4 };
+
+enum : int {
+  kModeLogLike = 1,      // write logLike
+  kModeRootProb = 2,     // write rootProb
+  kModeCounts = 4,       // outside pass + counts
+  kModeF81 = 8,          // F81 closed form instead of the eigenbasis path
+  kModeBT64 = 16,        // FP64 back-transform
+  kModeGrad = 32,        // gradient accumulation instead of counts output
+};
+
+enum : int { kMaskNone = 0, kMaskAuto = 1, kMaskGiven = 2 };
+
+// Offsets (in floats) of the per-plan tables inside the packed FP32 buffer.
+struct TableOffsets {
+  int MT;    // R x (A+1) x A : MT[n][j][b] = M_n[b][j] (j<A), MT[n][A][b] = sum_j M_n[b][j]
+  int MN;    // R x A x A     : MN[n][i][a] = M_n[i][a]
+  int J;     // R x A x A     : J[n][k][l]
+  int JT;    // R x A x A     : JT[n][l][k] = J[n][k][l]
+  int F81;   // R x 4         : alpha, beta, gamma, t
+  int Vu;    // A x A         : Vu[b][l] = sqrt(pi_b) V[b][l]
+  int Vd;    // A x A         : Vd[a][k] = V[a][k] / sqrt(pi_a)
+  int Ut;    // (A+1) x A     : Ut[tok][l] = Vu[tok][l], Ut[A][l] = sum_b Vu[b][l]
+  int pi;    // A
+  int V;     // A x A         : V[i][k] (FP32 copy)
+  int S;     // A x A         : S[i][j] = sum_k V_ik mu_k V_jk
+  int ME;    // R x A         : mu_k e^{mu_k t_n} (distance gradient)
+  int total;
+};
+
+// A table copied into shared memory at kernel start.
+struct SmemTable {
+  int gofs;   // offset in the packed buffer (floats)
+  int sofs;   // offset in shared memory (floats)
+  int n;      // floats
+};
+
+constexpr int kMaxSmemTables = 8;
+
+struct KParams {
+  const int32_t *aln;     // (R, C)
+  int C, R, A, nInt;
+  int mode;
+  int mask_mode;
+  const uint8_t *mask;    // (R, C) when mask_mode == kMaskGiven
+  const float *tab;       // packed FP32 tables (device)
+  const double *tab64;    // V (A x A), S (A x A) in FP64
+  TableOffsets off;
+  const int4 *steps;      // (nInt,) device
+  const int4 *slots;      // (nInt,) device
+  int root_is_leaf;
+  float f81_mu;
+  // scratch: vectors [slot][worker][A] floats, words [slot][worker][2] ints
+  float *scrV;
+  int *scrW;
+  int nworkers;           // threads (small kernel) or warps (warp kernel) in the grid
+  // outputs
+  float *logL;
+  float *counts;
+  float *rootp;
+  // gradient outputs (kModeGrad): per-block partial sums
+  const float *g;         // (C,) cotangent or NULL (= ones)
+  double *grad_t;         // (gridDim.x, R)  partial d/dt
+  double *grad_C;         // (gridDim.x, A, A) partial sum_c g_c C_c (eigenbasis)
+  // shared-memory tables
+  int ntab;
+  SmemTable stab[kMaxSmemTables];
+  int smem_steps;         // sofs of steps (ints) in shared memory, -1 = read from global
+  int smem_slots;
+};
+
+// launchers (k_small.cu / k_warp.cu)
+int launch_small(const KParams &p, int A, int grid, int block, size_t smem, cudaStream_t s);
+int launch_warp(const KParams &p, int A, int grid, int block, size_t smem, cudaStream_t s);
+bool small_supported(int A);
+bool warp_supported(int A);
+int small_block();
+int warp_block();
+size_t warp_smem_per_warp(int A);
+
+}  // namespace subby

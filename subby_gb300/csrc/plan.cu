@@ -1,0 +1,685 @@
+// Host side of the subby_gb300 C ABI: tree validation and scheduling, FP64
+// model preparation, J(t) prologue kernel, workspace management and kernel
+// dispatch.  See include/subby_gb300.h for the contract.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "common.cuh"
+#include "subby_gb300.h"
+
+using namespace subby;
+
+namespace {
+
+thread_local std::string g_last_error;
+thread_local int g_launches = 0;
+
+int fail(int code, const std::string &msg) {
+  g_last_error = msg;
+  return code;
+}
+
+int cuda_fail(cudaError_t e, const char *where) {
+  return fail(SUBBY_ERR_CUDA, std::string(where) + ": " + cudaGetErrorString(e));
+}
+
+#define CU(call)                                   \
+  do {                                             \
+    cudaError_t e_ = (call);                       \
+    if (e_ != cudaSuccess) return cuda_fail(e_, #call); \
+  } while (0)
+
+// J(t) prologue.  J_kl(t) = (e^{mu_k t} - e^{mu_l t}) / (mu_k - mu_l), and
+// t e^{mu_k t} when |mu_k - mu_l| < 1e-8 (subby/oracle/oracle.py:931-959,
+// subby/jax/eigensub.py:7-50).  Pairs whose |dmu| t is below 1e-3 (the
+// near-degenerate ones, where the difference of exponentials cancels) are
+// evaluated in FP64; the others in FP32 through the cancellation-free form
+// e^{mu_l t} expm1(dmu t) / dmu with dmu taken from the FP64 eigenvalues.
+__global__ void k_compute_J(const double *__restrict__ mu, const double *__restrict__ t, int R,
+                            int A, float *__restrict__ J, float *__restrict__ JT) {
+  const int total = R * A * A;
+  for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < total;
+       idx += gridDim.x * blockDim.x) {
+    const int n = idx / (A * A);
+    const int k = (idx / A) % A;
+    const int l = idx % A;
+    const double tn = t[n];
+    const double dmu = mu[k] - mu[l];
+    float v;
+    if (fabs(dmu) < 1e-8) {
+      v = (float)(tn * exp(mu[k] * tn));
+    } else if (fabs(dmu) * tn < 1e-3) {
+      v = (float)((exp(mu[k] * tn) - exp(mu[l] * tn)) / dmu);
+    } else {
+      const float x = (float)(dmu * tn);
+      v = expf((float)(mu[l] * tn)) * expm1f(x) / (float)dmu;
+    }
+    J[idx] = v;
+    JT[(size_t)n * A * A + l * A + k] = v;
+  }
+}
+
+struct DevBuf {
+  void *p = nullptr;
+  size_t bytes = 0;
+  int grow(size_t need) {
+    if (need <= bytes) return 0;
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+    size_t want = need + need / 4;
+    cudaError_t e = cudaMalloc(&p, want);
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      e = cudaMalloc(&p, need);
+      if (e != cudaSuccess) {
+        cudaGetLastError();
+        p = nullptr;
+        return fail(SUBBY_ERR_NOMEM, "device allocation of " + std::to_string(need) + " bytes failed");
+      }
+      want = need;
+    }
+    bytes = want;
+    return 0;
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+  }
+};
+
+}  // namespace
+
+struct subby_plan {
+  int R = 0, A = 0, nInt = 0, device = 0, nsm = 0;
+  int root_is_leaf = 0;
+  std::vector<int4> steps, slots;
+  int nslots = 0;
+  std::vector<double> V, mu, pi;
+  float f81_mu = 0.f;
+  TableOffsets off{};
+  float *d_tab = nullptr;
+  double *d_tab64 = nullptr;
+  int4 *d_steps = nullptr, *d_slots = nullptr;
+  size_t tab_bytes = 0;
+  DevBuf work;     // scratch + gradient partials
+  DevBuf io;       // staging of alignment/mask/outputs in host-pointer mode
+  std::mutex lock;
+};
+
+namespace {
+
+int validate_tree(const int32_t *parent, int R, std::vector<int> &left, std::vector<int> &right) {
+  if (R < 1) return fail(SUBBY_ERR_TREE, "tree must have at least one node");
+  if (parent[0] >= 0) return fail(SUBBY_ERR_TREE, "parentIndex[0] must be negative (root)");
+  left.assign(R, -1);
+  right.assign(R, -1);
+  std::vector<int> cnt(R, 0);
+  for (int n = 1; n < R; ++n) {
+    const int p = parent[n];
+    if (p < 0 || p >= n)
+      return fail(SUBBY_ERR_TREE, "parentIndex[" + std::to_string(n) + "] = " + std::to_string(p) +
+                                       " is not in [0, " + std::to_string(n) + ")");
+    cnt[p]++;
+    if (left[p] < 0) left[p] = n;           // first seen = smaller index
+    else right[p] = n;
+  }
+  for (int n = 0; n < R; ++n)
+    if (cnt[n] != 0 && cnt[n] != 2)
+      return fail(SUBBY_ERR_TREE, "Node " + std::to_string(n) + " has " + std::to_string(cnt[n]) +
+                                       " children; expected 0 or 2.");
+  return 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *subby_version(void) { return "subby_gb300 0.1 (sm_103a)"; }
+
+const char *subby_strerror(int s) {
+  switch (s) {
+    case SUBBY_OK: return "ok";
+    case SUBBY_ERR_ARG: return "invalid argument";
+    case SUBBY_ERR_TREE: return "invalid tree";
+    case SUBBY_ERR_UNSUPPORTED: return "unsupported size";
+    case SUBBY_ERR_CUDA: return "CUDA error";
+    case SUBBY_ERR_NOMEM: return "out of memory";
+    case SUBBY_ERR_TIMEOUT: return "device wait timed out";
+    default: return "unknown status";
+  }
+}
+
+const char *subby_last_error(void) { return g_last_error.c_str(); }
+int subby_last_launch_count(void) { return g_launches; }
+
+int subby_plan_create(const int32_t *parent, const double *dist, const double *evals,
+                      const double *evecs, const double *pi, int R, int A, subby_plan **out) {
+  g_last_error.clear();
+  if (!out || !parent || !dist || !evals || !evecs || !pi) return fail(SUBBY_ERR_ARG, "null argument");
+  *out = nullptr;
+  if (!small_supported(A) && !warp_supported(A))
+    return fail(SUBBY_ERR_UNSUPPORTED, "alphabet size A=" + std::to_string(A) +
+                                            " not supported (2..8, 16, 20, 32, 64)");
+  if (R > (1 << 20)) return fail(SUBBY_ERR_UNSUPPORTED, "tree too large");
+  std::vector<int> left, right;
+  if (int rc = validate_tree(parent, R, left, right)) return rc;
+  for (int a = 0; a < A; ++a)
+    if (!(pi[a] > 0.0)) return fail(SUBBY_ERR_ARG, "pi must be strictly positive");
+  for (int n = 0; n < R; ++n)
+    if (!(dist[n] >= 0.0) || !std::isfinite(dist[n]))
+      return fail(SUBBY_ERR_ARG, "distances must be finite and non-negative");
+
+  auto *P = new subby_plan();
+  P->R = R;
+  P->A = A;
+  cudaGetDevice(&P->device);
+  cudaDeviceGetAttribute(&P->nsm, cudaDevAttrMultiProcessorCount, P->device);
+  P->root_is_leaf = (R == 1);
+
+  // DFS postorder of the internal nodes (children before parents).
+  std::vector<int> order;
+  if (R > 1) {
+    std::vector<std::pair<int, int>> st;
+    st.push_back({0, 0});
+    while (!st.empty()) {
+      auto &top = st.back();
+      const int v = top.first;
+      if (left[v] < 0) {  // leaf
+        st.pop_back();
+        continue;
+      }
+      if (top.second == 0) {
+        top.second = 1;
+        st.push_back({left[v], 0});
+      } else if (top.second == 1) {
+        top.second = 2;
+        st.push_back({right[v], 0});
+      } else {
+        order.push_back(v);
+        st.pop_back();
+      }
+    }
+  }
+  P->nInt = (int)order.size();
+  std::vector<int> slot(R, -1);
+  int ns = 0;
+  for (int v : order)
+    if (v != 0) slot[v] = ns++;
+  P->nslots = ns;
+  for (int v : order) {
+    const int l = left[v], r = right[v];
+    int flags = 0;
+    if (left[l] < 0) flags |= kLeafL;
+    if (left[r] < 0) flags |= kLeafR;
+    if (v == 0) flags |= kRoot;
+    P->steps.push_back(make_int4(v, l, r, flags));
+    P->slots.push_back(make_int4(slot[v], slot[l], slot[r], 0));
+  }
+
+  // ---- FP64 host tables
+  P->V.assign(evecs, evecs + (size_t)A * A);
+  P->mu.assign(evals, evals + A);
+  P->pi.assign(pi, pi + A);
+  std::vector<double> sp(A), isp(A);
+  double pi2 = 0.0;
+  for (int a = 0; a < A; ++a) {
+    sp[a] = std::sqrt(pi[a]);
+    isp[a] = 1.0 / sp[a];
+    pi2 += pi[a] * pi[a];
+  }
+  const double mu81 = 1.0 / (1.0 - pi2);
+  P->f81_mu = (float)mu81;
+
+  TableOffsets &o = P->off;
+  int cur = 0;
+  auto take = [&](int n) {
+    int at = cur;
+    cur += (n + 3) & ~3;  // 16-byte aligned tables
+    return at;
+  };
+  o.MT = take(R * (A + 1) * A);
+  // small block, contiguous in this order: Vu, Vd, Ut, pi, S, V
+  const int small_n = A * A + A * A + (A + 1) * A + A + A * A + A * A;
+  o.Vu = take(small_n);
+  o.Vd = o.Vu + A * A;
+  o.Ut = o.Vd + A * A;
+  o.pi = o.Ut + (A + 1) * A;
+  o.S = o.pi + A;
+  o.V = o.S + A * A;
+  o.MN = take(R * A * A);
+  o.J = take(R * A * A);
+  o.JT = take(R * A * A);
+  o.F81 = take(R * 4);
+  o.ME = take(R * A);
+  o.total = cur;
+  std::vector<float> tab((size_t)o.total, 0.f);
+  std::vector<double> E(A), M((size_t)A * A);
+  for (int n = 0; n < R; ++n) {
+    const double t = dist[n];
+    for (int k = 0; k < A; ++k) E[k] = std::exp(evals[k] * t);
+    for (int i = 0; i < A; ++i)
+      for (int j = 0; j < A; ++j) {
+        double s = 0.0;
+        for (int k = 0; k < A; ++k) s += evecs[i * A + k] * E[k] * evecs[j * A + k];
+        M[i * A + j] = isp[i] * sp[j] * s;  // subby/oracle/oracle.py:770-776
+      }
+    float *mt = tab.data() + o.MT + (size_t)n * (A + 1) * A;
+    float *mn = tab.data() + o.MN + (size_t)n * A * A;
+    for (int b = 0; b < A; ++b) {
+      double rs = 0.0;
+      for (int j = 0; j < A; ++j) {
+        mt[j * A + b] = (float)M[b * A + j];
+        rs += M[b * A + j];
+      }
+      mt[A * A + b] = (float)rs;
+    }
+    for (int i = 0; i < A * A; ++i) mn[i] = (float)M[i];
+    // F81 branch coefficients (subby/oracle/oracle.py:1226-1233)
+    const double e = std::exp(-mu81 * t), pp = 1.0 - e;
+    float *f = tab.data() + o.F81 + (size_t)n * 4;
+    f[0] = (float)(t * e);
+    f[1] = (float)(pp / mu81 - t * e);
+    f[2] = (float)(t * (1.0 + e) - 2.0 * pp / mu81);
+    f[3] = (float)t;
+    for (int k = 0; k < A; ++k) tab[o.ME + (size_t)n * A + k] = (float)(evals[k] * E[k]);
+  }
+  std::vector<double> S64((size_t)A * A);
+  for (int i = 0; i < A; ++i)
+    for (int j = 0; j < A; ++j) {
+      double s = 0.0;
+      for (int k = 0; k < A; ++k) s += evecs[i * A + k] * evals[k] * evecs[j * A + k];
+      S64[i * A + j] = s;
+    }
+  for (int b = 0; b < A; ++b)
+    for (int l = 0; l < A; ++l) {
+      tab[o.Vu + b * A + l] = (float)(sp[b] * evecs[b * A + l]);
+      tab[o.Vd + b * A + l] = (float)(isp[b] * evecs[b * A + l]);
+      tab[o.Ut + b * A + l] = (float)(sp[b] * evecs[b * A + l]);
+      tab[o.S + b * A + l] = (float)S64[b * A + l];
+      tab[o.V + b * A + l] = (float)evecs[b * A + l];
+    }
+  for (int l = 0; l < A; ++l) {
+    double s = 0.0;
+    for (int b = 0; b < A; ++b) s += sp[b] * evecs[b * A + l];
+    tab[o.Ut + A * A + l] = (float)s;
+  }
+  for (int a = 0; a < A; ++a) tab[o.pi + a] = (float)pi[a];
+
+  // ---- device upload
+  auto cleanup = [&](int rc) {
+    subby_plan_destroy(P);
+    return rc;
+  };
+  P->tab_bytes = (size_t)o.total * sizeof(float);
+  cudaError_t e = cudaMalloc(&P->d_tab, P->tab_bytes);
+  if (e != cudaSuccess) return cleanup(cuda_fail(e, "cudaMalloc(tables)"));
+  e = cudaMemcpy(P->d_tab, tab.data(), P->tab_bytes, cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) return cleanup(cuda_fail(e, "cudaMemcpy(tables)"));
+  e = cudaMalloc(&P->d_tab64, sizeof(double) * (2 * A * A + A + R));
+  if (e != cudaSuccess) return cleanup(cuda_fail(e, "cudaMalloc(tables64)"));
+  std::vector<double> t64((size_t)2 * A * A + A + R);
+  std::copy(evecs, evecs + A * A, t64.begin());
+  std::copy(S64.begin(), S64.end(), t64.begin() + A * A);
+  std::copy(evals, evals + A, t64.begin() + 2 * A * A);
+  std::copy(dist, dist + R, t64.begin() + 2 * A * A + A);
+  e = cudaMemcpy(P->d_tab64, t64.data(), sizeof(double) * t64.size(), cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) return cleanup(cuda_fail(e, "cudaMemcpy(tables64)"));
+  if (P->nInt > 0) {
+    e = cudaMalloc(&P->d_steps, sizeof(int4) * P->nInt);
+    if (e == cudaSuccess) e = cudaMalloc(&P->d_slots, sizeof(int4) * P->nInt);
+    if (e == cudaSuccess)
+      e = cudaMemcpy(P->d_steps, P->steps.data(), sizeof(int4) * P->nInt, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess)
+      e = cudaMemcpy(P->d_slots, P->slots.data(), sizeof(int4) * P->nInt, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return cleanup(cuda_fail(e, "schedule upload"));
+  }
+  {
+    const int total = R * A * A;
+    const int blk = 256, grd = std::max(1, std::min((total + blk - 1) / blk, 4096));
+    k_compute_J<<<grd, blk>>>(P->d_tab64 + 2 * A * A, P->d_tab64 + 2 * A * A + A, R, A,
+                              P->d_tab + o.J, P->d_tab + o.JT);
+    e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaDeviceSynchronize();
+    if (e != cudaSuccess) return cleanup(cuda_fail(e, "J(t) prologue"));
+  }
+  *out = P;
+  return SUBBY_OK;
+}
+
+int subby_plan_destroy(subby_plan *P) {
+  if (!P) return SUBBY_OK;
+  if (P->d_tab) cudaFree(P->d_tab);
+  if (P->d_tab64) cudaFree(P->d_tab64);
+  if (P->d_steps) cudaFree(P->d_steps);
+  if (P->d_slots) cudaFree(P->d_slots);
+  P->work.release();
+  P->io.release();
+  delete P;
+  return SUBBY_OK;
+}
+
+size_t subby_plan_device_bytes(const subby_plan *P) {
+  if (!P) return 0;
+  return P->tab_bytes + P->work.bytes + P->io.bytes + sizeof(int4) * 2 * P->nInt;
+}
+
+}  // extern "C"
+
+namespace {
+
+struct Launch {
+  KParams kp{};
+  bool small = true;
+  int grid = 1, block = 128;
+  size_t smem = 0;
+  int nworkers = 0;
+};
+
+// Shared-memory tables and grid size of the small (thread-per-column) kernel.
+int plan_small(subby_plan *P, int mode, int C, Launch &L) {
+  const int A = P->A, R = P->R;
+  KParams &k = L.kp;
+  int ntab = 0, sofs = 0;
+  auto add = [&](int gofs, int n) {
+    k.stab[ntab++] = SmemTable{gofs, sofs, n};
+    sofs += (n + 3) & ~3;
+  };
+  const TableOffsets &o = P->off;
+  add(o.MT, R * (A + 1) * A);
+  add(o.Vu, A * A * 4 + (A + 1) * A + A);
+  if (mode & (kModeCounts | kModeGrad)) {
+    add(o.MN, R * A * A);
+    if (mode & kModeF81) add(o.F81, R * 4);
+    else add(o.J, R * A * A);
+    if (mode & kModeGrad) add(o.ME, R * A);
+  }
+  k.ntab = ntab;
+  k.smem_steps = sofs;
+  sofs += 4 * P->nInt;
+  k.smem_slots = sofs;
+  sofs += 4 * P->nInt;
+  L.smem = (size_t)sofs * sizeof(float);
+  int maxsm = 0;
+  cudaDeviceGetAttribute(&maxsm, cudaDevAttrMaxSharedMemoryPerBlockOptin, P->device);
+  if (L.smem > (size_t)maxsm)
+    return fail(SUBBY_ERR_UNSUPPORTED, "tree too large for the shared-memory tables (R=" +
+                                           std::to_string(R) + ", A=" + std::to_string(A) + ")");
+  L.small = true;
+  L.block = small_block();
+  // occupancy-limited persistent grid
+  int per_sm = std::max(1, (int)(((size_t)maxsm + 1024) / (L.smem + 1024)));
+  per_sm = std::min(per_sm, 2048 / L.block);
+  int want = (C + L.block - 1) / L.block;
+  L.grid = std::max(1, std::min(want, P->nsm * per_sm));
+  L.nworkers = L.grid * L.block;
+  return 0;
+}
+
+int plan_warp(subby_plan *P, int mode, int C, Launch &L) {
+  (void)mode;
+  L.small = false;
+  L.block = warp_block();
+  const int wpb = L.block / 32;
+  L.smem = warp_smem_per_warp(P->A) * wpb;
+  L.kp.ntab = 0;
+  L.kp.smem_steps = -1;
+  int maxsm = 0;
+  cudaDeviceGetAttribute(&maxsm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, P->device);
+  int per_sm = std::max(1, (int)((size_t)maxsm / (L.smem + 1024)));
+  per_sm = std::min(per_sm, 8);
+  int want = (C + wpb - 1) / wpb;
+  L.grid = std::max(1, std::min(want, P->nsm * per_sm));
+  L.nworkers = L.grid * wpb;
+  return 0;
+}
+
+int run_common(subby_plan *P, const int32_t *d_aln, int C, float *d_logL, float *d_counts,
+               float *d_root, int mode, int mask_mode, const uint8_t *d_mask, const float *d_g,
+               double *d_gt, double *d_gC, int *grid_out, cudaStream_t stream) {
+  Launch L;
+  const bool small = small_supported(P->A);
+  int rc = small ? plan_small(P, mode, C, L) : plan_warp(P, mode, C, L);
+  if (rc) return rc;
+  KParams &k = L.kp;
+  k.aln = d_aln;
+  k.C = C;
+  k.R = P->R;
+  k.A = P->A;
+  k.nInt = P->nInt;
+  k.mode = mode;
+  k.mask_mode = mask_mode;
+  k.mask = d_mask;
+  k.tab = P->d_tab;
+  k.tab64 = P->d_tab64;
+  k.off = P->off;
+  k.steps = P->d_steps;
+  k.slots = P->d_slots;
+  k.root_is_leaf = P->root_is_leaf;
+  k.f81_mu = P->f81_mu;
+  k.nworkers = L.nworkers;
+  k.logL = d_logL;
+  k.counts = d_counts;
+  k.rootp = d_root;
+  k.g = d_g;
+  k.grad_t = d_gt;
+  k.grad_C = d_gC;
+  // scratch
+  const size_t nsl = (size_t)std::max(P->nslots, 1);
+  const size_t vbytes = nsl * L.nworkers * P->A * sizeof(float);
+  const size_t wbytes = nsl * L.nworkers * 2 * sizeof(int);
+  const size_t vb_al = (vbytes + 255) & ~(size_t)255;
+  if ((rc = P->work.grow(vb_al + wbytes))) return rc;
+  k.scrV = (float *)P->work.p;
+  k.scrW = (int *)((char *)P->work.p + vb_al);
+  if (grid_out) *grid_out = L.grid;
+  int lr = small ? launch_small(k, P->A, L.grid, L.block, L.smem, stream)
+                 : launch_warp(k, P->A, L.grid, L.block, L.smem, stream);
+  if (lr != 0) return fail(SUBBY_ERR_CUDA, std::string("kernel launch failed: ") +
+                                               cudaGetErrorString((cudaError_t)lr));
+  g_launches += 1;
+  return 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+int subby_plan_run(subby_plan *P, const int32_t *aln, int C, float *logL, float *counts,
+                   float *rootProb, int counts_kind, int mask_mode, const uint8_t *mask, int flags,
+                   void *stream_) {
+  g_last_error.clear();
+  g_launches = 0;
+  if (!P || !aln) return fail(SUBBY_ERR_ARG, "null plan or alignment");
+  if (C < 0) return fail(SUBBY_ERR_ARG, "negative column count");
+  if (mask_mode < 0 || mask_mode > 2) return fail(SUBBY_ERR_ARG, "bad mask_mode");
+  if (mask_mode == SUBBY_MASK_GIVEN && !mask) return fail(SUBBY_ERR_ARG, "mask required");
+  if (counts_kind != SUBBY_COUNTS_EIGEN && counts_kind != SUBBY_COUNTS_F81)
+    return fail(SUBBY_ERR_ARG, "bad counts_kind");
+  if (C == 0) return SUBBY_OK;
+  std::lock_guard<std::mutex> g(P->lock);
+  cudaStream_t stream = (cudaStream_t)stream_;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev != P->device) CU(cudaSetDevice(P->device));
+  const int A = P->A, R = P->R;
+  int mode = 0;
+  if (logL) mode |= kModeLogLike;
+  if (rootProb) mode |= kModeRootProb;
+  if (counts) mode |= kModeCounts;
+  if (counts && counts_kind == SUBBY_COUNTS_F81) mode |= kModeF81;
+  const bool bt64 = (flags & SUBBY_BT_FP64) || (!(flags & SUBBY_BT_FP32) && A <= 8);
+  if (bt64) mode |= kModeBT64;
+  if (!mode) return SUBBY_OK;
+  int rc = 0;
+  if (flags & SUBBY_DEVICE_PTRS) {
+    rc = run_common(P, aln, C, logL, counts, rootProb, mode, mask_mode, mask, nullptr, nullptr,
+                    nullptr, nullptr, stream);
+    if (rc == 0 && dev != P->device) cudaSetDevice(dev);
+    return rc;
+  }
+  // host pointers: stage through device buffers on `stream`
+  const size_t b_aln = (size_t)R * C * sizeof(int32_t);
+  const size_t b_mask = (mask_mode == SUBBY_MASK_GIVEN) ? (size_t)R * C : 0;
+  const size_t b_ll = logL ? (size_t)C * 4 : 0;
+  const size_t b_ct = counts ? (size_t)A * A * C * 4 : 0;
+  const size_t b_rp = rootProb ? (size_t)A * C * 4 : 0;
+  auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
+  const size_t total = al(b_aln) + al(b_mask) + al(b_ll) + al(b_ct) + al(b_rp);
+  if ((rc = P->io.grow(total))) return rc;
+  char *base = (char *)P->io.p;
+  int32_t *d_aln = (int32_t *)base;
+  base += al(b_aln);
+  uint8_t *d_mask = b_mask ? (uint8_t *)base : nullptr;
+  base += al(b_mask);
+  float *d_ll = b_ll ? (float *)base : nullptr;
+  base += al(b_ll);
+  float *d_ct = b_ct ? (float *)base : nullptr;
+  base += al(b_ct);
+  float *d_rp = b_rp ? (float *)base : nullptr;
+  CU(cudaMemcpyAsync(d_aln, aln, b_aln, cudaMemcpyHostToDevice, stream));
+  if (b_mask) CU(cudaMemcpyAsync(d_mask, mask, b_mask, cudaMemcpyHostToDevice, stream));
+  rc = run_common(P, d_aln, C, d_ll, d_ct, d_rp, mode, mask_mode, d_mask, nullptr, nullptr,
+                  nullptr, nullptr, stream);
+  if (rc) return rc;
+  if (b_ll) CU(cudaMemcpyAsync(logL, d_ll, b_ll, cudaMemcpyDeviceToHost, stream));
+  if (b_ct) CU(cudaMemcpyAsync(counts, d_ct, b_ct, cudaMemcpyDeviceToHost, stream));
+  if (b_rp) CU(cudaMemcpyAsync(rootProb, d_rp, b_rp, cudaMemcpyDeviceToHost, stream));
+  CU(cudaStreamSynchronize(stream));
+  if (dev != P->device) cudaSetDevice(dev);
+  return SUBBY_OK;
+}
+
+int subby_plan_grad(subby_plan *P, const int32_t *aln, int C, const float *g, float *logL,
+                    double *dldt, double *dldS, int flags, void *stream_) {
+  g_last_error.clear();
+  g_launches = 0;
+  if (!P || !aln || !dldt || !dldS) return fail(SUBBY_ERR_ARG, "null argument");
+  if (C <= 0) return fail(SUBBY_ERR_ARG, "C must be positive");
+  std::lock_guard<std::mutex> lk(P->lock);
+  cudaStream_t stream = (cudaStream_t)stream_;
+  const int A = P->A, R = P->R;
+  const bool dev = (flags & SUBBY_DEVICE_PTRS) != 0;
+  // staging for host pointers
+  const int32_t *d_aln = aln;
+  const float *d_g = g;
+  float *d_ll = logL;
+  auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
+  int rc = 0;
+  if (!dev) {
+    const size_t b_aln = (size_t)R * C * 4, b_g = g ? (size_t)C * 4 : 0, b_ll = logL ? (size_t)C * 4 : 0;
+    if ((rc = P->io.grow(al(b_aln) + al(b_g) + al(b_ll)))) return rc;
+    char *base = (char *)P->io.p;
+    int32_t *a = (int32_t *)base;
+    base += al(b_aln);
+    float *gg = b_g ? (float *)base : nullptr;
+    base += al(b_g);
+    float *ll = b_ll ? (float *)base : nullptr;
+    CU(cudaMemcpyAsync(a, aln, b_aln, cudaMemcpyHostToDevice, stream));
+    if (b_g) CU(cudaMemcpyAsync(gg, g, b_g, cudaMemcpyHostToDevice, stream));
+    d_aln = a;
+    d_g = gg;
+    d_ll = ll;
+  }
+  // gradient partials live in a separate small allocation per call
+  Launch L;
+  const int mode = kModeGrad | (logL ? kModeLogLike : 0);
+  rc = small_supported(A) ? plan_small(P, mode, C, L) : plan_warp(P, mode, C, L);
+  if (rc) return rc;
+  const size_t nb = (size_t)L.grid;
+  double *d_part = nullptr;
+  const size_t pbytes = nb * ((size_t)R + (size_t)A * A) * sizeof(double);
+  CU(cudaMalloc(&d_part, pbytes));
+  CU(cudaMemsetAsync(d_part, 0, pbytes, stream));
+  int grid = 0;
+  rc = run_common(P, d_aln, C, d_ll, nullptr, nullptr, mode, SUBBY_MASK_NONE, nullptr, d_g, d_part,
+                  d_part + nb * R, &grid, stream);
+  if (rc) {
+    cudaFree(d_part);
+    return rc;
+  }
+  std::vector<double> part(nb * ((size_t)R + (size_t)A * A));
+  cudaError_t e = cudaMemcpyAsync(part.data(), d_part, pbytes, cudaMemcpyDeviceToHost, stream);
+  if (e == cudaSuccess && logL && !dev)
+    e = cudaMemcpyAsync(logL, d_ll, (size_t)C * 4, cudaMemcpyDeviceToHost, stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
+  cudaFree(d_part);
+  if (e != cudaSuccess) return cuda_fail(e, "gradient readback");
+  if ((size_t)grid != nb) return fail(SUBBY_ERR_CUDA, "grid mismatch");
+  for (int n = 0; n < R; ++n) {
+    double s = 0.0;
+    for (size_t b = 0; b < nb; ++b) s += part[b * R + n];
+    dldt[n] = (n == 0) ? 0.0 : s;
+  }
+  std::vector<double> Cg((size_t)A * A, 0.0);
+  const double *pc = part.data() + nb * R;
+  for (size_t b = 0; b < nb; ++b)
+    for (int i = 0; i < A * A; ++i) Cg[i] += pc[b * A * A + i];
+  // dL/dS~ = V Cg V^T (FP64)
+  const std::vector<double> &V = P->V;
+  std::vector<double> T((size_t)A * A, 0.0);
+  for (int k = 0; k < A; ++k)
+    for (int j = 0; j < A; ++j) {
+      double s = 0.0;
+      for (int l = 0; l < A; ++l) s += Cg[k * A + l] * V[j * A + l];
+      T[k * A + j] = s;
+    }
+  for (int i = 0; i < A; ++i)
+    for (int j = 0; j < A; ++j) {
+      double s = 0.0;
+      for (int k = 0; k < A; ++k) s += V[i * A + k] * T[k * A + j];
+      dldS[i * A + j] = s;
+    }
+  return SUBBY_OK;
+}
+
+static int one_shot(const int32_t *aln, const int32_t *parent, const double *dist, const double *ev,
+                    const double *evec, const double *pi, int R, int C, int A, float *ll, float *ct,
+                    float *rp, int kind, int mask_mode, const uint8_t *mask, int flags, void *stream) {
+  subby_plan *P = nullptr;
+  int rc = subby_plan_create(parent, dist, ev, evec, pi, R, A, &P);
+  if (rc) return rc;
+  rc = subby_plan_run(P, aln, C, ll, ct, rp, kind, mask_mode, mask, flags, stream);
+  if (rc == 0 && (flags & SUBBY_DEVICE_PTRS)) {
+    cudaError_t e = cudaStreamSynchronize((cudaStream_t)stream);
+    if (e != cudaSuccess) rc = cuda_fail(e, "stream sync");
+  }
+  std::string keep = g_last_error;
+  subby_plan_destroy(P);
+  g_last_error = keep;
+  return rc;
+}
+
+int subby_loglike(const int32_t *aln, const int32_t *parent, const double *dist, const double *ev,
+                  const double *evec, const double *pi, int R, int C, int A, float *logL, int flags,
+                  void *stream) {
+  if (!logL) return fail(SUBBY_ERR_ARG, "null output");
+  return one_shot(aln, parent, dist, ev, evec, pi, R, C, A, logL, nullptr, nullptr, 0,
+                  SUBBY_MASK_NONE, nullptr, flags, stream);
+}
+
+int subby_counts(const int32_t *aln, const int32_t *parent, const double *dist, const double *ev,
+                 const double *evec, const double *pi, int R, int C, int A, int kind, int mask_mode,
+                 const uint8_t *mask, float *counts, int flags, void *stream) {
+  if (!counts) return fail(SUBBY_ERR_ARG, "null output");
+  return one_shot(aln, parent, dist, ev, evec, pi, R, C, A, nullptr, counts, nullptr, kind,
+                  mask_mode, mask, flags, stream);
+}
+
+int subby_rootprob(const int32_t *aln, const int32_t *parent, const double *dist, const double *ev,
+                   const double *evec, const double *pi, int R, int C, int A, float *rootProb,
+                   int flags, void *stream) {
+  if (!rootProb) return fail(SUBBY_ERR_ARG, "null output");
+  return one_shot(aln, parent, dist, ev, evec, pi, R, C, A, nullptr, nullptr, rootProb, 0,
+                  SUBBY_MASK_NONE, nullptr, flags, stream);
+}
+
+}  // extern "C"

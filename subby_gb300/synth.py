@@ -75,23 +75,33 @@ def sub_matrices64(model: DiagModel, distances) -> np.ndarray:
 
 
 def simulate_states(tree: Tree, model: DiagModel, C: int, rng: np.random.Generator) -> np.ndarray:
-    """States at every node, (R, C) int32: root ~ pi, child ~ row of M(t)."""
+    """States at every node, (R, C) int32: root ~ pi, child ~ row of M(t).
+
+    Inverse-CDF sampling with FP64 transition rows (rounded to FP32
+    thresholds): child = #{k < A-1 : u >= cumM[parent_state, k]}.
+    """
     pi = np.asarray(model.pi, dtype=np.float64)
     A = len(pi)
     R = len(tree.parentIndex)
     M = sub_matrices64(model, tree.distanceToParent)
-    cumM = np.cumsum(M, axis=-1)
+    cumM = np.cumsum(M, axis=-1).astype(np.float32)
     cumM[..., -1] = 1.0
-    states = np.empty((R, C), dtype=np.int32)
-    cpi = np.cumsum(pi)
+    st_dtype = np.int8 if A <= 127 else np.int16
+    states = np.empty((R, C), dtype=st_dtype)
+    cpi = np.cumsum(pi).astype(np.float32)
     cpi[-1] = 1.0
-    states[0] = np.searchsorted(cpi, rng.random(C), side='right').clip(0, A - 1)
+    u = rng.random(C, dtype=np.float32)
+    states[0] = np.searchsorted(cpi, u, side='right').clip(0, A - 1)
     for n in range(1, R):
         p = tree.parentIndex[n]
-        u = rng.random(C)
-        rows = cumM[n][states[p]]                       # (C, A)
-        states[n] = (u[:, None] >= rows).sum(axis=1).clip(0, A - 1)
-    return states
+        u = rng.random(C, dtype=np.float32)
+        sp = states[p]
+        out = np.zeros(C, dtype=st_dtype)
+        cn = cumM[n]
+        for k in range(A - 1):
+            out += (u >= cn[:, k][sp])
+        states[n] = out
+    return states.astype(np.int32)
 
 
 def leaf_mask(tree: Tree) -> np.ndarray:
@@ -110,10 +120,10 @@ def simulated_alignment(tree: Tree, model: DiagModel, C: int, gap_rate: float,
     aln = simulate_states(tree, model, C, rng)
     leaf = leaf_mask(tree)
     aln[~leaf] = A
-    g = rng.random(aln.shape) < gap_rate
+    g = rng.random(aln.shape, dtype=np.float32) < gap_rate
     g &= leaf[:, None]
     if unobserved_split:
-        half = rng.random(aln.shape) < 0.5
+        half = rng.random(aln.shape, dtype=np.float32) < 0.5
         aln[g & half] = A
         aln[g & ~half] = A + 1
     else:

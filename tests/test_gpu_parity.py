@@ -1,0 +1,192 @@
+"""GPU parity: the CUDA path through the C ABI vs the FP64 oracle.
+
+Every case compares LogLike, Counts (unmasked, Steiner-masked, F81 fast
+path) and RootProb with the tolerances of tests/_tol.py, on
+* the golden fixtures made by the reference oracle (tests/golden/*.npz), and
+* seeded synthetic workloads at sizes the oracle finishes in seconds.
+"""
+import numpy as np
+import pytest
+
+import oracle
+from tests import _golden
+from tests._tol import (assert_cols, assert_loglike, COUNTS_RTOL, ROOTPROB_RTOL)
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+if not torch.cuda.is_available():  # pragma: no cover
+    pytest.skip("needs a CUDA GPU", allow_module_level=True)
+
+import subby_gb300 as sg  # noqa: E402
+from subby_gb300 import synth, models  # noqa: E402
+
+
+def _model_dict(m):
+    return {'eigenvalues': np.asarray(m.eigenvalues), 'eigenvectors': np.asarray(m.eigenvectors),
+            'pi': np.asarray(m.pi)}
+
+
+def _check_all(aln, tree, model, f81=False, masked=True, rp=True, bt64=None):
+    """Run every output through one plan and compare with the oracle."""
+    md = _model_dict(model)
+    otree = oracle.Tree(tree.parentIndex, tree.distanceToParent)
+    plan = sg.Plan(tree, model)
+    r = plan.run(aln, loglike=True, counts=True, rootprob=rp, branch_mask=None, bt64=bt64)
+    assert_loglike(r['logLike'], oracle.LogLike(aln, otree, md))
+    assert_cols(r['counts'], oracle.Counts(aln, otree, md, branch_mask=None), COUNTS_RTOL, "counts")
+    if rp:
+        assert_cols(r['rootProb'], oracle.RootProb(aln, otree, md), ROOTPROB_RTOL, "rootProb")
+    if masked:
+        rm = plan.run(aln, loglike=False, counts=True, branch_mask="auto", bt64=bt64)
+        assert_cols(rm['counts'], oracle.Counts(aln, otree, md), COUNTS_RTOL, "masked counts")
+    if f81:
+        rf = plan.run(aln, loglike=False, counts=True, f81=True, branch_mask=None)
+        assert_cols(rf['counts'], oracle.Counts(aln, otree, md, f81_fast=True, branch_mask=None),
+                    COUNTS_RTOL, "f81 counts")
+        if masked:
+            rfm = plan.run(aln, loglike=False, counts=True, f81=True, branch_mask="auto")
+            assert_cols(rfm['counts'], oracle.Counts(aln, otree, md, f81_fast=True), COUNTS_RTOL,
+                        "f81 masked counts")
+    plan.close()
+
+
+@pytest.mark.parametrize("name", _golden.names())
+def test_golden(name):
+    g = _golden.load(name)
+    tree = sg.Tree(g['parentIndex'], g['distanceToParent'])
+    model = sg.DiagModel(g['eigenvalues'], g['eigenvectors'], g['pi'])
+    plan = sg.Plan(tree, model)
+    r = plan.run(g['alignment'], loglike=True, counts=True, rootprob=True, branch_mask=None)
+    assert_loglike(r['logLike'], g['logLike'])
+    assert_cols(r['counts'], g['counts'], COUNTS_RTOL, "counts")
+    assert_cols(r['rootProb'], g['root_prob'], ROOTPROB_RTOL, "rootProb")
+    if 'counts_masked' in g:
+        rm = plan.run(g['alignment'], loglike=False, counts=True, branch_mask="auto")
+        assert_cols(rm['counts'], g['counts_masked'], COUNTS_RTOL, "masked counts")
+    if 'counts_f81' in g:
+        rf = plan.run(g['alignment'], loglike=False, counts=True, f81=True, branch_mask=None)
+        assert_cols(rf['counts'], g['counts_f81'], COUNTS_RTOL, "f81 counts")
+    if 'counts_f81_masked' in g:
+        rf = plan.run(g['alignment'], loglike=False, counts=True, f81=True, branch_mask="auto")
+        assert_cols(rf['counts'], g['counts_f81_masked'], COUNTS_RTOL, "f81 masked counts")
+    # the given-mask mode reproduces "auto" when handed the reference's own mask
+    if 'counts_masked' in g:
+        rg = plan.run(g['alignment'], loglike=False, counts=True, branch_mask=g['branch_mask'])
+        assert_cols(rg['counts'], g['counts_masked'], COUNTS_RTOL, "given-mask counts")
+    plan.close()
+
+
+def test_plain_small_full():
+    w = synth.plain_small(seed=1, C=1024)
+    _check_all(w['alignment'], w['tree'], w['model'])
+
+
+def test_plain_large_subset_hky_and_f81():
+    for f81 in (False, True):
+        w = synth.plain_large(seed=2, C=3000, f81=f81)
+        _check_all(w['alignment'], w['tree'], w['model'], f81=f81)
+
+
+@pytest.mark.parametrize("A,leaves,C", [(16, 12, 40), (20, 9, 33), (32, 6, 20), (64, 10, 24)])
+def test_reversible_larger_alphabets(A, leaves, C):
+    rng = np.random.default_rng(100 + A)
+    base, _, _ = models.random_reversible(A, rng)
+    m, _ = models.force_near_degenerate(base, rng)
+    tree = synth.random_tree(leaves, 0.1, rng)
+    aln = synth.simulated_alignment(tree, base, C, 0.1, rng)
+    _check_all(aln, tree, m)
+
+
+def test_precision64_subset():
+    w = synth.precision64(seed=3, C=48)
+    _check_all(w['alignment'], w['tree'], w['model'], masked=False)
+
+
+@pytest.mark.parametrize("A", [2, 3, 5, 8])
+def test_small_alphabets(A):
+    rng = np.random.default_rng(200 + A)
+    base, _, _ = models.random_reversible(A, rng)
+    tree = synth.random_tree(20, 0.2, rng)
+    aln = synth.simulated_alignment(tree, base, 77, 0.1, rng)
+    _check_all(aln, tree, base)
+
+
+def test_jc_and_f81_fast_paths_large_alphabet():
+    rng = np.random.default_rng(7)
+    tree = synth.random_tree(14, 0.1, rng)
+    for m in (models.jukes_cantor_model(64), models.f81_model(rng.dirichlet(np.ones(20)))):
+        aln = synth.simulated_alignment(tree, m, 19, 0.1, rng)
+        _check_all(aln, tree, m, f81=True)
+
+
+def test_edge_cases():
+    rng = np.random.default_rng(9)
+    m = models.hky85_diag(2.0, [0.3, 0.2, 0.25, 0.25])
+    # R = 1 (root only) and R = 3
+    for tree in (sg.Tree(np.array([-1], np.int32), np.array([0.0])),
+                 sg.Tree(np.array([-1, 0, 0], np.int32), np.array([0.0, 0.3, 0.05]))):
+        R = len(tree.parentIndex)
+        aln = rng.integers(-1, 6, size=(R, 37)).astype(np.int32)
+        _check_all(aln, tree, m)
+    # C = 1, C not a multiple of 32, all-gap columns, all-unobserved columns
+    tree = synth.random_tree(30, 0.1, rng)
+    for C in (1, 31, 33, 129):
+        aln = synth.simulated_alignment(tree, m, C, 0.2, rng)
+        aln[:, 0] = -1
+        _check_all(aln, tree, m)
+    # BFS-numbered balanced tree (not DFS order), as in the reference tests
+    R = 31
+    parent = np.array([-1] + [(i - 1) // 2 for i in range(1, R)], np.int32)
+    dist = rng.uniform(0.01, 0.5, R)
+    dist[0] = 0
+    tree = sg.Tree(parent, dist)
+    aln = rng.integers(-1, 5, size=(R, 50)).astype(np.int32)
+    _check_all(aln, tree, m)
+
+
+def test_device_pointer_path_matches_host_path():
+    w = synth.plain_large(seed=2, C=2048)
+    plan = sg.Plan(w['tree'], w['model'])
+    host = plan.run(w['alignment'], loglike=True, counts=True, rootprob=True)
+    dev = plan.run(torch.as_tensor(w['alignment']).cuda(), loglike=True, counts=True, rootprob=True)
+    torch.cuda.synchronize()
+    for k in host:
+        np.testing.assert_array_equal(dev[k].cpu().numpy(), host[k])
+
+
+def test_deterministic_repeat():
+    w = synth.plain_large(seed=2, C=4096)
+    plan = sg.Plan(w['tree'], w['model'])
+    a = plan.run(w['alignment'], counts=True, rootprob=True)
+    b = plan.run(w['alignment'], counts=True, rootprob=True)
+    for k in a:
+        np.testing.assert_array_equal(a[k], b[k])
+
+
+def test_subby_jax_style_api():
+    w = synth.plain_small(seed=1, C=256)
+    aln, tree, m = w['alignment'], w['tree'], w['model']
+    md = _model_dict(m)
+    otree = oracle.Tree(tree.parentIndex, tree.distanceToParent)
+    assert_loglike(sg.LogLike(aln, tree, m), oracle.LogLike(aln, otree, md))
+    assert_cols(sg.Counts(aln, tree, m), oracle.Counts(aln, otree, md), COUNTS_RTOL, "Counts")
+    assert_cols(sg.Counts(aln, tree, m, branch_mask=None),
+                oracle.Counts(aln, otree, md, branch_mask=None), COUNTS_RTOL, "Counts unmasked")
+    assert_cols(sg.RootProb(aln, tree, m), oracle.RootProb(aln, otree, md), ROOTPROB_RTOL, "RootProb")
+    # RateModel input is diagonalised on the host
+    Q = models.reversible_rate_matrix(np.zeros(6), m.pi)
+    rm = sg.RateModel(Q, m.pi)
+    dm = models.diagonalize_rate_matrix(Q, m.pi)
+    np.testing.assert_allclose(sg.LogLike(aln, tree, rm), sg.LogLike(aln, tree, dm), rtol=1e-6)
+
+
+def test_fp32_vs_fp64_back_transform_both_within_tolerance():
+    w = synth.plain_small(seed=1, C=512)
+    md = _model_dict(w['model'])
+    otree = oracle.Tree(w['tree'].parentIndex, w['tree'].distanceToParent)
+    ref = oracle.Counts(w['alignment'], otree, md, branch_mask=None)
+    plan = sg.Plan(w['tree'], w['model'])
+    for bt in (True, False):
+        r = plan.run(w['alignment'], loglike=False, counts=True, branch_mask=None, bt64=bt)
+        assert_cols(r['counts'], ref, COUNTS_RTOL, f"counts bt64={bt}")

@@ -113,30 +113,60 @@ def random_reversible(A: int, rng: np.random.Generator, exch_sigma: float = 1.0,
     return diagonalize_rate_matrix(Q, pi), log_exch, pi
 
 
-def force_near_degenerate(model: DiagModel, rng: np.random.Generator,
-                          target_fraction: float = 0.05, cluster: int = 5,
-                          lo: float = 1e-10, hi: float = 1e-7):
-    """Pull clusters of consecutive non-zero eigenvalues to within ``hi``.
+def near_degenerate_reversible(A: int, rng: np.random.Generator, target_fraction: float = 0.05,
+                               exch_sigma: float = 1.0, dirichlet_alpha: float = 1.0,
+                               split_max: float = 9e-8):
+    """Random reversible model with ~``target_fraction`` of its eigenvalue
+    pairs within ~1e-7 of each other, and M(t) >= 0 for every t.
 
-    Each cluster member gets eigenvalue base + delta with delta log-uniform in
-    [lo, hi] (the first member keeps delta = 0), so every pair inside a
-    cluster differs by less than ``hi``: the pairs straddle the 1e-8
-    degeneracy threshold of the J(t) integrals.  Eigenvectors are kept, so
-    M(t) rows still sum to one.  Returns (model, number of forced pairs).
+    s_ij ~ LogNormal(0, sigma), pi ~ Dirichlet(alpha), then a block B of d
+    states is made exchangeable (common pi inside B, one common within-block
+    exchangeability, and for every outside state k one common s_ik).  That
+    gives an exactly (d-1)-fold eigenvalue; d is the smallest size whose
+    (d-1)(d-2)/2 pairs reach the target.  The within-block exchangeabilities
+    are then multiplied by (1 + c eps_ij), eps ~ U(-1, 1), which splits the
+    degenerate eigenvalue into a cluster; c is chosen so that the widest pair
+    sits just under ``split_max`` and the pairwise gaps spread over
+    ~1e-10..1e-7 (straddling the 1e-8 degeneracy threshold of the J(t)
+    integrals).  Returns (DiagModel, log_exch, pi, forced_pairs).
     """
-    ev = np.array(model.eigenvalues, dtype=np.float64)
-    A = len(ev)
-    order = np.argsort(ev)
-    nz = [i for i in order if abs(ev[i]) > 1e-12]
-    need = int(np.ceil(target_fraction * A * (A - 1) / 2))
-    per = cluster * (cluster - 1) // 2
-    n_clusters = min(len(nz) // cluster, int(np.ceil(need / per)))
-    starts = np.sort(rng.choice(len(nz) // cluster, size=n_clusters, replace=False)) * cluster
-    pairs = 0
-    for s0 in starts:
-        idx = nz[s0:s0 + cluster]
-        base = ev[idx[0]]
-        for j, i in enumerate(idx):
-            ev[i] = base if j == 0 else base + np.exp(rng.uniform(np.log(lo), np.log(hi)))
-        pairs += per
-    return DiagModel(ev, np.array(model.eigenvectors), np.array(model.pi)), pairs
+    need = target_fraction * A * (A - 1) / 2
+    d = 3
+    while (d - 1) * (d - 2) / 2 < need and d < A:
+        d += 1
+    log_exch = rng.normal(0.0, exch_sigma, size=exchangeability_count(A))
+    pi = rng.dirichlet(np.full(A, dirichlet_alpha))
+    pi = np.maximum(pi, 1e-6)
+    pi /= pi.sum()
+    s = np.zeros((A, A))
+    iu = np.triu_indices(A, 1)
+    s[iu] = np.exp(log_exch)
+    s = s + s.T
+    B = np.sort(rng.choice(A, size=d, replace=False))
+    inB = np.zeros(A, dtype=bool)
+    inB[B] = True
+    pi[B] = pi[B].mean()
+    cin = np.exp(rng.normal(0.0, exch_sigma))
+    for k in np.nonzero(~inB)[0]:
+        s[B, k] = s[k, B] = s[B[0], k]
+    eps = rng.uniform(-1.0, 1.0, size=(d, d))
+
+    def build(scale):
+        ss = s.copy()
+        for a in range(d):
+            for b in range(a + 1, d):
+                ss[B[a], B[b]] = ss[B[b], B[a]] = cin * (1.0 + scale * eps[a, b])
+        le = np.log(ss[iu])
+        Q = reversible_rate_matrix(le, pi)
+        return diagonalize_rate_matrix(Q, pi), le
+
+    # eigenvalue splits are linear in the perturbation: scale it so that the
+    # widest pair of the cluster sits just under `split_max`
+    probe = 1e-4
+    m0, _ = build(probe)
+    ev = np.sort(m0.eigenvalues)
+    # the cluster is the run of d-1 eigenvalues with the smallest total spread
+    widths = np.array([ev[i + d - 2] - ev[i] for i in range(len(ev) - d + 2)])
+    w = widths.min()
+    model, log_exch = build(probe * split_max / max(w, 1e-300))
+    return model, log_exch, pi, (d - 1) * (d - 2) // 2

@@ -9,9 +9,10 @@ seed.  The recipes follow the five workload definitions of this backend:
                     tokens A and A+1, internal rows token A.
 * ``plain_large``   A=4 HKY85 and F81, 128 leaves (R=255), Exp(mean 0.05),
                     C=2^20 simulated down the tree, 10% gaps.
-* ``precision64``   A=64 random reversible (s~LogNormal(0,1), pi~Dir(1^64)),
-                    ~5% eigenvalue pairs forced within 1e-7, 64 leaves
-                    (R=127), Exp(mean 0.1), C=65536 simulated.
+* ``precision64``   A=64 random reversible (s~LogNormal(0,1), pi~Dir(1^64))
+                    with ~5% of the eigenvalue pairs within 1e-7 (an
+                    exchangeable block, see models.near_degenerate_reversible),
+                    64 leaves (R=127), Exp(mean 0.1), C=65536 simulated.
 * ``grad20``        A=20 random reversible (s~LogNormal(0,0.5),
                     pi~Dir(2^20)), 200 leaves (R=399), Exp(mean 0.08),
                     C=100000 simulated, 15% gaps.
@@ -164,10 +165,9 @@ def plain_large(seed: int = 2, C: int = 1 << 20, f81: bool = False):
 
 def precision64(seed: int = 3, C: int = 65536, A: int = 64, n_leaves: int = 64):
     rng = np.random.default_rng(seed)
-    base, log_exch, pi = _models.random_reversible(A, rng, 1.0, 1.0)
-    model, pairs = _models.force_near_degenerate(base, rng)
+    model, log_exch, pi, pairs = _models.near_degenerate_reversible(A, rng)
     tree = random_tree(n_leaves, 0.1, rng)
-    aln = simulated_alignment(tree, base, C, 0.0, rng)
+    aln = simulated_alignment(tree, model, C, 0.0, rng)
     return dict(name="precision64", alignment=aln, tree=tree, model=model, A=A, seed=seed,
                 forced_pairs=pairs, log_exch=log_exch, pi=pi)
 

@@ -132,10 +132,9 @@ def main():
     # random reversible A=16 and A=20 with near-degenerate eigenvalue pairs
     for A, L, C, seed in [(16, 8, 8, 15), (20, 6, 5, 16)]:
         rng = np.random.default_rng(seed)
-        base, _, _ = models.random_reversible(A, rng, 1.0, 1.0)
-        m, _ = models.force_near_degenerate(base, rng, target_fraction=0.08, cluster=3)
+        m, _, _, _ = models.near_degenerate_reversible(A, rng, target_fraction=0.08)
         tr = synth.random_tree(L, 0.1, rng)
-        aln = synth.simulated_alignment(tr, base, C, 0.1, rng)
+        aln = synth.simulated_alignment(tr, m, C, 0.1, rng)
         run_case(oracle, RTree, f"reversible_{A}", aln, tr.parentIndex, tr.distanceToParent,
                  m._asdict(), False)
 

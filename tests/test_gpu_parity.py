@@ -91,15 +91,18 @@ def test_plain_large_subset_hky_and_f81():
 @pytest.mark.parametrize("A,leaves,C", [(16, 12, 40), (20, 9, 33), (32, 6, 20), (64, 10, 24)])
 def test_reversible_larger_alphabets(A, leaves, C):
     rng = np.random.default_rng(100 + A)
-    base, _, _ = models.random_reversible(A, rng)
-    m, _ = models.force_near_degenerate(base, rng)
+    m, _, _, _ = models.near_degenerate_reversible(A, rng)
     tree = synth.random_tree(leaves, 0.1, rng)
-    aln = synth.simulated_alignment(tree, base, C, 0.1, rng)
+    aln = synth.simulated_alignment(tree, m, C, 0.1, rng)
     _check_all(aln, tree, m)
 
 
 def test_precision64_subset():
     w = synth.precision64(seed=3, C=48)
+    ev = np.sort(np.asarray(w['model'].eigenvalues))
+    gaps = np.abs(ev[:, None] - ev[None, :])[np.triu_indices(len(ev), 1)]
+    assert np.mean(gaps < 1e-7) >= 0.04          # ~5% near-degenerate pairs
+    assert np.any(gaps < 1e-8) and np.any((gaps > 1e-8) & (gaps < 1e-7))
     _check_all(w['alignment'], w['tree'], w['model'], masked=False)
 
 

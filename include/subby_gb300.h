@@ -138,6 +138,12 @@ int subby_rootprob(const int32_t *alignment, const int32_t *parent_index,
                    const double *eigenvectors, const double *pi,
                    int R, int C, int A, float *rootProb, int flags, void *stream);
 
+/* Test hook: 0 (default) runs alphabets A in {2,4,6,8} through the
+ * tree-program kernel, 1 routes them through the thread-per-column kernel
+ * instead, so both code paths can be checked against the oracle.  No
+ * reference counterpart. */
+int subby_debug_set_kernel(int which);
+
 /* Number of kernel launches the most recent subby_plan_run /
  * subby_plan_grad on this thread enqueued (for launch accounting). */
 int subby_last_launch_count(void);

@@ -22,6 +22,7 @@ EXPORTS = (
     "subby_version", "subby_strerror", "subby_last_error", "subby_plan_create",
     "subby_plan_destroy", "subby_plan_device_bytes", "subby_plan_run", "subby_plan_grad",
     "subby_loglike", "subby_counts", "subby_rootprob", "subby_last_launch_count",
+    "subby_debug_set_kernel",
 )
 
 _lock = threading.Lock()
@@ -51,6 +52,8 @@ def _declare(lib):
     lib.subby_strerror.argtypes = [ct.c_int]
     lib.subby_last_error.restype = ct.c_char_p
     lib.subby_last_launch_count.restype = ct.c_int
+    lib.subby_debug_set_kernel.restype = ct.c_int
+    lib.subby_debug_set_kernel.argtypes = [ct.c_int]
     lib.subby_plan_create.restype = ct.c_int
     lib.subby_plan_create.argtypes = [_p, _p, _p, _p, _p, ct.c_int, ct.c_int, ct.POINTER(ct.c_void_p)]
     lib.subby_plan_destroy.restype = ct.c_int

@@ -82,11 +82,19 @@ struct KParams {
   SmemTable stab[kMaxSmemTables];
   int smem_steps;         // sofs of steps (ints) in shared memory, -1 = read from global
   int smem_slots;
+  // tree-program kernel (k_tree.cu)
+  const int4 *prog;       // (nsteps, 4) int4
+  int nsteps;
+  int nslots;
+  int smem_words;         // sofs of the slot words (k_tree, shared-memory slots)
 };
 
 // launchers (k_small.cu / k_warp.cu)
 int launch_small(const KParams &p, int A, int grid, int block, size_t smem, cudaStream_t s);
 int launch_warp(const KParams &p, int A, int grid, int block, size_t smem, cudaStream_t s);
+int launch_tree(const KParams &p, int A, bool global_slots, int grid, int block, size_t smem,
+                cudaStream_t s);
+bool tree_supported(int A);
 bool small_supported(int A);
 bool warp_supported(int A);
 int small_block();

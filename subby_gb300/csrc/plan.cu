@@ -20,6 +20,9 @@ namespace {
 
 thread_local std::string g_last_error;
 thread_local int g_launches = 0;
+// Test hook: route small alphabets through the thread-per-column kernel
+// (k_small) instead of the tree program (set by subby_debug_set_kernel).
+int g_force_v1 = 0;
 
 int fail(int code, const std::string &msg) {
   g_last_error = msg;
@@ -103,6 +106,10 @@ struct subby_plan {
   int root_is_leaf = 0;
   std::vector<int4> steps, slots;
   int nslots = 0;
+  // tree program of k_tree (stored / derived node classification)
+  std::vector<int4> prog;
+  int prog_steps = 0, prog_slots = 0;
+  int4 *d_prog = nullptr;
   std::vector<double> V, mu, pi;
   float f81_mu = 0.f;
   TableOffsets off{};
@@ -159,6 +166,12 @@ const char *subby_strerror(int s) {
 }
 
 const char *subby_last_error(void) { return g_last_error.c_str(); }
+
+int subby_debug_set_kernel(int which) {
+  if (which < 0 || which > 1) return fail(SUBBY_ERR_ARG, "kernel selector must be 0 or 1");
+  g_force_v1 = which;
+  return SUBBY_OK;
+}
 int subby_last_launch_count(void) { return g_launches; }
 
 int subby_plan_create(const int32_t *parent, const double *dist, const double *evals,
@@ -223,6 +236,42 @@ int subby_plan_create(const int32_t *parent, const double *dist, const double *e
     if (v == 0) flags |= kRoot;
     P->steps.push_back(make_int4(v, l, r, flags));
     P->slots.push_back(make_int4(slot[v], slot[l], slot[r], 0));
+  }
+
+  // ---- tree program (k_tree): a node is DERIVED when both children are
+  // leaves or stored (its CC is recomputed from them), otherwise STORED.
+  {
+    std::vector<int> kind(R, -1);  // -1 leaf, -2 derived, -3 root, >= 0 slot
+    int nsl = 0;
+    for (int v : order) {          // postorder of internal nodes
+      if (v == 0) {
+        kind[v] = -3;
+        continue;
+      }
+      const bool ok = (kind[left[v]] == -1 || kind[left[v]] >= 0) &&
+                      (kind[right[v]] == -1 || kind[right[v]] >= 0);
+      kind[v] = ok ? -2 : nsl++;
+    }
+    for (int v : order) {
+      if (!(v == 0 || kind[v] >= 0)) continue;
+      int4 c[2];
+      int gk[4] = {0, 0, 0, 0};
+      for (int side = 0; side < 2; ++side) {
+        const int ch = side ? right[v] : left[v];
+        const int kl = left[ch], kr = right[ch];
+        c[side] = make_int4(ch, kind[ch], kl, kr);
+        if (kind[ch] == -2) {
+          gk[2 * side] = kind[kl];
+          gk[2 * side + 1] = kind[kr];
+        }
+      }
+      P->prog.push_back(make_int4(v, v == 0 ? -1 : kind[v], v == 0 ? 1 : 0, 0));
+      P->prog.push_back(c[0]);
+      P->prog.push_back(c[1]);
+      P->prog.push_back(make_int4(gk[0], gk[1], gk[2], gk[3]));
+    }
+    P->prog_steps = (int)P->prog.size() / 4;
+    P->prog_slots = nsl;
   }
 
   // ---- FP64 host tables
@@ -342,6 +391,12 @@ int subby_plan_create(const int32_t *parent, const double *dist, const double *e
       e = cudaMemcpy(P->d_slots, P->slots.data(), sizeof(int4) * P->nInt, cudaMemcpyHostToDevice);
     if (e != cudaSuccess) return cleanup(cuda_fail(e, "schedule upload"));
   }
+  if (P->prog_steps > 0) {
+    e = cudaMalloc(&P->d_prog, sizeof(int4) * P->prog.size());
+    if (e == cudaSuccess)
+      e = cudaMemcpy(P->d_prog, P->prog.data(), sizeof(int4) * P->prog.size(), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return cleanup(cuda_fail(e, "program upload"));
+  }
   {
     const int total = R * A * A;
     const int blk = 256, grd = std::max(1, std::min((total + blk - 1) / blk, 4096));
@@ -361,6 +416,7 @@ int subby_plan_destroy(subby_plan *P) {
   if (P->d_tab64) cudaFree(P->d_tab64);
   if (P->d_steps) cudaFree(P->d_steps);
   if (P->d_slots) cudaFree(P->d_slots);
+  if (P->d_prog) cudaFree(P->d_prog);
   P->work.release();
   P->io.release();
   delete P;
@@ -378,6 +434,8 @@ namespace {
 
 struct Launch {
   KParams kp{};
+  int kernel = 0;        // 0 small (thread/column), 1 warp/column, 2 tree program
+  bool global_slots = false;
   bool small = true;
   int grid = 1, block = 128;
   size_t smem = 0;
@@ -442,12 +500,69 @@ int plan_warp(subby_plan *P, int mode, int C, Launch &L) {
   return 0;
 }
 
+// Tree-program kernel: one CTA per SM, as many threads as the per-column slot
+// state allows in shared memory (global-memory slots when even 64 do not fit).
+int plan_tree(subby_plan *P, int mode, int C, Launch &L) {
+  const int A = P->A, R = P->R;
+  KParams &k = L.kp;
+  int ntab = 0, sofs = 0;
+  auto add = [&](int gofs, int n) {
+    k.stab[ntab++] = SmemTable{gofs, sofs, n};
+    sofs += (n + 3) & ~3;
+  };
+  const TableOffsets &o = P->off;
+  add(o.MT, R * (A + 1) * A);
+  add(o.Vu, A * A * 4 + (A + 1) * A + A);
+  if (mode & kModeCounts) {
+    if (mode & kModeF81) add(o.F81, R * 4);
+    else add(o.J, R * A * A);
+  }
+  k.ntab = ntab;
+  k.smem_steps = sofs;
+  sofs += 16 * P->prog_steps;
+  int maxsm = 0;
+  cudaDeviceGetAttribute(&maxsm, cudaDevAttrMaxSharedMemoryPerBlockOptin, P->device);
+  const size_t fixed = (size_t)sofs * sizeof(float);
+  const size_t per_thread = (size_t)P->prog_slots * (A + 1) * sizeof(float);
+  if (fixed + 1024 > (size_t)maxsm)
+    return fail(SUBBY_ERR_UNSUPPORTED, "tree too large for the shared-memory tables (R=" +
+                                           std::to_string(R) + ", A=" + std::to_string(A) + ")");
+  const int kMaxThreads = 384;
+  int threads = kMaxThreads;
+  if (per_thread > 0) threads = (int)(((size_t)maxsm - fixed) / per_thread);
+  threads = std::min(kMaxThreads, threads / 32 * 32);
+  L.kernel = 2;
+  L.small = false;
+  if (threads >= 64) {
+    L.global_slots = false;
+    L.block = threads;
+    k.smem_slots = sofs;
+    sofs += P->prog_slots * threads * A;
+    k.smem_words = sofs;
+    sofs += P->prog_slots * threads;
+  } else {
+    L.global_slots = true;
+    L.block = 256;
+    k.smem_slots = -1;
+    k.smem_words = -1;
+  }
+  L.smem = (size_t)sofs * sizeof(float);
+  const int want = (C + L.block - 1) / L.block;
+  L.grid = std::max(1, std::min(want, P->nsm));
+  L.nworkers = L.grid * L.block;
+  k.prog = P->d_prog;
+  k.nsteps = P->prog_steps;
+  k.nslots = P->prog_slots;
+  return 0;
+}
+
 int run_common(subby_plan *P, const int32_t *d_aln, int C, float *d_logL, float *d_counts,
                float *d_root, int mode, int mask_mode, const uint8_t *d_mask, const float *d_g,
                double *d_gt, double *d_gC, int *grid_out, cudaStream_t stream) {
   Launch L;
+  const bool tree = tree_supported(P->A) && !(mode & kModeGrad) && !g_force_v1;
   const bool small = small_supported(P->A);
-  int rc = small ? plan_small(P, mode, C, L) : plan_warp(P, mode, C, L);
+  int rc = tree ? plan_tree(P, mode, C, L) : small ? plan_small(P, mode, C, L) : plan_warp(P, mode, C, L);
   if (rc) return rc;
   KParams &k = L.kp;
   k.aln = d_aln;
@@ -473,16 +588,17 @@ int run_common(subby_plan *P, const int32_t *d_aln, int C, float *d_logL, float 
   k.grad_t = d_gt;
   k.grad_C = d_gC;
   // scratch
-  const size_t nsl = (size_t)std::max(P->nslots, 1);
-  const size_t vbytes = nsl * L.nworkers * P->A * sizeof(float);
-  const size_t wbytes = nsl * L.nworkers * 2 * sizeof(int);
+  const size_t nsl = (size_t)std::max(tree ? P->prog_slots : P->nslots, 1);
+  const size_t vbytes = (tree && !L.global_slots) ? 0 : nsl * L.nworkers * P->A * sizeof(float);
+  const size_t wbytes = (tree && !L.global_slots) ? 0 : nsl * L.nworkers * 2 * sizeof(int);
   const size_t vb_al = (vbytes + 255) & ~(size_t)255;
-  if ((rc = P->work.grow(vb_al + wbytes))) return rc;
+  if ((rc = P->work.grow(vb_al + wbytes + 256))) return rc;
   k.scrV = (float *)P->work.p;
   k.scrW = (int *)((char *)P->work.p + vb_al);
   if (grid_out) *grid_out = L.grid;
-  int lr = small ? launch_small(k, P->A, L.grid, L.block, L.smem, stream)
-                 : launch_warp(k, P->A, L.grid, L.block, L.smem, stream);
+  int lr = tree ? launch_tree(k, P->A, L.global_slots, L.grid, L.block, L.smem, stream)
+           : small ? launch_small(k, P->A, L.grid, L.block, L.smem, stream)
+                   : launch_warp(k, P->A, L.grid, L.block, L.smem, stream);
   if (lr != 0) return fail(SUBBY_ERR_CUDA, std::string("kernel launch failed: ") +
                                                cudaGetErrorString((cudaError_t)lr));
   g_launches += 1;

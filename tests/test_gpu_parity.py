@@ -19,7 +19,15 @@ if not torch.cuda.is_available():  # pragma: no cover
     pytest.skip("needs a CUDA GPU", allow_module_level=True)
 
 import subby_gb300 as sg  # noqa: E402
-from subby_gb300 import synth, models  # noqa: E402
+from subby_gb300 import synth, models, _lib  # noqa: E402
+
+
+@pytest.fixture(params=["tree", "thread"])
+def kernel(request):
+    """Run a test through the tree-program kernel and the thread-per-column kernel."""
+    _lib.load().subby_debug_set_kernel(1 if request.param == "thread" else 0)
+    yield request.param
+    _lib.load().subby_debug_set_kernel(0)
 
 
 def _model_dict(m):
@@ -52,7 +60,7 @@ def _check_all(aln, tree, model, f81=False, masked=True, rp=True, bt64=None):
 
 
 @pytest.mark.parametrize("name", _golden.names())
-def test_golden(name):
+def test_golden(name, kernel):
     g = _golden.load(name)
     tree = sg.Tree(g['parentIndex'], g['distanceToParent'])
     model = sg.DiagModel(g['eigenvalues'], g['eigenvectors'], g['pi'])
@@ -77,12 +85,12 @@ def test_golden(name):
     plan.close()
 
 
-def test_plain_small_full():
+def test_plain_small_full(kernel):
     w = synth.plain_small(seed=1, C=1024)
     _check_all(w['alignment'], w['tree'], w['model'])
 
 
-def test_plain_large_subset_hky_and_f81():
+def test_plain_large_subset_hky_and_f81(kernel):
     for f81 in (False, True):
         w = synth.plain_large(seed=2, C=3000, f81=f81)
         _check_all(w['alignment'], w['tree'], w['model'], f81=f81)
@@ -106,8 +114,8 @@ def test_precision64_subset():
     _check_all(w['alignment'], w['tree'], w['model'], masked=False)
 
 
-@pytest.mark.parametrize("A", [2, 3, 5, 8])
-def test_small_alphabets(A):
+@pytest.mark.parametrize("A", [2, 3, 4, 5, 6, 8])
+def test_small_alphabets(A, kernel):
     rng = np.random.default_rng(200 + A)
     base, _, _ = models.random_reversible(A, rng)
     tree = synth.random_tree(20, 0.2, rng)
@@ -123,7 +131,7 @@ def test_jc_and_f81_fast_paths_large_alphabet():
         _check_all(aln, tree, m, f81=True)
 
 
-def test_edge_cases():
+def test_edge_cases(kernel):
     rng = np.random.default_rng(9)
     m = models.hky85_diag(2.0, [0.3, 0.2, 0.25, 0.25])
     # R = 1 (root only) and R = 3

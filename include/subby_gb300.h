@@ -138,10 +138,11 @@ int subby_rootprob(const int32_t *alignment, const int32_t *parent_index,
                    const double *eigenvectors, const double *pi,
                    int R, int C, int A, float *rootProb, int flags, void *stream);
 
-/* Test hook: 0 (default) runs alphabets A in {2,4,6,8} through the
- * tree-program kernel, 1 routes them through the thread-per-column kernel
- * instead, so both code paths can be checked against the oracle.  No
- * reference counterpart. */
+/* Test hook selecting the kernel for alphabets A <= 8 so that every code
+ * path can be checked against the oracle: 0 automatic (tree program, slot
+ * vectors in tensor memory when A = 4 and they fit), 1 thread-per-column
+ * kernel, 2 tree program with shared-memory slots, 3 tree program with
+ * global-memory slots.  No reference counterpart. */
 int subby_debug_set_kernel(int which);
 
 /* Number of kernel launches the most recent subby_plan_run /

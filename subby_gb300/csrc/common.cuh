@@ -92,7 +92,8 @@ struct KParams {
 // launchers (k_small.cu / k_warp.cu)
 int launch_small(const KParams &p, int A, int grid, int block, size_t smem, cudaStream_t s);
 int launch_warp(const KParams &p, int A, int grid, int block, size_t smem, cudaStream_t s);
-int launch_tree(const KParams &p, int A, bool global_slots, int grid, int block, size_t smem,
+// store: 0 shared-memory slots, 1 global-memory slots, 2 tensor-memory slots (A = 4)
+int launch_tree(const KParams &p, int A, int store, int grid, int block, size_t smem,
                 cudaStream_t s);
 bool tree_supported(int A);
 bool small_supported(int A);

@@ -181,43 +181,86 @@ struct Derived {
   Node<A> k[2]; // its children (leaves or stored)
 };
 
-template <int A, bool G>
+// Where the per-column slot vectors live.
+enum : int { kStSmem = 0, kStGlobal = 1, kStTmem = 2 };
+
+// Tensor memory as per-thread scratch: with the 32x32b access shape each
+// thread of a warp owns one TMEM lane (lanes 32*(warp%4) ..), and warps
+// w and w+4 use disjoint column halves.  Every access is warp-uniform.
+__device__ __forceinline__ void tm_st4(uint32_t ta, float a, float b, float c, float d) {
+  asm volatile("tcgen05.st.sync.aligned.32x32b.x4.b32 [%0], {%1, %2, %3, %4};" ::"r"(ta),
+               "r"(__float_as_uint(a)), "r"(__float_as_uint(b)), "r"(__float_as_uint(c)),
+               "r"(__float_as_uint(d))
+               : "memory");
+}
+__device__ __forceinline__ void tm_ld4(uint32_t ta, float &a, float &b, float &c, float &d) {
+  uint32_t x, y, z, w;
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x4.b32 {%0, %1, %2, %3}, [%4];"
+               : "=r"(x), "=r"(y), "=r"(z), "=r"(w)
+               : "r"(ta)
+               : "memory");
+  asm volatile("tcgen05.wait::ld.sync.aligned;" : "+r"(x), "+r"(y), "+r"(z), "+r"(w)::"memory");
+  a = __uint_as_float(x);
+  b = __uint_as_float(y);
+  c = __uint_as_float(z);
+  d = __uint_as_float(w);
+}
+__device__ __forceinline__ void tm_wait_st() { asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory"); }
+
+template <int A, int ST>
 struct Ctx {
   const int32_t *alnc;
   int C;
   const float *MT;
-  float *svec;   // this thread's slot 0 vector
+  float *svec;   // this thread's slot 0 vector (shared or global memory)
+  uint32_t tb;   // this thread's slot 0 vector (tensor memory address)
   int *sword;    // this thread's slot 0 word
   int vstride;   // floats between consecutive slots of one thread
   int wstride;   // ints between consecutive slots of one thread
 
+  __device__ __forceinline__ void vload(V<A> &o, int slot) const {
+    if constexpr (ST == kStTmem) {
+      static_assert(A == 4, "tensor-memory slots hold 4 states");
+      tm_ld4(tb + 4 * slot, o.p[0].x, o.p[0].y, o.p[1].x, o.p[1].y);
+    } else {
+      vld<A>(o, svec + slot * vstride);
+    }
+  }
+  __device__ __forceinline__ void vstore(int slot, const V<A> &v) const {
+    if constexpr (ST == kStTmem) {
+      tm_st4(tb + 4 * slot, v.p[0].x, v.p[0].y, v.p[1].x, v.p[1].y);
+    } else {
+      vst<A>(svec + slot * vstride, v);
+    }
+  }
+
   __device__ __forceinline__ int tok(int n) const { return __ldg(alnc + (size_t)n * C); }
 
-  __device__ __forceinline__ void leaf(Node<A> &o, int n) const {
-    const int t = tok(n);
+  __device__ __forceinline__ void leaf(Node<A> &o, int n, int t) const {
     o.code = tcode(t, A);
     vld<A>(o.cc, MT + (n * (A + 1) + o.code) * A);
     o.e = 0;
     o.h = o.init = tungapped(t, A);
   }
   __device__ __forceinline__ void stored(Node<A> &o, int slot) const {
-    vld<A>(o.cc, svec + slot * vstride);
+    vload(o.cc, slot);
     const int w = sword[slot * wstride];
     o.e = w >> 2;
     o.h = (w >> 1) & 1;
     o.init = w & 1;
     o.code = -1;
   }
-  __device__ __forceinline__ void basic(Node<A> &o, int n, int ks) const {
-    if (ks < 0) leaf(o, n);
+  __device__ __forceinline__ void basic(Node<A> &o, int n, int ks, int t) const {
+    if (ks < 0) leaf(o, n, t);
     else stored(o, ks);
   }
-  // Recompute a derived node n from its children (leaves or stored).
+  // Recompute a derived node n from its children (leaves or stored); t, tl,
+  // tr are the tokens of n and of its two children.
   __device__ __forceinline__ void derive(Node<A> &o, Derived<A> &d, int n, int nl, int nr, int ksl,
-                                         int ksr) const {
-    basic(d.k[0], nl, ksl);
-    basic(d.k[1], nr, ksr);
-    d.codec = tcode(tok(n), A);
+                                         int ksr, int t, int tl, int tr) const {
+    basic(d.k[0], nl, ksl, tl);
+    basic(d.k[1], nr, ksr, tr);
+    d.codec = tcode(t, A);
     vmul<A>(d.u, d.k[0].cc, d.k[1].cc);
     vobs<A>(d.u, d.codec);
     o.e = d.k[0].e + d.k[1].e + vrescale<A>(d.u);
@@ -227,10 +270,22 @@ struct Ctx {
     vmat<A>(o.cc, d.u, MT + n * (A + 1) * A);
   }
   __device__ __forceinline__ void put(int slot, const V<A> &v, int w) const {
-    vst<A>(svec + slot * vstride, v);
+    vstore(slot, v);
     sword[slot * wstride] = w;
   }
 };
+
+// Tokens one program step reads: p, l, r and the children of l and r
+// (used when l / r is derived).  Loaded one step ahead of their use.
+struct Tok7 {
+  int t[7];
+};
+
+__device__ __forceinline__ void load_tok7(Tok7 &o, const int32_t *alnc, int C, int4 s0, int4 s1, int4 s2) {
+  const int n[7] = {s0.x, s1.x, s2.x, max(s1.z, 0), max(s1.w, 0), max(s2.z, 0), max(s2.w, 0)};
+#pragma unroll
+  for (int i = 0; i < 7; ++i) o.t[i] = __ldg(alnc + (size_t)n[i] * C);
+}
 
 template <int A>
 struct Acc {
@@ -249,8 +304,8 @@ struct Acc {
   }
 };
 
-template <int A, bool G>
-__global__ void __launch_bounds__(384, 1) k_tree(const KParams P) {
+template <int A, int ST>
+__global__ void __launch_bounds__(256, 1) k_tree(const KParams P) {
   extern __shared__ __align__(16) float sm[];
   for (int t = 0; t < P.ntab; ++t) {
     const SmemTable tb = P.stab[t];
@@ -279,19 +334,39 @@ __global__ void __launch_bounds__(384, 1) k_tree(const KParams P) {
   const bool counts = (P.mode & kModeCounts) != 0;
   const bool f81 = (P.mode & kModeF81) != 0;
 
-  Ctx<A, G> cx;
+  Ctx<A, ST> cx;
   cx.C = C;
   cx.MT = MT;
-  if (G) {
+  cx.tb = 0;
+  cx.svec = nullptr;
+  if (ST == kStGlobal) {
     const size_t per_cta = (size_t)P.nslots * nb;
     cx.svec = P.scrV + ((size_t)blockIdx.x * per_cta + threadIdx.x) * A;
     cx.sword = P.scrW + (size_t)blockIdx.x * per_cta + threadIdx.x;
   } else {
-    cx.svec = sm + P.smem_slots + threadIdx.x * A;
+    if (ST == kStSmem) cx.svec = sm + P.smem_slots + threadIdx.x * A;
     cx.sword = reinterpret_cast<int *>(sm + P.smem_words) + threadIdx.x;
   }
   cx.vstride = nb * A;
   cx.wstride = nb;
+  uint32_t tmem_base = 0;
+  if constexpr (ST == kStTmem) {
+    // One CTA per SM owns all 512 TMEM columns (blockDim 128 or 256).
+    __shared__ uint32_t s_taddr;
+    const int warp = threadIdx.x >> 5;
+    if (warp == 0) {
+      const uint32_t dst = (uint32_t)__cvta_generic_to_shared(&s_taddr);
+      asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(dst), "r"(512)
+                   : "memory");
+      asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    tmem_base = s_taddr;
+    const uint32_t cols_per_thread = 512u / (uint32_t)(nb >> 7);
+    cx.tb = tmem_base + (((uint32_t)(warp & 3) * 32u) << 16) + (uint32_t)(warp >> 2) * cols_per_thread;
+  }
 
   V<A> piv;
   vld<A>(piv, pi);
@@ -300,24 +375,34 @@ __global__ void __launch_bounds__(384, 1) k_tree(const KParams P) {
     const bool valid = c0 + lane < C;
     const int col = valid ? c0 + lane : C - 1;
     cx.alnc = P.aln + col;
+    {
+      // Pull this thread's next column into L2 while this one is processed.
+      const int nxt = c0 + stride + lane;
+      if (nxt < C)
+        for (int n = 0; n < P.R; ++n) asm volatile("prefetch.global.L2 [%0];" ::"l"(P.aln + (size_t)n * C + nxt));
+    }
     // ---------------------------------------------------------------- inside
     V<A> ur;
     int eRoot = 0, iRoot = 0;
     if (P.root_is_leaf) {
       vfill<A>(ur, 1.f);
-      vobs<A>(ur, tcode(cx.tok(0), A));
+      vobs<A>(ur, tcode(__ldg(cx.alnc), A));
     }
+    Tok7 tk, tn;
+    if (P.nsteps > 0) load_tok7(tk, cx.alnc, C, prog[0], prog[1], prog[2]);
     for (int i = 0; i < P.nsteps; ++i) {
       const int4 s0 = prog[4 * i], s1 = prog[4 * i + 1], s2 = prog[4 * i + 2], s3 = prog[4 * i + 3];
+      if (i + 1 < P.nsteps) load_tok7(tn, cx.alnc, C, prog[4 * i + 4], prog[4 * i + 5], prog[4 * i + 6]);
+      if constexpr (ST == kStTmem) tm_wait_st();
       Node<A> nl, nr;
       Derived<A> dl, dr;
-      if (s1.y == -2) cx.derive(nl, dl, s1.x, s1.z, s1.w, s3.x, s3.y);
-      else cx.basic(nl, s1.x, s1.y);
-      if (s2.y == -2) cx.derive(nr, dr, s2.x, s2.z, s2.w, s3.z, s3.w);
-      else cx.basic(nr, s2.x, s2.y);
+      if (s1.y == -2) cx.derive(nl, dl, s1.x, s1.z, s1.w, s3.x, s3.y, tk.t[1], tk.t[3], tk.t[4]);
+      else cx.basic(nl, s1.x, s1.y, tk.t[1]);
+      if (s2.y == -2) cx.derive(nr, dr, s2.x, s2.z, s2.w, s3.z, s3.w, tk.t[2], tk.t[5], tk.t[6]);
+      else cx.basic(nr, s2.x, s2.y, tk.t[2]);
       V<A> u;
       vmul<A>(u, nl.cc, nr.cc);
-      vobs<A>(u, tcode(cx.tok(s0.x), A));
+      vobs<A>(u, tcode(tk.t[0], A));
       const int eU = nl.e + nr.e + vrescale<A>(u);
       const int h = nl.h | nr.h, init = nl.h & nr.h;
       if (s0.z) {
@@ -329,6 +414,7 @@ __global__ void __launch_bounds__(384, 1) k_tree(const KParams P) {
         vmat<A>(cc, u, MT + s0.x * (A + 1) * A);
         cx.put(s0.y, cc, (eU << 2) | (h << 1) | init);
       }
+      tk = tn;
     }
     float Pp = 0.f;
 #pragma unroll
@@ -407,15 +493,21 @@ __global__ void __launch_bounds__(384, 1) k_tree(const KParams P) {
       return vrescale<A>(O);
     };
 
+    {
+      const int j = P.nsteps - 1;
+      load_tok7(tk, cx.alnc, C, prog[4 * j], prog[4 * j + 1], prog[4 * j + 2]);
+    }
     for (int i = P.nsteps - 1; i >= 0; --i) {
       const int4 s0 = prog[4 * i], s1 = prog[4 * i + 1], s2 = prog[4 * i + 2], s3 = prog[4 * i + 3];
+      if (i > 0) load_tok7(tn, cx.alnc, C, prog[4 * i - 4], prog[4 * i - 3], prog[4 * i - 2]);
+      if constexpr (ST == kStTmem) tm_wait_st();
       Node<A> nl, nr;
       Derived<A> dl, dr;
-      if (s1.y == -2) cx.derive(nl, dl, s1.x, s1.z, s1.w, s3.x, s3.y);
-      else cx.basic(nl, s1.x, s1.y);
-      if (s2.y == -2) cx.derive(nr, dr, s2.x, s2.z, s2.w, s3.z, s3.w);
-      else cx.basic(nr, s2.x, s2.y);
-      const int codep = tcode(cx.tok(s0.x), A);
+      if (s1.y == -2) cx.derive(nl, dl, s1.x, s1.z, s1.w, s3.x, s3.y, tk.t[1], tk.t[3], tk.t[4]);
+      else cx.basic(nl, s1.x, s1.y, tk.t[1]);
+      if (s2.y == -2) cx.derive(nr, dr, s2.x, s2.z, s2.w, s3.z, s3.w, tk.t[2], tk.t[5], tk.t[6]);
+      else cx.basic(nr, s2.x, s2.y, tk.t[2]);
+      const int codep = tcode(tk.t[0], A);
       V<A> O;
       int eO, stp;
       if (s0.z) {
@@ -425,7 +517,7 @@ __global__ void __launch_bounds__(384, 1) k_tree(const KParams P) {
         stp = iRoot;
       } else {
         V<A> D;
-        vld<A>(D, cx.svec + s0.y * cx.vstride);
+        cx.vload(D, s0.y);
         const int wd = cx.sword[s0.y * cx.wstride];
         const int eD = wd >> 2;
         stp = (wd >> 1) & 1;
@@ -482,6 +574,7 @@ __global__ void __launch_bounds__(384, 1) k_tree(const KParams P) {
           }
         }
       }
+      tk = tn;
     }
     // ---------------------------------------------------------------- epilogue
     if (!valid) continue;
@@ -547,14 +640,23 @@ __global__ void __launch_bounds__(384, 1) k_tree(const KParams P) {
         }
     }
   }
+  if constexpr (ST == kStTmem) {
+    tm_wait_st();
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    if ((threadIdx.x >> 5) == 0)
+      asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem_base), "r"(512)
+                   : "memory");
+  }
 }
 
-template <int A, bool G>
+template <int A, int ST>
 int tlaunch(const KParams &p, int grid, int block, size_t smem, cudaStream_t s) {
-  cudaError_t e = cudaFuncSetAttribute(k_tree<A, G>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  cudaError_t e = cudaFuncSetAttribute(k_tree<A, ST>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)smem);
   if (e != cudaSuccess) return (int)e;
-  k_tree<A, G><<<grid, block, smem, s>>>(p);
+  k_tree<A, ST><<<grid, block, smem, s>>>(p);
   return (int)cudaGetLastError();
 }
 
@@ -562,13 +664,18 @@ int tlaunch(const KParams &p, int grid, int block, size_t smem, cudaStream_t s) 
 
 bool tree_supported(int A) { return A == 2 || A == 4 || A == 6 || A == 8; }
 
-int launch_tree(const KParams &p, int A, bool global_slots, int grid, int block, size_t smem,
+int launch_tree(const KParams &p, int A, int store, int grid, int block, size_t smem,
                 cudaStream_t s) {
+  if (store == kStTmem) {
+    if (A != 4) return -1;
+    return tlaunch<4, kStTmem>(p, grid, block, smem, s);
+  }
+  const bool g = store == kStGlobal;
   switch (A) {
-    case 2: return global_slots ? tlaunch<2, true>(p, grid, block, smem, s) : tlaunch<2, false>(p, grid, block, smem, s);
-    case 4: return global_slots ? tlaunch<4, true>(p, grid, block, smem, s) : tlaunch<4, false>(p, grid, block, smem, s);
-    case 6: return global_slots ? tlaunch<6, true>(p, grid, block, smem, s) : tlaunch<6, false>(p, grid, block, smem, s);
-    case 8: return global_slots ? tlaunch<8, true>(p, grid, block, smem, s) : tlaunch<8, false>(p, grid, block, smem, s);
+    case 2: return g ? tlaunch<2, kStGlobal>(p, grid, block, smem, s) : tlaunch<2, kStSmem>(p, grid, block, smem, s);
+    case 4: return g ? tlaunch<4, kStGlobal>(p, grid, block, smem, s) : tlaunch<4, kStSmem>(p, grid, block, smem, s);
+    case 6: return g ? tlaunch<6, kStGlobal>(p, grid, block, smem, s) : tlaunch<6, kStSmem>(p, grid, block, smem, s);
+    case 8: return g ? tlaunch<8, kStGlobal>(p, grid, block, smem, s) : tlaunch<8, kStSmem>(p, grid, block, smem, s);
     default: return -1;
   }
 }

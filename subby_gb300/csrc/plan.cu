@@ -20,9 +20,10 @@ namespace {
 
 thread_local std::string g_last_error;
 thread_local int g_launches = 0;
-// Test hook: route small alphabets through the thread-per-column kernel
-// (k_small) instead of the tree program (set by subby_debug_set_kernel).
-int g_force_v1 = 0;
+// Test hook (subby_debug_set_kernel): 0 automatic, 1 thread-per-column
+// kernel (k_small) for A <= 8, 2 tree program with shared-memory slots,
+// 3 tree program with global-memory slots.
+int g_kernel_sel = 0;
 
 int fail(int code, const std::string &msg) {
   g_last_error = msg;
@@ -168,8 +169,8 @@ const char *subby_strerror(int s) {
 const char *subby_last_error(void) { return g_last_error.c_str(); }
 
 int subby_debug_set_kernel(int which) {
-  if (which < 0 || which > 1) return fail(SUBBY_ERR_ARG, "kernel selector must be 0 or 1");
-  g_force_v1 = which;
+  if (which < 0 || which > 3) return fail(SUBBY_ERR_ARG, "kernel selector must be 0..3");
+  g_kernel_sel = which;
   return SUBBY_OK;
 }
 int subby_last_launch_count(void) { return g_launches; }
@@ -436,6 +437,7 @@ struct Launch {
   KParams kp{};
   int kernel = 0;        // 0 small (thread/column), 1 warp/column, 2 tree program
   bool global_slots = false;
+  int store = 0;         // k_tree slot storage: 0 shared, 1 global, 2 tensor memory
   bool small = true;
   int grid = 1, block = 128;
   size_t smem = 0;
@@ -527,25 +529,48 @@ int plan_tree(subby_plan *P, int mode, int C, Launch &L) {
   if (fixed + 1024 > (size_t)maxsm)
     return fail(SUBBY_ERR_UNSUPPORTED, "tree too large for the shared-memory tables (R=" +
                                            std::to_string(R) + ", A=" + std::to_string(A) + ")");
-  const int kMaxThreads = 384;
+  const int kMaxThreads = 256;
   int threads = kMaxThreads;
   if (per_thread > 0) threads = (int)(((size_t)maxsm - fixed) / per_thread);
   threads = std::min(kMaxThreads, threads / 32 * 32);
   L.kernel = 2;
   L.small = false;
-  if (threads >= 64) {
-    L.global_slots = false;
+  // Tensor memory holds the slot vectors when A = 4 and they fit (512
+  // columns per SM shared by 128 or 256 threads); the slot words stay in
+  // shared memory.  Otherwise shared-memory slots, else global-memory slots.
+  int tm_threads = 0;
+  if (A == 4 && P->prog_slots > 0 && g_kernel_sel != 2 && g_kernel_sel != 3) {
+    for (int t : {256, 128}) {
+      if (P->prog_slots * 4 <= 512 / (t / 128) &&
+          fixed + (size_t)P->prog_slots * t * sizeof(int) + 1024 <= (size_t)maxsm) {
+        tm_threads = t;
+        break;
+      }
+    }
+  }
+  if (tm_threads) {
+    L.store = 2;
+    L.block = tm_threads;
+    k.smem_slots = -1;
+    k.smem_words = sofs;
+    sofs += P->prog_slots * tm_threads;
+    // at least half of the SM's shared memory, so that exactly one CTA (the
+    // owner of all 512 TMEM columns) is resident per SM
+    sofs = std::max(sofs, (maxsm / 2 + 4096) / 4);
+  } else if (threads >= 64 && g_kernel_sel != 3) {
+    L.store = 0;
     L.block = threads;
     k.smem_slots = sofs;
     sofs += P->prog_slots * threads * A;
     k.smem_words = sofs;
     sofs += P->prog_slots * threads;
   } else {
-    L.global_slots = true;
+    L.store = 1;
     L.block = 256;
     k.smem_slots = -1;
     k.smem_words = -1;
   }
+  L.global_slots = (L.store == 1);
   L.smem = (size_t)sofs * sizeof(float);
   const int want = (C + L.block - 1) / L.block;
   L.grid = std::max(1, std::min(want, P->nsm));
@@ -560,7 +585,7 @@ int run_common(subby_plan *P, const int32_t *d_aln, int C, float *d_logL, float 
                float *d_root, int mode, int mask_mode, const uint8_t *d_mask, const float *d_g,
                double *d_gt, double *d_gC, int *grid_out, cudaStream_t stream) {
   Launch L;
-  const bool tree = tree_supported(P->A) && !(mode & kModeGrad) && !g_force_v1;
+  const bool tree = tree_supported(P->A) && !(mode & kModeGrad) && g_kernel_sel != 1;
   const bool small = small_supported(P->A);
   int rc = tree ? plan_tree(P, mode, C, L) : small ? plan_small(P, mode, C, L) : plan_warp(P, mode, C, L);
   if (rc) return rc;
@@ -596,7 +621,7 @@ int run_common(subby_plan *P, const int32_t *d_aln, int C, float *d_logL, float 
   k.scrV = (float *)P->work.p;
   k.scrW = (int *)((char *)P->work.p + vb_al);
   if (grid_out) *grid_out = L.grid;
-  int lr = tree ? launch_tree(k, P->A, L.global_slots, L.grid, L.block, L.smem, stream)
+  int lr = tree ? launch_tree(k, P->A, L.store, L.grid, L.block, L.smem, stream)
            : small ? launch_small(k, P->A, L.grid, L.block, L.smem, stream)
                    : launch_warp(k, P->A, L.grid, L.block, L.smem, stream);
   if (lr != 0) return fail(SUBBY_ERR_CUDA, std::string("kernel launch failed: ") +

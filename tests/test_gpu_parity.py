@@ -22,10 +22,13 @@ import subby_gb300 as sg  # noqa: E402
 from subby_gb300 import synth, models, _lib  # noqa: E402
 
 
-@pytest.fixture(params=["tree", "thread"])
+KERNELS = {"auto": 0, "thread": 1, "tree_smem": 2, "tree_global": 3}
+
+
+@pytest.fixture(params=list(KERNELS))
 def kernel(request):
-    """Run a test through the tree-program kernel and the thread-per-column kernel."""
-    _lib.load().subby_debug_set_kernel(1 if request.param == "thread" else 0)
+    """Run a test through every kernel / slot-storage variant for A <= 8."""
+    _lib.load().subby_debug_set_kernel(KERNELS[request.param])
     yield request.param
     _lib.load().subby_debug_set_kernel(0)
 

@@ -139,10 +139,11 @@ int subby_rootprob(const int32_t *alignment, const int32_t *parent_index,
                    int R, int C, int A, float *rootProb, int flags, void *stream);
 
 /* Test hook selecting the kernel for alphabets A <= 8 so that every code
- * path can be checked against the oracle: 0 automatic (tree program, slot
- * vectors in tensor memory when A = 4 and they fit), 1 thread-per-column
- * kernel, 2 tree program with shared-memory slots, 3 tree program with
- * global-memory slots.  No reference counterpart. */
+ * path can be checked against the oracle: 0 automatic (A = 4 tree kernel
+ * with tensor-memory slots when it fits), 1 thread-per-column kernel, 2
+ * tree program with shared-memory slots, 3 tree program with global-memory
+ * slots, 4 generic tree program with tensor-memory slots.  No reference
+ * counterpart. */
 int subby_debug_set_kernel(int which);
 
 /* Number of kernel launches the most recent subby_plan_run /

@@ -40,6 +40,7 @@ struct TableOffsets {
   int V;     // A x A         : V[i][k] (FP32 copy)
   int S;     // A x A         : S[i][j] = sum_k V_ik mu_k V_jk
   int ME;    // R x A         : mu_k e^{mu_k t_n} (distance gradient)
+  int K;     // R x (A+1) x A x A (A <= 8 only): K[n][code][k][l] = J[n][k][l] Ut[code][l]
   int total;
 };
 
@@ -96,6 +97,8 @@ int launch_warp(const KParams &p, int A, int grid, int block, size_t smem, cudaS
 int launch_tree(const KParams &p, int A, int store, int grid, int block, size_t smem,
                 cudaStream_t s);
 bool tree_supported(int A);
+int launch_tree4(const KParams &p, bool f81, int mask_mode, int grid, int block, size_t smem,
+                 cudaStream_t s);
 bool small_supported(int A);
 bool warp_supported(int A);
 int small_block();

@@ -22,7 +22,8 @@ thread_local std::string g_last_error;
 thread_local int g_launches = 0;
 // Test hook (subby_debug_set_kernel): 0 automatic, 1 thread-per-column
 // kernel (k_small) for A <= 8, 2 tree program with shared-memory slots,
-// 3 tree program with global-memory slots.
+// 3 tree program with global-memory slots, 4 generic tree program with
+// tensor-memory slots (bypassing the A = 4 specialisation).
 int g_kernel_sel = 0;
 
 int fail(int code, const std::string &msg) {
@@ -67,6 +68,21 @@ __global__ void k_compute_J(const double *__restrict__ mu, const double *__restr
     }
     J[idx] = v;
     JT[(size_t)n * A * A + l * A + k] = v;
+  }
+}
+
+// Leaf-branch weights K_n[code][k][l] = J_n[k][l] U~(code)_l (A <= 8), so
+// that a leaf branch's J-weighted outer product needs one multiply per entry.
+__global__ void k_compute_K(const float *__restrict__ J, const float *__restrict__ Ut, int R, int A,
+                            float *__restrict__ K) {
+  const int total = R * (A + 1) * A * A;
+  for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < total;
+       idx += gridDim.x * blockDim.x) {
+    const int l = idx % A;
+    const int k = (idx / A) % A;
+    const int code = (idx / (A * A)) % (A + 1);
+    const int n = idx / ((A + 1) * A * A);
+    K[idx] = J[(size_t)n * A * A + k * A + l] * Ut[code * A + l];
   }
 }
 
@@ -169,7 +185,7 @@ const char *subby_strerror(int s) {
 const char *subby_last_error(void) { return g_last_error.c_str(); }
 
 int subby_debug_set_kernel(int which) {
-  if (which < 0 || which > 3) return fail(SUBBY_ERR_ARG, "kernel selector must be 0..3");
+  if (which < 0 || which > 4) return fail(SUBBY_ERR_ARG, "kernel selector must be 0..4");
   g_kernel_sel = which;
   return SUBBY_OK;
 }
@@ -310,6 +326,7 @@ int subby_plan_create(const int32_t *parent, const double *dist, const double *e
   o.JT = take(R * A * A);
   o.F81 = take(R * 4);
   o.ME = take(R * A);
+  o.K = (A <= 8) ? take(R * (A + 1) * A * A) : 0;
   o.total = cur;
   std::vector<float> tab((size_t)o.total, 0.f);
   std::vector<double> E(A), M((size_t)A * A);
@@ -404,6 +421,12 @@ int subby_plan_create(const int32_t *parent, const double *dist, const double *e
     k_compute_J<<<grd, blk>>>(P->d_tab64 + 2 * A * A, P->d_tab64 + 2 * A * A + A, R, A,
                               P->d_tab + o.J, P->d_tab + o.JT);
     e = cudaGetLastError();
+    if (e == cudaSuccess && A <= 8) {
+      const int tk = R * (A + 1) * A * A;
+      k_compute_K<<<std::max(1, std::min((tk + 255) / 256, 4096)), 256>>>(P->d_tab + o.J, P->d_tab + o.Ut, R, A,
+                                                                         P->d_tab + o.K);
+      e = cudaGetLastError();
+    }
     if (e == cudaSuccess) e = cudaDeviceSynchronize();
     if (e != cudaSuccess) return cleanup(cuda_fail(e, "J(t) prologue"));
   }
@@ -581,14 +604,75 @@ int plan_tree(subby_plan *P, int mode, int C, Launch &L) {
   return 0;
 }
 
+// A = 4 tree kernel: all tables in shared memory, slot vectors in tensor
+// memory, one CTA of 256 (or 128) threads per SM.  Returns 1 when the plan
+// does not fit (the caller then uses the generic tree kernel).
+int plan_tree4(subby_plan *P, int mode, int C, Launch &L) {
+  const int R = P->R;
+  if (P->A != 4 || g_kernel_sel != 0) return 1;
+  KParams &k = L.kp;
+  int ntab = 0, sofs = 0;
+  auto add = [&](int gofs, int n) {
+    k.stab[ntab++] = SmemTable{gofs, sofs, n};
+    sofs += (n + 3) & ~3;
+  };
+  const TableOffsets &o = P->off;
+  const bool f81 = (mode & kModeF81) != 0;
+  add(o.MT, R * 20);
+  add(o.Vu, 16 * 4 + 20 + 4);
+  if (f81) add(o.F81, R * 4);
+  else add(o.J, R * 16);
+  if (!f81) add(o.K, R * 80);
+  // observation rows (filled in the kernel): 5 x 4 + 5, rounded up
+  k.stab[ntab++] = SmemTable{0, sofs, 0};
+  sofs += 28;
+  k.ntab = ntab;
+  k.smem_steps = sofs;
+  sofs += 16 * P->prog_steps;
+  int maxsm = 0;
+  cudaDeviceGetAttribute(&maxsm, cudaDevAttrMaxSharedMemoryPerBlockOptin, P->device);
+  int threads = 0;
+  for (int t : {256, 128}) {
+    if (P->prog_slots * 4 <= 512 / (t / 128) &&
+        (size_t)(sofs + P->prog_slots * t) * sizeof(float) + 1024 <= (size_t)maxsm) {
+      threads = t;
+      break;
+    }
+  }
+  if (!threads) return 1;
+  k.smem_slots = -1;
+  k.smem_words = sofs;
+  sofs += P->prog_slots * threads;
+  sofs = std::max(sofs, (maxsm / 2 + 4096) / 4);  // one CTA (TMEM owner) per SM
+  L.kernel = 3;
+  L.small = false;
+  L.store = 2;
+  L.block = threads;
+  L.smem = (size_t)sofs * sizeof(float);
+  const int want = (C + L.block - 1) / L.block;
+  L.grid = std::max(1, std::min(want, P->nsm));
+  L.nworkers = L.grid * L.block;
+  k.prog = P->d_prog;
+  k.nsteps = P->prog_steps;
+  k.nslots = P->prog_slots;
+  return 0;
+}
+
 int run_common(subby_plan *P, const int32_t *d_aln, int C, float *d_logL, float *d_counts,
                float *d_root, int mode, int mask_mode, const uint8_t *d_mask, const float *d_g,
                double *d_gt, double *d_gC, int *grid_out, cudaStream_t stream) {
   Launch L;
   const bool tree = tree_supported(P->A) && !(mode & kModeGrad) && g_kernel_sel != 1;
   const bool small = small_supported(P->A);
-  int rc = tree ? plan_tree(P, mode, C, L) : small ? plan_small(P, mode, C, L) : plan_warp(P, mode, C, L);
-  if (rc) return rc;
+  int rc;
+  bool tree4 = false;
+  if (tree && (rc = plan_tree4(P, mode, C, L)) == 0) {
+    tree4 = true;
+  } else {
+    L = Launch();
+    rc = tree ? plan_tree(P, mode, C, L) : small ? plan_small(P, mode, C, L) : plan_warp(P, mode, C, L);
+    if (rc) return rc;
+  }
   KParams &k = L.kp;
   k.aln = d_aln;
   k.C = C;
@@ -621,7 +705,8 @@ int run_common(subby_plan *P, const int32_t *d_aln, int C, float *d_logL, float 
   k.scrV = (float *)P->work.p;
   k.scrW = (int *)((char *)P->work.p + vb_al);
   if (grid_out) *grid_out = L.grid;
-  int lr = tree ? launch_tree(k, P->A, L.store, L.grid, L.block, L.smem, stream)
+  int lr = tree4 ? launch_tree4(k, (mode & kModeF81) != 0, mask_mode, L.grid, L.block, L.smem, stream)
+           : tree ? launch_tree(k, P->A, L.store, L.grid, L.block, L.smem, stream)
            : small ? launch_small(k, P->A, L.grid, L.block, L.smem, stream)
                    : launch_warp(k, P->A, L.grid, L.block, L.smem, stream);
   if (lr != 0) return fail(SUBBY_ERR_CUDA, std::string("kernel launch failed: ") +

@@ -22,7 +22,7 @@ import subby_gb300 as sg  # noqa: E402
 from subby_gb300 import synth, models, _lib  # noqa: E402
 
 
-KERNELS = {"auto": 0, "thread": 1, "tree_smem": 2, "tree_global": 3}
+KERNELS = {"auto": 0, "thread": 1, "tree_smem": 2, "tree_global": 3, "tree_tmem": 4}
 
 
 @pytest.fixture(params=list(KERNELS))

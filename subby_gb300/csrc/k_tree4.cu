@@ -111,7 +111,7 @@ struct N4 {
 // Shared-memory table layout (float offsets), set by the host in KParams:
 //   stab[0] MT   R x 5 x 4      stab[1] small block (Vu, Vd, Ut, pi, S, V)
 //   stab[2] J    R x 16 (eigen) or F81 R x 4
-//   stab[3] K    R x 5 x 16 (eigen: K_n[code][k][l] = J_n[k][l] Ut[code][l])
+//   stab[3] K    R x 5 x 20 (eigen: K_n[code][k][l] = J_n[k][l] Ut[code][l], rows padded)
 //   stab[4] LV   5 x 4 (observation rows), followed by piL[5] (pi . L(code))
 template <bool F81, int MASK>
 __global__ void __launch_bounds__(256, 1) k_tree4(const KParams P) {
@@ -189,10 +189,10 @@ __global__ void __launch_bounds__(256, 1) k_tree4(const KParams P) {
       o[0] = tok(s0.x);
       o[1] = tok(s1.x);
       o[2] = tok(s2.x);
-      o[3] = tok(max(s1.z, 0));
-      o[4] = tok(max(s1.w, 0));
-      o[5] = tok(max(s2.z, 0));
-      o[6] = tok(max(s2.w, 0));
+      o[3] = tok(s1.z);  // grandchildren indices are 0 when absent
+      o[4] = tok(s1.w);
+      o[5] = tok(s2.z);
+      o[6] = tok(s2.w);
     };
     // Gather the children of a step: leaves from tables, stored ones from
     // tensor memory (all loads issued before one wait), derived ones
@@ -203,9 +203,8 @@ __global__ void __launch_bounds__(256, 1) k_tree4(const KParams P) {
     };
     auto gather = [&](const int4 &s1, const int4 &s2, const int4 &s3, const int (&t)[7], N4 &nl, N4 &nr,
                       Dv &dl, Dv &dr, bool wantD, int slotD, F4 &D, int &wD) {
-      uint32_t r0[4] = {0, 0, 0, 0}, r1[4] = {0, 0, 0, 0}, r2[4] = {0, 0, 0, 0};
-      uint32_t r3[4] = {0, 0, 0, 0}, r4[4] = {0, 0, 0, 0}, r5[4] = {0, 0, 0, 0};
-      uint32_t r6[4] = {0, 0, 0, 0};
+      // registers of loads that a step does not issue are never read
+      uint32_t r0[4], r1[4], r2[4], r3[4], r4[4], r5[4], r6[4];
       // issue
       if (s1.y >= 0) tmld(tb + 4 * s1.y, r0);
       if (s2.y >= 0) tmld(tb + 4 * s2.y, r1);
@@ -333,7 +332,7 @@ __global__ void __launch_bounds__(256, 1) k_tree4(const KParams P) {
         dt = fma4(Ds.b.x, ld4s(Vd + 8), dt);
         dt = fma4(Ds.b.y, ld4s(Vd + 12), dt);
         if (code >= 0) {
-          const float *K = KT + (n * 5 + code) * 16;
+          const float *K = KT + (n * 5 + code) * 20;  // rows padded to 20: conflict-free
           acc[0] = fma4(dt.a.x, ld4s(K), acc[0]);
           acc[1] = fma4(dt.a.y, ld4s(K + 4), acc[1]);
           acc[2] = fma4(dt.b.x, ld4s(K + 8), acc[2]);

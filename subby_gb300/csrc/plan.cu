@@ -71,7 +71,8 @@ __global__ void k_compute_J(const double *__restrict__ mu, const double *__restr
   }
 }
 
-// Leaf-branch weights K_n[code][k][l] = J_n[k][l] U~(code)_l (A <= 8), so
+// Leaf-branch weights K_n[code][k][l] = J_n[k][l] U~(code)_l (A <= 8; row
+// stride A*A + 4), so
 // that a leaf branch's J-weighted outer product needs one multiply per entry.
 __global__ void k_compute_K(const float *__restrict__ J, const float *__restrict__ Ut, int R, int A,
                             float *__restrict__ K) {
@@ -82,7 +83,8 @@ __global__ void k_compute_K(const float *__restrict__ J, const float *__restrict
     const int k = (idx / A) % A;
     const int code = (idx / (A * A)) % (A + 1);
     const int n = idx / ((A + 1) * A * A);
-    K[idx] = J[(size_t)n * A * A + k * A + l] * Ut[code * A + l];
+    // rows of A*A + 4 floats (padding keeps per-thread rows on distinct banks)
+    K[((size_t)n * (A + 1) + code) * (A * A + 4) + k * A + l] = J[(size_t)n * A * A + k * A + l] * Ut[code * A + l];
   }
 }
 
@@ -276,7 +278,7 @@ int subby_plan_create(const int32_t *parent, const double *dist, const double *e
       for (int side = 0; side < 2; ++side) {
         const int ch = side ? right[v] : left[v];
         const int kl = left[ch], kr = right[ch];
-        c[side] = make_int4(ch, kind[ch], kl, kr);
+        c[side] = make_int4(ch, kind[ch], std::max(kl, 0), std::max(kr, 0));
         if (kind[ch] == -2) {
           gk[2 * side] = kind[kl];
           gk[2 * side + 1] = kind[kr];
@@ -326,7 +328,7 @@ int subby_plan_create(const int32_t *parent, const double *dist, const double *e
   o.JT = take(R * A * A);
   o.F81 = take(R * 4);
   o.ME = take(R * A);
-  o.K = (A <= 8) ? take(R * (A + 1) * A * A) : 0;
+  o.K = (A <= 8) ? take(R * (A + 1) * (A * A + 4)) : 0;
   o.total = cur;
   std::vector<float> tab((size_t)o.total, 0.f);
   std::vector<double> E(A), M((size_t)A * A);
@@ -622,7 +624,7 @@ int plan_tree4(subby_plan *P, int mode, int C, Launch &L) {
   add(o.Vu, 16 * 4 + 20 + 4);
   if (f81) add(o.F81, R * 4);
   else add(o.J, R * 16);
-  if (!f81) add(o.K, R * 80);
+  if (!f81) add(o.K, R * 100);
   // observation rows (filled in the kernel): 5 x 4 + 5, rounded up
   k.stab[ntab++] = SmemTable{0, sofs, 0};
   sofs += 28;

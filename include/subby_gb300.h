@@ -138,6 +138,32 @@ int subby_rootprob(const int32_t *alignment, const int32_t *parent_index,
                    const double *eigenvectors, const double *pi,
                    int R, int C, int A, float *rootProb, int flags, void *stream);
 
+/*
+ * Counts (and optionally LogLike) for A = 4 without allocating anything: no
+ * cudaMalloc / cudaFree and no host heap allocation.  For callers that
+ * cannot allocate device memory — a framework whose caching allocator owns
+ * the device heap, a plugin or callback that must not allocate, a service
+ * that fixes its device footprint at start-up.  Every table the kernel reads
+ * lives in one file-scope device array of 1 MiB that each GPU loading the
+ * library holds until exit; slot state stays in tensor / shared memory.
+ *   alignment (R, C) int32, mask (R, C) uint8 (SUBBY_MASK_GIVEN only),
+ *   counts (A*A*C) and logLike (C, may be NULL): DEVICE pointers.
+ *   Tree and model arrays: host pointers, as elsewhere.
+ * Limits: A = 4, R <= 1023 nodes, and the tree program must fit the A = 4
+ * kernel's on-chip budget; larger inputs return SUBBY_ERR_UNSUPPORTED.
+ * The first call on a device resolves the array's device address with that
+ * device current; make that first call before any stream capture.  Each call
+ * rewrites every table it uses, so nothing needs clearing between calls, but
+ * calls that overlap on the GPU share the array and race.  Work is enqueued
+ * on `stream`.  No counterpart in the reference.
+ */
+int subby_counts_noalloc(const int32_t *alignment, const int32_t *parent_index,
+                         const double *distances, const double *eigenvalues,
+                         const double *eigenvectors, const double *pi,
+                         int R, int C, int counts_kind, int mask_mode,
+                         const uint8_t *mask, float *counts, float *logLike,
+                         void *stream);
+
 /* Test hook selecting the kernel for alphabets A <= 8 so that every code
  * path can be checked against the oracle: 0 automatic (A = 4 tree kernel
  * with tensor-memory slots when it fits), 1 thread-per-column kernel, 2

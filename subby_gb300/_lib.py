@@ -22,7 +22,7 @@ EXPORTS = (
     "subby_version", "subby_strerror", "subby_last_error", "subby_plan_create",
     "subby_plan_destroy", "subby_plan_device_bytes", "subby_plan_run", "subby_plan_grad",
     "subby_loglike", "subby_counts", "subby_rootprob", "subby_last_launch_count",
-    "subby_debug_set_kernel",
+    "subby_debug_set_kernel", "subby_counts_noalloc",
 )
 
 _lock = threading.Lock()
@@ -68,6 +68,9 @@ def _declare(lib):
         f = getattr(lib, name)
         f.restype = ct.c_int
         f.argtypes = [_p, _p, _p, _p, _p, _p, ct.c_int, ct.c_int, ct.c_int, _p, ct.c_int, _p]
+    lib.subby_counts_noalloc.restype = ct.c_int
+    lib.subby_counts_noalloc.argtypes = [_p, _p, _p, _p, _p, _p, ct.c_int, ct.c_int, ct.c_int,
+                                         ct.c_int, _p, _p, _p, _p]
     lib.subby_counts.restype = ct.c_int
     lib.subby_counts.argtypes = [_p, _p, _p, _p, _p, _p, ct.c_int, ct.c_int, ct.c_int, ct.c_int,
                                  ct.c_int, _p, _p, ct.c_int, _p]

@@ -67,6 +67,22 @@ def rate_matrix_torch(log_exch: torch.Tensor, pi: torch.Tensor) -> torch.Tensor:
     return Q - torch.diag(Q.sum(1))
 
 
+def exchangeability_grad(G, log_exch, pi):
+    """d(sum g logL)/d(log s) from G = d(sum g logL)/dS~ (A x A, FP64).
+
+    dL/dQ_ij = sqrt(pi_i/pi_j) G_ij for S~ = diag(sqrt pi) Q diag(1/sqrt pi);
+    the chain through Q(log s) (with its normalisation) runs in FP64 torch.
+    """
+    pi = np.asarray(pi, dtype=np.float64)
+    sp = np.sqrt(pi)
+    dLdQ = torch.as_tensor(np.asarray(G, dtype=np.float64) * (sp[:, None] / sp[None, :]))
+    with torch.enable_grad():
+        le = torch.as_tensor(np.asarray(log_exch, dtype=np.float64)).clone().requires_grad_(True)
+        Q = rate_matrix_torch(le, torch.as_tensor(pi))
+        (dle,) = torch.autograd.grad(Q, le, grad_outputs=dLdQ)
+    return dle.numpy()
+
+
 class _LogLikeRev(torch.autograd.Function):
     @staticmethod
     def forward(ctx, distances, log_exch, alignment, parent, pi):
@@ -85,14 +101,9 @@ class _LogLikeRev(torch.autograd.Function):
         (log_exch,) = ctx.saved_tensors
         _, dldt, G = ctx.plan.grad(ctx.alignment, g=_as_np(g, np.float32), want_loglike=False)
         ctx.plan.close()
-        sp = np.sqrt(ctx.pi)
-        dLdQ = torch.as_tensor(G * (sp[:, None] / sp[None, :]))
-        with torch.enable_grad():
-            le = log_exch.detach().double().cpu().requires_grad_(True)
-            Q = rate_matrix_torch(le, torch.as_tensor(ctx.pi))
-            (dle,) = torch.autograd.grad(Q, le, grad_outputs=dLdQ)
+        dle = exchangeability_grad(G, log_exch.detach().double().cpu().numpy(), ctx.pi)
         return (torch.as_tensor(dldt, dtype=g.dtype, device=g.device),
-                dle.to(dtype=log_exch.dtype, device=log_exch.device), None, None, None)
+                torch.as_tensor(dle, dtype=log_exch.dtype, device=log_exch.device), None, None, None)
 
 
 def loglike_reversible(alignment, parentIndex, distances, log_exch, pi):

@@ -1,0 +1,69 @@
+"""World-size-2 gloo run of the column-sharding host logic on CPU.
+
+Each rank takes its column range, computes LogLike / Counts / RootProb for it
+(with the FP64 oracle standing in for the GPU, which this CPU test cannot
+use), the ranks gather along the column axis, and rank 0 checks the result
+equals the unsharded computation; the MAX reduction used for step timing is
+checked too.
+"""
+import os
+import socket
+
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+import torch.distributed as dist  # noqa: E402
+import torch.multiprocessing as mp  # noqa: E402
+
+
+def _free_port():
+    s = socket.socket()
+    s.bind(("127.0.0.1", 0))
+    port = s.getsockname()[1]
+    s.close()
+    return port
+
+
+def _worker(rank, world, port, q):
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    try:
+        import oracle
+        from subby_gb300 import synth, shard
+        w = synth.plain_small(seed=1, C=203)
+        aln, tree, m = w['alignment'], w['tree'], w['model']
+        t = oracle.Tree(tree.parentIndex, tree.distanceToParent)
+        md = m._asdict()
+        loc = shard.local_alignment(aln, rank, world)
+        ll = shard.gather_columns(oracle.LogLike(loc, t, md), aln.shape[1])
+        ct = shard.gather_columns(oracle.Counts(loc, t, md), aln.shape[1])
+        rp = shard.gather_columns(oracle.RootProb(loc, t, md), aln.shape[1])
+        mx = shard.max_over_ranks(1.0 + rank)
+        if rank == 0:
+            ok = (np.allclose(ll, oracle.LogLike(aln, t, md), rtol=0, atol=1e-12)
+                  and np.allclose(ct, oracle.Counts(aln, t, md), rtol=0, atol=1e-12)
+                  and np.allclose(rp, oracle.RootProb(aln, t, md), rtol=0, atol=1e-12)
+                  and mx == float(world))
+            q.put(ok)
+    finally:
+        dist.destroy_process_group()
+
+
+def test_column_ranges_partition():
+    from subby_gb300 import shard
+    for C in (0, 1, 7, 1024, 1025):
+        for world in (1, 2, 3, 8):
+            spans = [shard.column_range(C, r, world) for r in range(world)]
+            assert spans[0][0] == 0 and spans[-1][1] == C
+            assert all(a[1] == b[0] for a, b in zip(spans, spans[1:]))
+            assert max(b - a for a, b in spans) - min(b - a for a, b in spans) <= 1
+
+
+def test_sharded_results_equal_unsharded_gloo_world2():
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = _free_port()
+    mp.start_processes(_worker, args=(2, port, q), nprocs=2, join=True, start_method="spawn")
+    assert q.get(timeout=60) is True

@@ -163,6 +163,11 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--columns", type=int, default=1 << 20)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--workload", choices=["plain_large", "precision64", "grad20", "serving"],
+                    default="plain_large",
+                    help="plain_large is the headline line; the others print their own line")
+    ap.add_argument("--jobs", type=int, default=2000, help="serving: number of jobs")
+    ap.add_argument("--rate", type=float, default=200.0, help="serving: Poisson arrival rate (jobs/s)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -177,6 +182,12 @@ def main():
         if rank != 0:
             return 0
         return reference_arm(args, world)
+    if args.workload == "serving":
+        return serving_bench(args)
+    if args.workload == "precision64":
+        return precision64_bench(args)
+    if args.workload == "grad20":
+        return grad20_bench(args)
 
     # spawn pool for the CPU baseline before any GPU work
     pool = None
@@ -311,6 +322,119 @@ def main():
     print(json.dumps(line))
     if dist_on:
         torch.distributed.destroy_process_group()
+    return 0
+
+
+def _time_fn(fn, steps, warmup):
+    import torch
+    for _ in range(warmup):
+        fn()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(steps):
+        fn()
+    e1.record()
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / steps
+
+
+def precision64_bench(args):
+    """A=64 random reversible model with near-degenerate eigenvalue pairs,
+    R=127, C=65536: Counts columns/s and error vs the FP64 oracle."""
+    import torch
+    import oracle
+    import subby_gb300 as sg
+    from subby_gb300 import synth, _lib
+    from tests._tol import colwise_err, loglike_err
+    C = args.columns if args.columns != (1 << 20) else 65536
+    w = synth.precision64(seed=3, C=C)
+    plan = sg.Plan(w['tree'], w['model'])
+    d_aln = torch.as_tensor(w['alignment']).cuda()
+    out = {'counts': torch.empty((64, 64, C), dtype=torch.float32, device="cuda"),
+           'logLike': torch.empty(C, dtype=torch.float32, device="cuda")}
+    ms = _time_fn(lambda: plan.run(d_aln, loglike=True, counts=True, branch_mask=None, out=out),
+                  args.steps, args.warmup)
+    launches = _lib.last_launch_count()
+    sub = w['alignment'][:, :32]
+    md = w['model']._asdict()
+    t = oracle.Tree(w['tree'].parentIndex, w['tree'].distanceToParent)
+    err_c = colwise_err(out['counts'][:, :, :32].cpu().numpy(), oracle.Counts(sub, t, md, branch_mask=None))
+    err_l = loglike_err(out['logLike'][:32].cpu().numpy(), oracle.LogLike(sub, t, md))
+    print(json.dumps({"metric": "Counts columns/s (A=64 reversible, R=127, C=65536)", "value": C / (ms / 1e3),
+                      "unit": UNIT, "ms_per_step": ms, "steps": args.steps, "warmup": args.warmup,
+                      "higher_is_better": True, "dtype": "fp32", "kernel": "warp-per-column FP32",
+                      "forced_near_degenerate_pairs": w['forced_pairs'], "gpu_launches": launches * args.steps,
+                      "err_vs_oracle": {"loglike_rel": err_l, "counts_colwise": err_c, "columns": 32}}))
+    return 0
+
+
+def grad20_bench(args):
+    """A=20 reversible model, R=399, C=100000: forward + adjoint gradient
+    (d sum logL / d branch lengths and / d log-exchangeabilities)."""
+    import torch
+    import subby_gb300 as sg
+    from subby_gb300 import synth, autograd
+    C = args.columns if args.columns != (1 << 20) else 100000
+    w = synth.grad20(seed=4, C=C)
+    plan = sg.Plan(w['tree'], w['model'])
+    aln = w['alignment']
+    t0 = time.perf_counter()
+    for _ in range(args.warmup):
+        plan.grad(aln)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        _, dldt, G = plan.grad(aln)
+    ms = (time.perf_counter() - t0) * 1e3 / args.steps
+    dle = autograd.exchangeability_grad(G, w['log_exch'], w['pi'])
+    print(json.dumps({"metric": "LogLike + adjoint gradient columns/s (A=20, R=399, C=100000, host buffers)",
+                      "value": C / (ms / 1e3), "unit": UNIT, "ms_per_step": ms, "steps": args.steps,
+                      "higher_is_better": True, "dtype": "fp32",
+                      "grad_norms": {"d_dt": float(np.linalg.norm(dldt)), "d_dlogs": float(np.linalg.norm(dle))}}))
+    return 0
+
+
+def serving_bench(args):
+    """Poisson job stream (uneven R, C, A) through the continuous-batching
+    loop; per-job latency from arrival to results in host memory."""
+    import torch
+    import subby_gb300 as sg
+    from subby_gb300 import synth, serve, models
+    desc = synth.serving_jobs(n_jobs=args.jobs, rate=args.rate, seed=5)
+    jobs = []
+    for d in desc:
+        rng = np.random.default_rng(d['seed'])
+        A = d['A']
+        if d['kind'] == 'hky85':
+            model = models.hky85_diag(2.0, rng.dirichlet(np.ones(4)))
+        elif d['kind'] == 'f81':
+            model = models.f81_model(rng.dirichlet(np.ones(A)))
+        else:
+            model, _, _ = models.random_reversible(A, rng)
+        tree = synth.random_tree(d['leaves'], 0.1, rng)
+        R, C = len(tree.parentIndex), d['C']
+        leaf = synth.leaf_mask(tree)
+
+        def make(stream, device, R=R, C=C, A=A, leaf=leaf, seed=d['seed']):
+            # tokens generated on the device: uniform leaf states with 5% gaps, internal rows A
+            g = torch.Generator(device=device)
+            g.manual_seed(seed)
+            x = torch.randint(0, A, (R, C), dtype=torch.int32, device=device, generator=g)
+            gap = torch.rand((R, C), device=device, generator=g) < 0.05
+            x[gap] = A + 1
+            x[torch.as_tensor(~leaf, device=device)] = A
+            return x
+        jobs.append(serve.Job(id=d['id'], alignment=make, shape=(R, C), tree=tree, model=model,
+                              f81=(d['kind'] == 'f81'), want=("counts",), arrival=d['arrival']))
+    srv = serve.Server(max_inflight=16, device_budget=64 << 30)
+    done = srv.run(jobs, realtime=True)
+    st = serve.latency_stats(done)
+    srv.close()
+    print(json.dumps({"metric": "serving latency (Poisson arrivals, uneven R/C/A)", "value": st['p99_ms'],
+                      "unit": "ms (p99)", "higher_is_better": False, "p50_ms": st['p50_ms'],
+                      "p99_ms": st['p99_ms'], "max_ms": st['max_ms'], "jobs": st['jobs'],
+                      "columns_per_s": st['columns_per_s'], "span_s": st['span_s'], "rate_jobs_per_s": args.rate,
+                      "data": "synthetic: per-job random tree and model, uniform device-generated tokens"}))
     return 0
 
 

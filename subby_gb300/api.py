@@ -82,13 +82,15 @@ class Plan:
 
     # ------------------------------------------------------------------ run
     def run(self, alignment, loglike=True, counts=False, rootprob=False, f81=False,
-            branch_mask="auto", bt64=None, out=None):
+            branch_mask="auto", bt64=None, out=None, stream=None):
         """Run the hot path; returns a dict with the requested outputs.
 
         ``branch_mask``: "auto" (Steiner mask, the reference default for
         Counts), None (unmasked) or an (R, C) bool array.  ``bt64``: None =
         FP64 back-transform for A <= 8 and FP32 above; True/False forces it.
         ``out``: optional dict of preallocated output buffers (same keys).
+        ``stream``: torch.cuda.Stream for the device-pointer path (default:
+        the current stream).
         """
         lib = _lib.load()
         kind = _lib.COUNTS_F81 if f81 else _lib.COUNTS_EIGEN
@@ -132,7 +134,7 @@ class Plan:
                 dmask = dmask.to(device=dev, dtype=torch.uint8).contiguous()
                 if tuple(dmask.shape) != (self.R, C):
                     raise ValueError("branch_mask must have shape (R, C)")
-            stream = torch.cuda.current_stream(dev).cuda_stream
+            stream = (stream if stream is not None else torch.cuda.current_stream(dev)).cuda_stream
 
             def dp(t):
                 return ct.c_void_p(t.data_ptr()) if t is not None else None

@@ -71,6 +71,36 @@ __global__ void k_compute_J(const double *__restrict__ mu, const double *__restr
   }
 }
 
+// Substitution matrices M_n(t) = diag(1/sqrt pi) V e^{Lambda t} V^T diag(sqrt pi)
+// (subby/oracle/oracle.py:747-777), evaluated in FP64 from the FP64
+// eigensystem (the reference's own model-preparation precision) and stored
+// as FP32 tables: MT[n][j][b] = M_n[b][j], MT[n][A][b] = sum_j M_n[b][j]
+// (likelihood of an unobserved child), MN[n][b][j] = M_n[b][j].  One thread
+// per (node, row); preparing a plan on the device keeps tree set-up off the
+// host's critical path when many trees arrive.
+__global__ void k_compute_M(const double *__restrict__ V, const double *__restrict__ mu,
+                            const double *__restrict__ t, const double *__restrict__ pi, int R, int A,
+                            float *__restrict__ MT, float *__restrict__ MN) {
+  const int total = R * A;
+  for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < total; idx += gridDim.x * blockDim.x) {
+    const int n = idx / A, b = idx % A;
+    const double tn = t[n];
+    const double isb = 1.0 / sqrt(pi[b]);
+    double w[64];  // V[b][k] e^{mu_k t}, A <= 64
+    for (int k = 0; k < A; ++k) w[k] = V[b * A + k] * exp(mu[k] * tn);
+    double rs = 0.0;
+    for (int j = 0; j < A; ++j) {
+      double s = 0.0;
+      for (int k = 0; k < A; ++k) s += w[k] * V[j * A + k];
+      const double m = isb * sqrt(pi[j]) * s;
+      MT[((size_t)n * (A + 1) + j) * A + b] = (float)m;
+      MN[((size_t)n * A + b) * A + j] = (float)m;
+      rs += m;
+    }
+    MT[((size_t)n * (A + 1) + A) * A + b] = (float)rs;
+  }
+}
+
 // Leaf-branch weights K_n[code][k][l] = J_n[k][l] U~(code)_l (A <= 8; row
 // stride A*A + 4), so
 // that a leaf branch's J-weighted outer product needs one multiply per entry.
@@ -331,27 +361,12 @@ int subby_plan_create(const int32_t *parent, const double *dist, const double *e
   o.K = (A <= 8) ? take(R * (A + 1) * (A * A + 4)) : 0;
   o.total = cur;
   std::vector<float> tab((size_t)o.total, 0.f);
-  std::vector<double> E(A), M((size_t)A * A);
+  std::vector<double> E(A);
+  // M(t) itself (MT / MN tables) is formed by k_compute_M on the device, in
+  // FP64, right after the upload below.
   for (int n = 0; n < R; ++n) {
     const double t = dist[n];
     for (int k = 0; k < A; ++k) E[k] = std::exp(evals[k] * t);
-    for (int i = 0; i < A; ++i)
-      for (int j = 0; j < A; ++j) {
-        double s = 0.0;
-        for (int k = 0; k < A; ++k) s += evecs[i * A + k] * E[k] * evecs[j * A + k];
-        M[i * A + j] = isp[i] * sp[j] * s;  // subby/oracle/oracle.py:770-776
-      }
-    float *mt = tab.data() + o.MT + (size_t)n * (A + 1) * A;
-    float *mn = tab.data() + o.MN + (size_t)n * A * A;
-    for (int b = 0; b < A; ++b) {
-      double rs = 0.0;
-      for (int j = 0; j < A; ++j) {
-        mt[j * A + b] = (float)M[b * A + j];
-        rs += M[b * A + j];
-      }
-      mt[A * A + b] = (float)rs;
-    }
-    for (int i = 0; i < A * A; ++i) mn[i] = (float)M[i];
     // F81 branch coefficients (subby/oracle/oracle.py:1226-1233)
     const double e = std::exp(-mu81 * t), pp = 1.0 - e;
     float *f = tab.data() + o.F81 + (size_t)n * 4;
@@ -393,13 +408,14 @@ int subby_plan_create(const int32_t *parent, const double *dist, const double *e
   if (e != cudaSuccess) return cleanup(cuda_fail(e, "cudaMalloc(tables)"));
   e = cudaMemcpy(P->d_tab, tab.data(), P->tab_bytes, cudaMemcpyHostToDevice);
   if (e != cudaSuccess) return cleanup(cuda_fail(e, "cudaMemcpy(tables)"));
-  e = cudaMalloc(&P->d_tab64, sizeof(double) * (2 * A * A + A + R));
+  e = cudaMalloc(&P->d_tab64, sizeof(double) * (2 * A * A + A + R + A));
   if (e != cudaSuccess) return cleanup(cuda_fail(e, "cudaMalloc(tables64)"));
-  std::vector<double> t64((size_t)2 * A * A + A + R);
+  std::vector<double> t64((size_t)2 * A * A + A + R + A);
   std::copy(evecs, evecs + A * A, t64.begin());
   std::copy(S64.begin(), S64.end(), t64.begin() + A * A);
   std::copy(evals, evals + A, t64.begin() + 2 * A * A);
   std::copy(dist, dist + R, t64.begin() + 2 * A * A + A);
+  std::copy(pi, pi + A, t64.begin() + 2 * A * A + A + R);
   e = cudaMemcpy(P->d_tab64, t64.data(), sizeof(double) * t64.size(), cudaMemcpyHostToDevice);
   if (e != cudaSuccess) return cleanup(cuda_fail(e, "cudaMemcpy(tables64)"));
   if (P->nInt > 0) {
@@ -418,6 +434,12 @@ int subby_plan_create(const int32_t *parent, const double *dist, const double *e
     if (e != cudaSuccess) return cleanup(cuda_fail(e, "program upload"));
   }
   {
+    const int tm = R * A;
+    k_compute_M<<<std::max(1, std::min((tm + 127) / 128, 4096)), 128>>>(
+        P->d_tab64, P->d_tab64 + 2 * A * A, P->d_tab64 + 2 * A * A + A, P->d_tab64 + 2 * A * A + A + R, R, A,
+        P->d_tab + o.MT, P->d_tab + o.MN);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return cleanup(cuda_fail(e, "M(t) prologue"));
     const int total = R * A * A;
     const int blk = 256, grd = std::max(1, std::min((total + blk - 1) / blk, 4096));
     k_compute_J<<<grd, blk>>>(P->d_tab64 + 2 * A * A, P->d_tab64 + 2 * A * A + A, R, A,

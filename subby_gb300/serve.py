@@ -1,0 +1,223 @@
+"""Continuous-batching request loop for the eigensubstitution path.
+
+Jobs (alignment, tree, model, options) arrive over time.  The loop
+
+* admits a waiting job as soon as a device slot is free and its device
+  footprint (plan tables + tokens + outputs + workspace estimate) fits the
+  memory budget — requests that arrive while others are on the GPU are
+  admitted while those run;
+* keeps prepared plans (tree tables, eigendecomposition-derived tables, J(t))
+  resident in HBM in an LRU cache keyed by (tree, model), so a repeated
+  tree/model pays no preparation;
+* stages each job's tokens from pinned host memory on the slot's own CUDA
+  stream, enqueues the kernel on that stream and reads the results back on
+  it, so the work of concurrent jobs overlaps on the device (a small job's
+  grid covers only the SMs its columns need, leaving the rest to others);
+* never runs two jobs of the same plan at once (a plan's workspace is
+  per-plan), so such a job waits for its twin to finish;
+* completes jobs in whatever order their streams finish and records, per job,
+  the latency from arrival to results-in-host-memory.
+
+Results of a job do not depend on what else is in flight: every job runs the
+same kernel on the same inputs as it would alone (``tests/test_gpu_serving``
+checks this).
+"""
+from __future__ import annotations
+
+import collections
+import hashlib
+import threading
+import time
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from .api import Plan
+from .models import ensure_diag
+
+
+@dataclass
+class Job:
+    id: int
+    alignment: object              # (R, C) int32: host array, CUDA tensor, or a
+    #                                callable(stream, device) -> CUDA tensor
+    tree: object
+    model: object
+    f81: bool = False
+    branch_mask: object = "auto"
+    want: tuple = ("counts",)      # subset of ("logLike", "counts", "rootProb")
+    arrival: float = 0.0           # seconds since the loop started
+    shape: tuple = None            # (R, C), required when alignment is a callable
+    # filled by the server
+    start: float = -1.0
+    finish: float = -1.0
+    result: dict = field(default_factory=dict)
+
+    @property
+    def latency(self):
+        return self.finish - self.arrival
+
+    @property
+    def RC(self):
+        return tuple(self.shape) if self.shape is not None else tuple(self.alignment.shape)
+
+
+def _plan_key(tree, model):
+    m = ensure_diag(model)
+    h = hashlib.sha1()
+    for a in (tree.parentIndex, tree.distanceToParent, m.eigenvalues, m.eigenvectors, m.pi):
+        h.update(np.ascontiguousarray(a, dtype=np.float64).tobytes())
+    return h.hexdigest()
+
+
+def job_device_bytes(R: int, C: int, A: int) -> int:
+    """Device footprint estimate of one in-flight job (bytes)."""
+    tables = 4 * R * (A + 1) * A * 6 + 4 * R * (A + 1) * (A * A + 4) * (A <= 8)
+    tokens = 4 * R * C
+    outputs = 4 * C * (A * A + A + 1)
+    scratch = 4 * R * (A + 2) * min(C, 152 * 256)
+    return tables + tokens + outputs + scratch
+
+
+class Server:
+    """Continuous batching over CUDA streams with memory-budget admission."""
+
+    def __init__(self, max_inflight: int = 8, device_budget: int = 16 << 30, plan_cache: int = 64,
+                 device=None):
+        import torch
+        self.torch = torch
+        self.device = torch.device("cuda", torch.cuda.current_device() if device is None else device)
+        self.max_inflight = max_inflight
+        self.budget = device_budget
+        self.streams = [torch.cuda.Stream(device=self.device) for _ in range(max_inflight)]
+        self.free_slots = list(range(max_inflight))
+        self.plans = collections.OrderedDict()
+        self.plan_cache = plan_cache
+        self.inflight = []           # (job, slot, event, bytes, bufs)
+        self.used_bytes = 0
+        self.completed = []
+        self.lock = threading.Lock()
+
+    # ------------------------------------------------------------------ plans
+    @staticmethod
+    def _key(job):
+        k = getattr(job, "_plan_key", None)
+        if k is None:
+            k = _plan_key(job.tree, job.model)
+            job._plan_key = k
+        return k
+
+    def plan_for(self, tree, model, key=None) -> Plan:
+        k = key or _plan_key(tree, model)
+        p = self.plans.get(k)
+        if p is not None:
+            self.plans.move_to_end(k)
+            return p
+        p = Plan(tree, model, device=self.device)
+        self.plans[k] = p
+        while len(self.plans) > self.plan_cache:
+            self.plans.popitem(last=False)[1].close()
+        return p
+
+    # ---------------------------------------------------------------- submit
+    def _launch(self, job: Job, now: float):
+        torch = self.torch
+        R, C = job.RC
+        A = len(ensure_diag(job.model).pi)
+        nbytes = job_device_bytes(R, C, A)
+        slot = self.free_slots.pop()
+        stream = self.streams[slot]
+        plan = self.plan_for(job.tree, job.model, self._key(job))
+        h_aln = None
+        with torch.cuda.stream(stream):
+            if callable(job.alignment):
+                d_aln = job.alignment(stream, self.device)
+            elif isinstance(job.alignment, torch.Tensor) and job.alignment.is_cuda:
+                d_aln = job.alignment
+            else:
+                h_aln = torch.from_numpy(np.ascontiguousarray(job.alignment, dtype=np.int32))
+                if not h_aln.is_pinned():
+                    h_aln = h_aln.pin_memory()
+                d_aln = h_aln.to(self.device, non_blocking=True)
+            res = plan.run(d_aln, loglike="logLike" in job.want, counts="counts" in job.want,
+                           rootprob="rootProb" in job.want, f81=job.f81,
+                           branch_mask=job.branch_mask, stream=stream)
+            host = {}
+            for k, v in res.items():
+                hv = torch.empty(v.shape, dtype=v.dtype, pin_memory=True)
+                hv.copy_(v, non_blocking=True)
+                host[k] = hv
+            ev = torch.cuda.Event()
+            ev.record(stream)
+        job.start = now
+        self.used_bytes += nbytes
+        self.inflight.append((job, slot, ev, nbytes, (h_aln, d_aln, res, host)))
+
+    def fits(self, job: Job) -> bool:
+        R, C = job.RC
+        A = len(ensure_diag(job.model).pi)
+        need = job_device_bytes(R, C, A)
+        if not self.free_slots:
+            return False
+        key = self._key(job)
+        if any(self._key(j) == key for j, *_ in self.inflight):
+            return False
+        return self.used_bytes + need <= self.budget or not self.inflight
+
+    def poll(self, now_fn):
+        """Retire finished jobs; returns how many finished."""
+        done = 0
+        keep = []
+        for job, slot, ev, nbytes, bufs in self.inflight:
+            if ev.query():
+                job.finish = now_fn()
+                job.result = {k: v.numpy() for k, v in bufs[3].items()}
+                self.free_slots.append(slot)
+                self.used_bytes -= nbytes
+                self.completed.append(job)
+                done += 1
+            else:
+                keep.append((job, slot, ev, nbytes, bufs))
+        self.inflight = keep
+        return done
+
+    # ------------------------------------------------------------------- run
+    def run(self, jobs, realtime: bool = True, on_admit=None):
+        """Serve ``jobs`` (sorted by ``arrival``).  With ``realtime`` the loop
+        admits a job only once the wall clock reaches its arrival time;
+        otherwise all jobs are available at t=0.  Returns the completed jobs."""
+        t0 = time.perf_counter()
+        now = lambda: time.perf_counter() - t0  # noqa: E731
+        pending = collections.deque(sorted(jobs, key=lambda j: j.arrival))
+        waiting = collections.deque()
+        while pending or waiting or self.inflight:
+            t = now()
+            while pending and (not realtime or pending[0].arrival <= t):
+                j = pending.popleft()
+                if not realtime:
+                    j.arrival = t
+                waiting.append(j)
+            while waiting and self.fits(waiting[0]):
+                j = waiting.popleft()
+                self._launch(j, now())
+                if on_admit:
+                    on_admit(j)
+            if self.poll(now) == 0:
+                if self.inflight:
+                    time.sleep(0.0002)
+                elif pending and realtime:
+                    time.sleep(max(0.0, min(0.002, pending[0].arrival - now())))
+        return self.completed
+
+    def close(self):
+        for p in self.plans.values():
+            p.close()
+        self.plans.clear()
+
+
+def latency_stats(jobs):
+    lat = np.array([j.latency for j in jobs]) * 1000.0
+    cols = sum(j.RC[1] for j in jobs)
+    span = max(j.finish for j in jobs) - min(j.arrival for j in jobs)
+    return {"jobs": len(jobs), "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+            "max_ms": float(lat.max()), "columns": int(cols), "columns_per_s": cols / span, "span_s": span}

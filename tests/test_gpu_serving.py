@@ -1,0 +1,61 @@
+"""Continuous-batching loop: jobs of uneven R, C and A run concurrently on
+several streams; each job's result equals the same job run alone (and the
+oracle on a column subsample), within the parity tolerances."""
+import numpy as np
+import pytest
+
+import oracle
+from tests._tol import assert_cols, assert_loglike, COUNTS_RTOL
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+if not torch.cuda.is_available():  # pragma: no cover
+    pytest.skip("needs a CUDA GPU", allow_module_level=True)
+
+import subby_gb300 as sg  # noqa: E402
+from subby_gb300 import synth, serve  # noqa: E402
+
+
+def _jobs(n=24, seed=8):
+    desc = synth.serving_jobs(n_jobs=n, rate=1000.0, seed=seed, max_columns=3000, min_columns=40,
+                              min_leaves=4, max_leaves=48)
+    jobs = []
+    for d in desc:
+        aln, tree, model = synth.materialize_job(d)
+        jobs.append(serve.Job(id=d['id'], alignment=aln, tree=tree, model=model, f81=(d['kind'] == 'f81'),
+                              want=("logLike", "counts"), arrival=d['arrival']))
+    return jobs
+
+
+def test_results_identical_alone_and_in_the_mix():
+    jobs = _jobs()
+    srv = serve.Server(max_inflight=6, device_budget=1 << 30)
+    done = srv.run(jobs, realtime=False)
+    assert len(done) == len(jobs)
+    assert len({j.id for j in done}) == len(jobs)
+    for j in done:
+        plan = sg.Plan(j.tree, j.model)
+        alone = plan.run(j.alignment, loglike=True, counts=True, f81=j.f81)
+        plan.close()
+        assert_cols(j.result['counts'], alone['counts'], COUNTS_RTOL, f"job {j.id} counts")
+        assert_loglike(j.result['logLike'], alone['logLike'])
+    # oracle spot check on the first columns of three jobs
+    for j in done[:3]:
+        sub = j.alignment[:, :16]
+        t = oracle.Tree(j.tree.parentIndex, j.tree.distanceToParent)
+        md = sg.models.ensure_diag(j.model)._asdict()
+        assert_cols(j.result['counts'][:, :, :16], oracle.Counts(sub, t, md, f81_fast=j.f81),
+                    COUNTS_RTOL, "oracle")
+    stats = serve.latency_stats(done)
+    assert stats['p99_ms'] >= stats['p50_ms'] > 0
+    srv.close()
+
+
+def test_admission_respects_budget_and_slots():
+    jobs = _jobs(n=10, seed=9)
+    srv = serve.Server(max_inflight=3, device_budget=1)   # budget below any job: one at a time
+    peak = []
+    srv.run(jobs, realtime=False, on_admit=lambda j: peak.append(len(srv.inflight)))
+    assert max(peak) == 1
+    srv.close()

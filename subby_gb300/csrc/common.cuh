@@ -97,6 +97,15 @@ int launch_warp(const KParams &p, int A, int grid, int block, size_t smem, cudaS
 int launch_tree(const KParams &p, int A, int store, int grid, int block, size_t smem,
                 cudaStream_t s);
 bool tree_supported(int A);
+// large-alphabet walk + accumulation (k_big.cu)
+bool big_supported(int A);
+int big_tile();
+int big_acc_group(int A);
+// mode: 0 inside pass only (LogLike / RootProb), 1 stage eigen vectors, 2 stage F81 vectors
+int launch_walk(const KParams &p, int A, int mode, float *sa, float *sb, int c_base, int c_count, int grid,
+                cudaStream_t s);
+int launch_acc(const KParams &p, int A, bool f81, const float *sa, const float *sb, int c_base, int c_count,
+               int grid, cudaStream_t s);
 int launch_tree4(const KParams &p, bool f81, int mask_mode, int grid, int block, size_t smem,
                  cudaStream_t s);
 bool small_supported(int A);

@@ -682,9 +682,88 @@ int plan_tree4(subby_plan *P, int mode, int C, Launch &L) {
   return 0;
 }
 
+// Large alphabets (A = 16, 20, 32, 64): k_walk (tree walk, 128 columns per
+// CTA, stored-node slots in global memory) then, for Counts, k_acc over the
+// staged per-branch vectors.  Columns are processed in chunks so that the
+// staging (2 (R-1) A floats per column) stays within kStageBudget bytes.
+constexpr size_t kStageBudget = size_t(1) << 30;
+
+int run_big(subby_plan *P, const int32_t *d_aln, int C, float *d_logL, float *d_counts, float *d_root,
+            int mode, int mask_mode, const uint8_t *d_mask, cudaStream_t stream) {
+  const int A = P->A, R = P->R;
+  KParams k{};
+  k.aln = d_aln;
+  k.C = C;
+  k.R = R;
+  k.A = A;
+  k.nInt = P->nInt;
+  k.mode = mode;
+  k.mask_mode = mask_mode;
+  k.mask = d_mask;
+  k.tab = P->d_tab;
+  k.tab64 = P->d_tab64;
+  k.off = P->off;
+  k.root_is_leaf = P->root_is_leaf;
+  k.f81_mu = P->f81_mu;
+  k.logL = d_logL;
+  k.counts = d_counts;
+  k.rootp = d_root;
+  k.prog = P->d_prog;
+  k.nsteps = P->prog_steps;
+  k.nslots = std::max(P->prog_slots, 1);
+  const int tile = big_tile();
+  const int H = (A + 31) / 32;
+  const bool counts = (mode & kModeCounts) != 0 && R > 1;
+  // chunk of columns (multiple of the tile) bounded by the staging budget
+  int chunk = C;
+  if (counts) {
+    const size_t per_col = (size_t)2 * (R - 1) * A * sizeof(float);
+    size_t cmax = std::max<size_t>(tile, kStageBudget / per_col);
+    cmax = cmax / tile * tile;
+    chunk = (int)std::min<size_t>((size_t)C, cmax);
+  }
+  const int walk_grid = std::max(1, std::min((chunk + tile - 1) / tile, P->nsm * (H == 2 ? 1 : 2)));
+  const size_t slot_floats = (size_t)walk_grid * k.nslots * tile * A;
+  const size_t slot_ints = (size_t)walk_grid * k.nslots * tile;
+  const size_t stage_floats = counts ? (size_t)(R - 1) * chunk * A : 0;
+  auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
+  int rc;
+  if ((rc = P->work.grow(al(slot_floats * 4) + al(slot_ints * 4) + 2 * al(stage_floats * 4) + 256))) return rc;
+  char *base = (char *)P->work.p;
+  k.scrV = (float *)base;
+  base += al(slot_floats * 4);
+  k.scrW = (int *)base;
+  base += al(slot_ints * 4);
+  float *sa = (float *)base;
+  base += al(stage_floats * 4);
+  float *sb = (float *)base;
+  const int wmode = counts ? ((mode & kModeF81) ? 2 : 1) : 0;
+  if (!counts && (mode & kModeCounts)) {
+    // a single-node tree has no branch: counts are zero
+    cudaError_t e = cudaMemsetAsync(d_counts, 0, (size_t)A * A * C * sizeof(float), stream);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync");
+  }
+  for (int c0 = 0; c0 < C; c0 += chunk) {
+    const int cc = std::min(chunk, C - c0);
+    int lr = launch_walk(k, A, wmode, sa, sb, c0, cc, walk_grid, stream);
+    if (lr != 0) return fail(SUBBY_ERR_CUDA, std::string("walk launch failed: ") + cudaGetErrorString((cudaError_t)lr));
+    g_launches += 1;
+    if (counts) {
+      const int G = big_acc_group(A);
+      const int agrid = std::max(1, std::min((cc + G - 1) / G, P->nsm));
+      lr = launch_acc(k, A, (mode & kModeF81) != 0, sa, sb, c0, cc, agrid, stream);
+      if (lr != 0) return fail(SUBBY_ERR_CUDA, std::string("accumulate launch failed: ") + cudaGetErrorString((cudaError_t)lr));
+      g_launches += 1;
+    }
+  }
+  return 0;
+}
+
 int run_common(subby_plan *P, const int32_t *d_aln, int C, float *d_logL, float *d_counts,
                float *d_root, int mode, int mask_mode, const uint8_t *d_mask, const float *d_g,
                double *d_gt, double *d_gC, int *grid_out, cudaStream_t stream) {
+  if (big_supported(P->A) && !(mode & kModeGrad) && g_kernel_sel != 1)
+    return run_big(P, d_aln, C, d_logL, d_counts, d_root, mode, mask_mode, d_mask, stream);
   Launch L;
   const bool tree = tree_supported(P->A) && !(mode & kModeGrad) && g_kernel_sel != 1;
   const bool small = small_supported(P->A);

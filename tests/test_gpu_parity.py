@@ -25,6 +25,14 @@ from subby_gb300 import synth, models, _lib  # noqa: E402
 KERNELS = {"auto": 0, "thread": 1, "tree_smem": 2, "tree_global": 3, "tree_tmem": 4}
 
 
+@pytest.fixture(params=["auto", "thread"])
+def big_kernel(request):
+    """Large alphabets: walk + staged accumulation (auto) or warp per column."""
+    _lib.load().subby_debug_set_kernel(KERNELS[request.param])
+    yield request.param
+    _lib.load().subby_debug_set_kernel(0)
+
+
 @pytest.fixture(params=list(KERNELS))
 def kernel(request):
     """Run a test through every kernel / slot-storage variant for A <= 8."""
@@ -99,8 +107,9 @@ def test_plain_large_subset_hky_and_f81(kernel):
         _check_all(w['alignment'], w['tree'], w['model'], f81=f81)
 
 
-@pytest.mark.parametrize("A,leaves,C", [(16, 12, 40), (20, 9, 33), (32, 6, 20), (64, 10, 24)])
-def test_reversible_larger_alphabets(A, leaves, C):
+@pytest.mark.parametrize("A,leaves,C", [(16, 12, 40), (20, 9, 33), (32, 6, 20), (64, 10, 24), (64, 30, 300),
+                                        (16, 40, 1000)])
+def test_reversible_larger_alphabets(A, leaves, C, big_kernel):
     rng = np.random.default_rng(100 + A)
     m, _, _, _ = models.near_degenerate_reversible(A, rng)
     tree = synth.random_tree(leaves, 0.1, rng)
@@ -108,7 +117,7 @@ def test_reversible_larger_alphabets(A, leaves, C):
     _check_all(aln, tree, m)
 
 
-def test_precision64_subset():
+def test_precision64_subset(big_kernel):
     w = synth.precision64(seed=3, C=48)
     ev = np.sort(np.asarray(w['model'].eigenvalues))
     gaps = np.abs(ev[:, None] - ev[None, :])[np.triu_indices(len(ev), 1)]
@@ -126,7 +135,7 @@ def test_small_alphabets(A, kernel):
     _check_all(aln, tree, base)
 
 
-def test_jc_and_f81_fast_paths_large_alphabet():
+def test_jc_and_f81_fast_paths_large_alphabet(big_kernel):
     rng = np.random.default_rng(7)
     tree = synth.random_tree(14, 0.1, rng)
     for m in (models.jukes_cantor_model(64), models.f81_model(rng.dirichlet(np.ones(20)))):

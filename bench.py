@@ -351,21 +351,37 @@ def precision64_bench(args):
     w = synth.precision64(seed=3, C=C)
     plan = sg.Plan(w['tree'], w['model'])
     d_aln = torch.as_tensor(w['alignment']).cuda()
-    out = {'counts': torch.empty((64, 64, C), dtype=torch.float32, device="cuda"),
-           'logLike': torch.empty(C, dtype=torch.float32, device="cuda")}
-    ms = _time_fn(lambda: plan.run(d_aln, loglike=True, counts=True, branch_mask=None, out=out),
-                  args.steps, args.warmup)
-    launches = _lib.last_launch_count()
     sub = w['alignment'][:, :32]
     md = w['model']._asdict()
     t = oracle.Tree(w['tree'].parentIndex, w['tree'].distanceToParent)
-    err_c = colwise_err(out['counts'][:, :, :32].cpu().numpy(), oracle.Counts(sub, t, md, branch_mask=None))
-    err_l = loglike_err(out['logLike'][:32].cpu().numpy(), oracle.LogLike(sub, t, md))
-    print(json.dumps({"metric": "Counts columns/s (A=64 reversible, R=127, C=65536)", "value": C / (ms / 1e3),
-                      "unit": UNIT, "ms_per_step": ms, "steps": args.steps, "warmup": args.warmup,
-                      "higher_is_better": True, "dtype": "fp32", "kernel": "warp-per-column FP32",
-                      "forced_near_degenerate_pairs": w['forced_pairs'], "gpu_launches": launches * args.steps,
-                      "err_vs_oracle": {"loglike_rel": err_l, "counts_colwise": err_c, "columns": 32}}))
+    ref_c = oracle.Counts(sub, t, md, branch_mask=None)
+    ref_l = oracle.LogLike(sub, t, md)
+    res = {}
+    lib = _lib.load()
+    # 0: tensor-core walk (split-BF16) ; 2: plain FP32 CUDA-core walk
+    for name, sel in (("split_bf16_tensor_core", 0), ("fp32_cuda_core", 2)):
+        lib.subby_debug_set_kernel(sel)
+        out = {'counts': torch.empty((64, 64, C), dtype=torch.float32, device="cuda"),
+               'logLike': torch.empty(C, dtype=torch.float32, device="cuda")}
+        ms = _time_fn(lambda: plan.run(d_aln, loglike=True, counts=True, branch_mask=None, out=out),
+                      args.steps, args.warmup)
+        launches = _lib.last_launch_count()
+        res[name] = {"value": C / (ms / 1e3), "ms_per_step": ms, "gpu_launches": launches * args.steps,
+                     "err_vs_oracle": {"loglike_rel": loglike_err(out['logLike'][:32].cpu().numpy(), ref_l),
+                                       "counts_colwise": colwise_err(out['counts'][:, :, :32].cpu().numpy(), ref_c),
+                                       "columns": 32}}
+        # LogLike alone (inside pass only)
+        ll = {'logLike': out['logLike']}
+        ms_ll = _time_fn(lambda: plan.run(d_aln, loglike=True, out=ll), args.steps, args.warmup)
+        res[name]["loglike_only_columns_per_s"] = C / (ms_ll / 1e3)
+    lib.subby_debug_set_kernel(0)
+    tc, fp = res["split_bf16_tensor_core"], res["fp32_cuda_core"]
+    print(json.dumps({"metric": "Counts columns/s (A=64 reversible, R=127, C=65536)", "value": tc["value"],
+                      "unit": UNIT, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
+                      "dtype": "fp32 (split-bf16 tensor-core products)", "forced_near_degenerate_pairs": w['forced_pairs'],
+                      "tensor_core_vs_fp32_speedup": tc["value"] / fp["value"],
+                      "loglike_tensor_core_vs_fp32_speedup": tc["loglike_only_columns_per_s"] / fp["loglike_only_columns_per_s"],
+                      "variants": res}))
     return 0
 
 

@@ -164,12 +164,13 @@ int subby_counts_noalloc(const int32_t *alignment, const int32_t *parent_index,
                          const uint8_t *mask, float *counts, float *logLike,
                          void *stream);
 
-/* Test hook selecting the kernel for alphabets A <= 8 so that every code
- * path can be checked against the oracle: 0 automatic (A = 4 tree kernel
- * with tensor-memory slots when it fits), 1 thread-per-column kernel, 2
- * tree program with shared-memory slots, 3 tree program with global-memory
- * slots, 4 generic tree program with tensor-memory slots.  No reference
- * counterpart. */
+/* Test hook selecting the kernel so that every code path can be checked
+ * against the oracle: 0 automatic (A = 4 tree kernel with tensor-memory
+ * slots when it fits; A = 64 tree walk on the tensor cores), 1
+ * thread-per-column kernel (A <= 8) / warp-per-column kernel (larger A), 2
+ * tree program with shared-memory slots (A <= 8) / FP32 CUDA-core tree walk
+ * (larger A), 3 tree program with global-memory slots, 4 generic tree
+ * program with tensor-memory slots.  No reference counterpart. */
 int subby_debug_set_kernel(int which);
 
 /* Number of kernel launches the most recent subby_plan_run /

@@ -88,6 +88,11 @@ struct KParams {
   int nsteps;
   int nslots;
   int smem_words;         // sofs of the slot words (k_tree, shared-memory slots)
+  // tensor-core walk (A = 64): BF16 hi/lo operand tiles in the canonical
+  // K-major layout; per node n at n*16384: [M hi | M lo | M^T hi | M^T lo]
+  // (4096 elements each), then [Vd^T hi | lo | Vu^T hi | lo] at R*16384
+  const uint16_t *tab16;
+  int *err;               // device status: bounded waits that gave up (tensor-core walk)
 };
 
 // launchers (k_small.cu / k_warp.cu)
@@ -102,8 +107,8 @@ bool big_supported(int A);
 int big_tile();
 int big_acc_group(int A);
 // mode: 0 inside pass only (LogLike / RootProb), 1 stage eigen vectors, 2 stage F81 vectors
-int launch_walk(const KParams &p, int A, int mode, float *sa, float *sb, int c_base, int c_count, int grid,
-                cudaStream_t s);
+int launch_walk(const KParams &p, int A, int mode, bool tc, float *sa, float *sb, int c_base, int c_count,
+                int grid, cudaStream_t s);
 int launch_acc(const KParams &p, int A, bool f81, const float *sa, const float *sb, int c_base, int c_count,
                int grid, cudaStream_t s);
 int launch_tree4(const KParams &p, bool f81, int mask_mode, int grid, int block, size_t smem,

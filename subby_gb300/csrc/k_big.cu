@@ -20,6 +20,8 @@
 // F81 rank-3 terms — with 4 x 4 (k, l) register blocks, J rows and staged
 // vectors double-buffered through shared memory, then back-transforms
 // V C V^T (oracle.py:1087-1137) through shared memory and writes counts.
+#include <cuda_bf16.h>
+
 #include "common.cuh"
 
 namespace subby {
@@ -48,6 +50,44 @@ __device__ __forceinline__ void pair_sync(int warp) {
   asm volatile("bar.sync %0, 64;" ::"r"(1 + (warp & 3)) : "memory");
 }
 
+// ---- tensor-core (tcgen05) helpers for the A = 64 walk -------------------
+// Operands use the canonical K-major layout without swizzle: element (r, k)
+// of a tile with K = 64 sits at byte (r&7)*16 + (r>>3)*1024 + (k&7)*2 +
+// (k>>3)*128 (8 x 16-byte core matrices; 128 B between K-adjacent and
+// 1024 B between M/N-adjacent core matrices).
+__device__ __forceinline__ uint32_t kmaj_off(int r, int k) {
+  return (uint32_t)((r & 7) * 16 + (r >> 3) * 1024 + (k & 7) * 2 + (k >> 3) * 128);
+}
+__device__ __forceinline__ uint64_t umma_desc(uint32_t saddr) {
+  return (uint64_t)((saddr >> 4) & 0x3FFF) | ((uint64_t)(128 >> 4) << 16) | ((uint64_t)(1024 >> 4) << 32) |
+         ((uint64_t)1 << 46);
+}
+// kind::f16, BF16 x BF16 -> F32, K-major A and B, M = 128, N = 64
+constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(64 >> 3) << 17) |
+                            ((uint32_t)(128 >> 4) << 24);
+constexpr int kWaitLimit = 1 << 24;  // bounded mbarrier waits
+
+__device__ __forceinline__ bool mbar_wait(uint32_t mb, uint32_t phase) {
+  for (int it = 0; it < kWaitLimit; ++it) {
+    uint32_t done;
+    asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+                 : "=r"(done)
+                 : "r"(mb), "r"(phase)
+                 : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+
+struct TcState {
+  uint32_t tmem;    // accumulator: 128 lanes x 64 fp32 columns
+  uint32_t sA;      // A operand hi (16 KB) then lo (16 KB), shared address
+  uint32_t sB;      // B operand hi (8 KB) then lo (8 KB)
+  uint32_t mbB, mbM;
+  uint32_t nmv;     // matvecs issued (mbarrier phase)
+  int *err;         // shared: set when a bounded wait gives up
+};
+
 template <int A>
 struct Walk {
   static constexpr int H = Geo<A>::H;
@@ -55,6 +95,82 @@ struct Walk {
   int c, h, warp;
   float *xch;     // shared exchange buffer: [2][32 states][128 cols] floats
   int *xmax;      // shared [2][128] ints (exponent-field exchange)
+  TcState tcs;    // tensor-core state (per thread copy; used when use_tc)
+  bool use_tc;
+
+  // y = (B x) on the tensor cores for the 128 columns of the tile at once:
+  // D[c][b] = sum_j X[c][j] B[b][j] with X, B split into BF16 hi + lo and
+  // three MMAs (hi.hi + hi.lo + lo.hi) accumulating in FP32 in TMEM.
+  // Bg: the B tile (hi block, lo block 4096 elements later) in the canonical
+  // layout in global memory, brought in by one bulk copy per half.
+  __device__ __forceinline__ void matvec_tc(BV<A> &y, const BV<A> &x, const uint16_t *Bg) {
+    static_assert(A == 64, "tensor-core walk is A = 64");
+    TcState &T = tcs;
+    const uint32_t phase = T.nmv & 1;
+    if (threadIdx.x == 0) {
+      asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(T.mbB), "r"(16384) : "memory");
+      asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                   ::"r"(T.sB), "l"(Bg), "r"(8192), "r"(T.mbB) : "memory");
+      asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                   ::"r"(T.sB + 8192), "l"(Bg + 4096), "r"(8192), "r"(T.mbB) : "memory");
+    }
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      uint32_t hi[4], lo[4];
+#pragma unroll
+      for (int pp = 0; pp < 4; ++pp) {
+        const float a0 = x.v[8 * q + 2 * pp], a1 = x.v[8 * q + 2 * pp + 1];
+        const __nv_bfloat162 hh = __floats2bfloat162_rn(a0, a1);
+        const float2 hf = __bfloat1622float2(hh);
+        const __nv_bfloat162 ll = __floats2bfloat162_rn(a0 - hf.x, a1 - hf.y);
+        hi[pp] = *reinterpret_cast<const uint32_t *>(&hh);
+        lo[pp] = *reinterpret_cast<const uint32_t *>(&ll);
+      }
+      const uint32_t off = kmaj_off(c, 32 * h + 8 * q);
+      asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};" ::"r"(T.sA + off), "r"(hi[0]), "r"(hi[1]), "r"(hi[2]),
+                   "r"(hi[3]) : "memory");
+      asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};" ::"r"(T.sA + 16384 + off), "r"(lo[0]), "r"(lo[1]),
+                   "r"(lo[2]), "r"(lo[3]) : "memory");
+    }
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    if (threadIdx.x == 0) {
+      if (!mbar_wait(T.mbB, phase)) *T.err = 1;
+#pragma unroll
+      for (int ks = 0; ks < 4; ++ks) {
+#pragma unroll
+        for (int prod = 0; prod < 3; ++prod) {
+          const uint32_t a = T.sA + (prod == 2 ? 16384 : 0) + ks * 256;
+          const uint32_t b = T.sB + (prod == 1 ? 8192 : 0) + ks * 256;
+          const uint32_t accum = (ks | prod) != 0;
+          asm volatile("{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+                       " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}"
+                       ::"r"(T.tmem), "l"(umma_desc(a)), "l"(umma_desc(b)), "r"(kIdesc), "r"(accum) : "memory");
+        }
+      }
+      asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(T.mbM)
+                   : "memory");
+    }
+    if (!mbar_wait(T.mbM, phase)) *T.err = 1;
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    uint32_t r[32];
+    const uint32_t ta = T.tmem + ((uint32_t)(32 * (warp & 3)) << 16) + 32u * h;
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+                 "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+                   "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]),
+                   "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]),
+                   "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]),
+                   "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+                 : "r"(ta)
+                 : "memory");
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < 32; ++i) y.v[i] = __uint_as_float(r[i]);
+    T.nmv += 1;
+  }
 
   __device__ __forceinline__ void ld(BV<A> &o, const float *p) const {  // S contiguous floats
 #pragma unroll
@@ -100,8 +216,16 @@ struct Walk {
     for (int i = 0; i < S; ++i) x.v[i] *= s;
     return E - 127;
   }
-  // y_b = sum_j T[j][b] x_j over all A inputs j (T rows contiguous, stride A)
-  __device__ __forceinline__ void matvec(BV<A> &y, const BV<A> &x, const float *__restrict__ T) const {
+  // y_b = sum_j T[j][b] x_j over all A inputs j (T rows contiguous, stride A);
+  // on the tensor cores when enabled, with Bg the same product's B tile.
+  __device__ __forceinline__ void matvec(BV<A> &y, const BV<A> &x, const float *__restrict__ T,
+                                         const uint16_t *Bg = nullptr) {
+    if constexpr (A == 64) {
+      if (use_tc) {
+        matvec_tc(y, x, Bg);
+        return;
+      }
+    }
     if constexpr (H == 1) {
 #pragma unroll
       for (int i = 0; i < S; ++i) y.v[i] = 0.f;
@@ -154,14 +278,50 @@ struct BN {
   int e, hh, init, code;
 };
 
-template <int A, int MODE>  // MODE: 0 inside only, 1 eigen staging, 2 F81 staging
+template <int A, int MODE, bool TC>  // MODE: 0 inside only, 1 eigen staging, 2 F81 staging
 __global__ void __launch_bounds__(128 * Geo<A>::H, 1) k_walk(const KParams P, float *__restrict__ stage_a,
                                                               float *__restrict__ stage_b, int c_base,
                                                               int c_count) {
   constexpr int S = Geo<A>::S;
-  __shared__ __align__(16) float s_xch[Geo<A>::H == 2 ? 2 * 32 * kTile : 4];
+  __shared__ __align__(16) float s_xch[(Geo<A>::H == 2 && !TC) ? 2 * 32 * kTile : 2 * kTile];
   __shared__ int s_xmax[2 * kTile];
   Walk<A> wk;
+  wk.use_tc = TC;
+  __shared__ TcState s_tc;
+  __shared__ __align__(8) uint64_t s_mbar[2];
+  __shared__ uint32_t s_taddr;
+  __shared__ int s_err;
+  extern __shared__ __align__(1024) unsigned char s_dyn[];  // TC: A (32 KB) + B (16 KB) operands
+  if constexpr (TC) {
+    if ((threadIdx.x >> 5) == 0) {
+      const uint32_t dst = (uint32_t)__cvta_generic_to_shared(&s_taddr);
+      asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(dst), "r"(64)
+                   : "memory");
+      asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    if (threadIdx.x == 0) {
+      s_err = 0;
+      for (int i = 0; i < 2; ++i) {
+        const uint32_t mb = (uint32_t)__cvta_generic_to_shared(&s_mbar[i]);
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mb) : "memory");
+      }
+      asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    if (threadIdx.x == 0) {
+      s_tc.tmem = s_taddr;
+      s_tc.sA = (uint32_t)__cvta_generic_to_shared(s_dyn);
+      s_tc.sB = s_tc.sA + 32768;
+      s_tc.mbB = (uint32_t)__cvta_generic_to_shared(&s_mbar[0]);
+      s_tc.mbM = (uint32_t)__cvta_generic_to_shared(&s_mbar[1]);
+      s_tc.nmv = 0;
+      s_tc.err = &s_err;
+    }
+    __syncthreads();
+    wk.tcs = s_tc;
+  }
   wk.warp = threadIdx.x >> 5;
   const int lane = threadIdx.x & 31;
   wk.c = lane + 32 * (wk.warp & 3);
@@ -221,7 +381,7 @@ __global__ void __launch_bounds__(128 * Geo<A>::H, 1) k_walk(const KParams P, fl
       o.hh = k0.hh | k1.hh;
       o.init = k0.hh & k1.hh;
       o.code = -1;
-      wk.matvec(o.cc, u, MT + (size_t)n * (A + 1) * A);
+      wk.matvec(o.cc, u, MT + (size_t)n * (A + 1) * A, P.tab16 + (size_t)n * 16384);
     };
 
     // ---------------------------------------------------------------- inside
@@ -255,7 +415,7 @@ __global__ void __launch_bounds__(128 * Geo<A>::H, 1) k_walk(const KParams P, fl
         iRoot = init;
       } else {
         BV<A> cc;
-        wk.matvec(cc, u, MT + (size_t)s0.x * (A + 1) * A);
+        wk.matvec(cc, u, MT + (size_t)s0.x * (A + 1) * A, P.tab16 + (size_t)s0.x * 16384);
         wk.st(slotv(s0.y), cc);
         if (h == 0) slotw(s0.y) = (eU << 2) | (hh << 1) | init;
       }
@@ -300,9 +460,9 @@ __global__ void __launch_bounds__(128 * Geo<A>::H, 1) k_walk(const KParams P, fl
       BV<A> Ds, dt, ut;
 #pragma unroll
       for (int q = 0; q < S; ++q) Ds.v[q] = D.v[q] * s;
-      wk.matvec(dt, Ds, Vd);
+      wk.matvec(dt, Ds, Vd, P.tab16 + (size_t)P.R * 16384);
       if (leafcode >= 0) wk.ld(ut, Ut + leafcode * A + 32 * h);
-      else wk.matvec(ut, U, Vu);
+      else wk.matvec(ut, U, Vu, P.tab16 + (size_t)P.R * 16384 + 8192);
       if (valid) {
         wk.st(pa, dt);
         wk.st(pb, ut);
@@ -315,13 +475,18 @@ __global__ void __launch_bounds__(128 * Geo<A>::H, 1) k_walk(const KParams P, fl
     };
     for (int i = P.nsteps - 1; i >= 0; --i) {
       const int4 s0 = prog[4 * i], s1 = prog[4 * i + 1], s2 = prog[4 * i + 2], s3 = prog[4 * i + 3];
-      BN<A> nl, nr, k[4];
-      BV<A> du[2];
-      int dcode[2] = {-1, -1};
-      if (s1.y == -2) derive(nl, du[0], k[0], k[1], dcode[0], s1.x, s1, s3.x, s3.y);
-      else basic(nl, s1.x, s1.y);
-      if (s2.y == -2) derive(nr, du[1], k[2], k[3], dcode[1], s2.x, s2, s3.z, s3.w);
-      else basic(nr, s2.x, s2.y);
+      BN<A> nl, nr;
+      {
+        // derived children's U and children are recomputed when they are
+        // processed below instead of being held here (register pressure)
+        BV<A> u;
+        BN<A> k0, k1;
+        int cd;
+        if (s1.y == -2) derive(nl, u, k0, k1, cd, s1.x, s1, s3.x, s3.y);
+        else basic(nl, s1.x, s1.y);
+        if (s2.y == -2) derive(nr, u, k0, k1, cd, s2.x, s2, s3.z, s3.w);
+        else basic(nr, s2.x, s2.y);
+      }
       const int codep = btcode(tok(s0.x), A);
       BV<A> O;
       int eO, stp;
@@ -342,7 +507,7 @@ __global__ void __launch_bounds__(128 * Geo<A>::H, 1) k_walk(const KParams P, fl
         wk.obs(U, codep);
         const int eUp = nl.e + nr.e + wk.rescale(U);
         emit(s0.x, D, U, -1, eD + eUp, actp);
-        wk.matvec(O, D, MN + (size_t)s0.x * A * A);
+        wk.matvec(O, D, MN + (size_t)s0.x * A * A, P.tab16 + (size_t)s0.x * 16384 + 8192);
         wk.obs(O, codep);
         eO = eD + wk.rescale(O);
       }
@@ -367,17 +532,28 @@ __global__ void __launch_bounds__(128 * Geo<A>::H, 1) k_walk(const KParams P, fl
           wk.st(slotv(sc.y), Dc);
           if (h == 0) slotw(sc.y) = (eDc << 2) | (stc << 1) | actc;
         } else {
-          emit(sc.x, Dc, du[side], -1, eDc + me.e, actc);
-          BV<A> Oc;
-          wk.matvec(Oc, Dc, MN + (size_t)sc.x * A * A);
-          wk.obs(Oc, dcode[side]);
-          const int eOc = eDc + wk.rescale(Oc);
           const int gks[2] = {side ? s3.z : s3.x, side ? s3.w : s3.y};
           const int gn[2] = {sc.z, sc.w};
+          BN<A> kk[2];
+          basic(kk[0], gn[0], gks[0]);
+          basic(kk[1], gn[1], gks[1]);
+          const int dcode = btcode(tok(sc.x), A);
+          {
+            BV<A> du;
+#pragma unroll
+            for (int q = 0; q < S; ++q) du.v[q] = kk[0].cc.v[q] * kk[1].cc.v[q];
+            wk.obs(du, dcode);
+            wk.rescale(du);  // same exponent as in the gather: eU_c = me.e
+            emit(sc.x, Dc, du, -1, eDc + me.e, actc);
+          }
+          BV<A> Oc;
+          wk.matvec(Oc, Dc, MN + (size_t)sc.x * A * A, P.tab16 + (size_t)sc.x * 16384 + 8192);
+          wk.obs(Oc, dcode);
+          const int eOc = eDc + wk.rescale(Oc);
 #pragma unroll
           for (int gs = 0; gs < 2; ++gs) {
-            const BN<A> &g = k[2 * side + gs];
-            const BN<A> &gsib = k[2 * side + 1 - gs];
+            const BN<A> &g = kk[gs];
+            const BN<A> &gsib = kk[1 - gs];
             BV<A> Dg;
 #pragma unroll
             for (int q = 0; q < S; ++q) Dg.v[q] = Oc.v[q] * gsib.cc.v[q];
@@ -397,6 +573,14 @@ __global__ void __launch_bounds__(128 * Geo<A>::H, 1) k_walk(const KParams P, fl
         }
       }
     }
+  }
+  if constexpr (TC) {
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    if ((threadIdx.x >> 5) == 0)
+      asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(wk.tcs.tmem), "r"(64) : "memory");
+    if (threadIdx.x == 0 && s_err && P.err) atomicAdd(P.err, 1);
   }
 }
 
@@ -448,27 +632,36 @@ __global__ void __launch_bounds__(256, 1) k_acc(const KParams P, const float *__
 #pragma unroll
       for (int q = 0; q < 8; ++q) zv[q] = 0.f;
     }
+    // J_n (eigen) and the staged vectors of branch n for this group's columns,
+    // copied asynchronously (cp.async, 16 B; out-of-range columns zero-filled)
+    auto cp16 = [](float *dst, const float *src, bool in) {
+      const uint32_t d = (uint32_t)__cvta_generic_to_shared(dst);
+      asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(d), "l"(src), "r"(in ? 16 : 0)
+                   : "memory");
+    };
     auto load = [&](int n, float *dst) {
-      // J_n (eigen) and the staged vectors of branch n for this group's columns
       if (!F81)
-        for (int i = t; i < A * A / 4; i += blockDim.x)
-          reinterpret_cast<float4 *>(dst)[i] = __ldg(reinterpret_cast<const float4 *>(J + (size_t)(n + 1) * A * A) + i);
+        for (int i = t; i < A * A / 4; i += blockDim.x) cp16(dst + 4 * i, J + (size_t)(n + 1) * A * A + 4 * i, true);
       const size_t off = ((size_t)n * c_count + g0) * A;
       float *da = dst + A * A, *db = dst + A * A + G * A;
       for (int i = t; i < G * A / 4; i += blockDim.x) {
         const bool in = i * 4 < gcols * A;
-        reinterpret_cast<float4 *>(da)[i] = in ? __ldg(reinterpret_cast<const float4 *>(stage_a + off) + i)
-                                              : make_float4(0.f, 0.f, 0.f, 0.f);
-        reinterpret_cast<float4 *>(db)[i] = in ? __ldg(reinterpret_cast<const float4 *>(stage_b + off) + i)
-                                              : make_float4(0.f, 0.f, 0.f, 0.f);
+        cp16(da + 4 * i, stage_a + off + (in ? 4 * i : 0), in);
+        cp16(db + 4 * i, stage_b + off + (in ? 4 * i : 0), in);
       }
+      asm volatile("cp.async.commit_group;" ::: "memory");
     };
     load(0, buf[0]);
-    __syncthreads();
     float *scal = sm + 2 * (A * A + 2 * G * A);  // F81: piU, Dsum per column
     for (int n = 0; n < nbr; ++n) {
       float *cur = buf[n & 1];
-      if (n + 1 < nbr) load(n + 1, buf[(n + 1) & 1]);
+      if (n + 1 < nbr) {
+        load(n + 1, buf[(n + 1) & 1]);
+        asm volatile("cp.async.wait_group 1;" ::: "memory");
+      } else {
+        asm volatile("cp.async.wait_group 0;" ::: "memory");
+      }
+      __syncthreads();
       if (F81) {
         if (t < G) {
           const float *Ds = cur + A * A + t * A, *U = cur + A * A + G * A + t * A;
@@ -648,14 +841,31 @@ __global__ void __launch_bounds__(256, 1) k_acc(const KParams P, const float *__
   }
 }
 
-template <int A>
-int walk_launch(const KParams &p, int mode, float *sa, float *sb, int c_base, int c_count, int grid,
-                cudaStream_t s) {
+template <int A, int MODE, bool TC>
+int walk_launch1(const KParams &p, float *sa, float *sb, int c_base, int c_count, int grid, cudaStream_t s) {
   const int threads = 128 * Geo<A>::H;
-  if (mode == 0) k_walk<A, 0><<<grid, threads, 0, s>>>(p, sa, sb, c_base, c_count);
-  else if (mode == 1) k_walk<A, 1><<<grid, threads, 0, s>>>(p, sa, sb, c_base, c_count);
-  else k_walk<A, 2><<<grid, threads, 0, s>>>(p, sa, sb, c_base, c_count);
+  const size_t dyn = TC ? 48 * 1024 + 1024 : 0;
+  if (TC) {
+    cudaError_t e = cudaFuncSetAttribute(k_walk<A, MODE, TC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
+    if (e != cudaSuccess) return (int)e;
+  }
+  k_walk<A, MODE, TC><<<grid, threads, dyn, s>>>(p, sa, sb, c_base, c_count);
   return (int)cudaGetLastError();
+}
+
+template <int A>
+int walk_launch(const KParams &p, int mode, bool tc, float *sa, float *sb, int c_base, int c_count, int grid,
+                cudaStream_t s) {
+  if constexpr (A == 64) {
+    if (tc) {
+      if (mode == 0) return walk_launch1<A, 0, true>(p, sa, sb, c_base, c_count, grid, s);
+      if (mode == 1) return walk_launch1<A, 1, true>(p, sa, sb, c_base, c_count, grid, s);
+      return walk_launch1<A, 2, true>(p, sa, sb, c_base, c_count, grid, s);
+    }
+  }
+  if (mode == 0) return walk_launch1<A, 0, false>(p, sa, sb, c_base, c_count, grid, s);
+  if (mode == 1) return walk_launch1<A, 1, false>(p, sa, sb, c_base, c_count, grid, s);
+  return walk_launch1<A, 2, false>(p, sa, sb, c_base, c_count, grid, s);
 }
 
 template <int A>
@@ -692,13 +902,13 @@ int big_acc_group(int A) {
   }
 }
 
-int launch_walk(const KParams &p, int A, int mode, float *sa, float *sb, int c_base, int c_count, int grid,
-                cudaStream_t s) {
+int launch_walk(const KParams &p, int A, int mode, bool tc, float *sa, float *sb, int c_base, int c_count,
+                int grid, cudaStream_t s) {
   switch (A) {
-    case 16: return walk_launch<16>(p, mode, sa, sb, c_base, c_count, grid, s);
-    case 20: return walk_launch<20>(p, mode, sa, sb, c_base, c_count, grid, s);
-    case 32: return walk_launch<32>(p, mode, sa, sb, c_base, c_count, grid, s);
-    case 64: return walk_launch<64>(p, mode, sa, sb, c_base, c_count, grid, s);
+    case 16: return walk_launch<16>(p, mode, false, sa, sb, c_base, c_count, grid, s);
+    case 20: return walk_launch<20>(p, mode, false, sa, sb, c_base, c_count, grid, s);
+    case 32: return walk_launch<32>(p, mode, false, sa, sb, c_base, c_count, grid, s);
+    case 64: return walk_launch<64>(p, mode, tc, sa, sb, c_base, c_count, grid, s);
     default: return -1;
   }
 }

@@ -11,6 +11,8 @@
 #include <string>
 #include <vector>
 
+#include <cuda_bf16.h>
+
 #include "common.cuh"
 #include "subby_gb300.h"
 
@@ -21,9 +23,10 @@ namespace {
 thread_local std::string g_last_error;
 thread_local int g_launches = 0;
 // Test hook (subby_debug_set_kernel): 0 automatic, 1 thread-per-column
-// kernel (k_small) for A <= 8, 2 tree program with shared-memory slots,
-// 3 tree program with global-memory slots, 4 generic tree program with
-// tensor-memory slots (bypassing the A = 4 specialisation).
+// kernel (k_small) for A <= 8 / warp-per-column kernel (k_warp) above, 2
+// tree program with shared-memory slots / FP32 CUDA-core walk (no tensor
+// cores) for large A, 3 tree program with global-memory slots, 4 generic
+// tree program with tensor-memory slots (bypassing the A = 4 specialisation).
 int g_kernel_sel = 0;
 
 int fail(int code, const std::string &msg) {
@@ -101,6 +104,34 @@ __global__ void k_compute_M(const double *__restrict__ V, const double *__restri
   }
 }
 
+// BF16 hi/lo operand tiles (A = 64) for the tensor-core walk, in the
+// canonical K-major layout without swizzle (element (r, k) at byte
+// (r&7)*16 + (r>>3)*1024 + (k&7)*2 + (k>>3)*128 of a 64 x 64 tile):
+// per node n, B = M_n (rows b, K = j) and B = M_n^T (rows a, K = i); then
+// Vd^T and Vu^T.  hi = bf16(v), lo = bf16(v - hi).
+__global__ void k_pack16(const float *__restrict__ MN, const float *__restrict__ Vd, const float *__restrict__ Vu,
+                         int R, uint16_t *__restrict__ out) {
+  const int ntiles = 2 * R + 2;
+  const int total = ntiles * 4096;
+  for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < total; idx += gridDim.x * blockDim.x) {
+    const int tile = idx / 4096, e = idx % 4096, r = e / 64, k = e % 64;
+    float v;
+    if (tile < 2 * R) {
+      const int n = tile / 2;
+      v = (tile & 1) ? MN[(size_t)n * 4096 + k * 64 + r] : MN[(size_t)n * 4096 + r * 64 + k];
+    } else {
+      const float *Vt = (tile == 2 * R) ? Vd : Vu;
+      v = Vt[k * 64 + r];  // B[r][k] = V[k][r]
+    }
+    const __nv_bfloat16 hi = __float2bfloat16_rn(v);
+    const __nv_bfloat16 lo = __float2bfloat16_rn(v - __bfloat162float(hi));
+    const size_t base = (size_t)tile * 8192;  // elements: hi 4096 then lo 4096
+    const int off = ((r & 7) * 16 + (r >> 3) * 1024 + (k & 7) * 2 + (k >> 3) * 128) / 2;
+    out[base + off] = __bfloat16_as_ushort(hi);
+    out[base + 4096 + off] = __bfloat16_as_ushort(lo);
+  }
+}
+
 // Leaf-branch weights K_n[code][k][l] = J_n[k][l] U~(code)_l (A <= 8; row
 // stride A*A + 4), so
 // that a leaf branch's J-weighted outer product needs one multiply per entry.
@@ -164,6 +195,8 @@ struct subby_plan {
   TableOffsets off{};
   float *d_tab = nullptr;
   double *d_tab64 = nullptr;
+  uint16_t *d_tab16 = nullptr;   // A = 64: BF16 hi/lo operand tiles of the tensor-core walk
+  int *d_err = nullptr;          // device status word (bounded waits that gave up)
   int4 *d_steps = nullptr, *d_slots = nullptr;
   size_t tab_bytes = 0;
   DevBuf work;     // scratch + gradient partials
@@ -451,6 +484,17 @@ int subby_plan_create(const int32_t *parent, const double *dist, const double *e
                                                                          P->d_tab + o.K);
       e = cudaGetLastError();
     }
+    if (e == cudaSuccess && A == 64) {
+      e = cudaMalloc(&P->d_tab16, sizeof(uint16_t) * (size_t)(2 * R + 2) * 8192);
+      if (e == cudaSuccess) {
+        const int tt = (2 * R + 2) * 4096;
+        k_pack16<<<std::max(1, std::min((tt + 255) / 256, 8192)), 256>>>(P->d_tab + o.MN, P->d_tab + o.Vd,
+                                                                         P->d_tab + o.Vu, R, P->d_tab16);
+        e = cudaGetLastError();
+      }
+    }
+    if (e == cudaSuccess) e = cudaMalloc(&P->d_err, sizeof(int));
+    if (e == cudaSuccess) e = cudaMemset(P->d_err, 0, sizeof(int));
     if (e == cudaSuccess) e = cudaDeviceSynchronize();
     if (e != cudaSuccess) return cleanup(cuda_fail(e, "J(t) prologue"));
   }
@@ -465,6 +509,8 @@ int subby_plan_destroy(subby_plan *P) {
   if (P->d_steps) cudaFree(P->d_steps);
   if (P->d_slots) cudaFree(P->d_slots);
   if (P->d_prog) cudaFree(P->d_prog);
+  if (P->d_tab16) cudaFree(P->d_tab16);
+  if (P->d_err) cudaFree(P->d_err);
   P->work.release();
   P->io.release();
   delete P;
@@ -711,6 +757,9 @@ int run_big(subby_plan *P, const int32_t *d_aln, int C, float *d_logL, float *d_
   k.prog = P->d_prog;
   k.nsteps = P->prog_steps;
   k.nslots = std::max(P->prog_slots, 1);
+  k.tab16 = P->d_tab16;
+  k.err = P->d_err;
+  const bool tc = (A == 64) && P->d_tab16 && g_kernel_sel == 0;
   const int tile = big_tile();
   const int H = (A + 31) / 32;
   const bool counts = (mode & kModeCounts) != 0 && R > 1;
@@ -745,7 +794,7 @@ int run_big(subby_plan *P, const int32_t *d_aln, int C, float *d_logL, float *d_
   }
   for (int c0 = 0; c0 < C; c0 += chunk) {
     const int cc = std::min(chunk, C - c0);
-    int lr = launch_walk(k, A, wmode, sa, sb, c0, cc, walk_grid, stream);
+    int lr = launch_walk(k, A, wmode, tc, sa, sb, c0, cc, walk_grid, stream);
     if (lr != 0) return fail(SUBBY_ERR_CUDA, std::string("walk launch failed: ") + cudaGetErrorString((cudaError_t)lr));
     g_launches += 1;
     if (counts) {
@@ -883,6 +932,14 @@ int subby_plan_run(subby_plan *P, const int32_t *aln, int C, float *logL, float 
   if (b_ct) CU(cudaMemcpyAsync(counts, d_ct, b_ct, cudaMemcpyDeviceToHost, stream));
   if (b_rp) CU(cudaMemcpyAsync(rootProb, d_rp, b_rp, cudaMemcpyDeviceToHost, stream));
   CU(cudaStreamSynchronize(stream));
+  if (P->d_err) {
+    int dev_err = 0;
+    CU(cudaMemcpy(&dev_err, P->d_err, sizeof(int), cudaMemcpyDeviceToHost));
+    if (dev_err) {
+      cudaMemset(P->d_err, 0, sizeof(int));
+      return fail(SUBBY_ERR_TIMEOUT, "a bounded device wait gave up (tensor-core walk)");
+    }
+  }
   if (dev != P->device) cudaSetDevice(dev);
   return SUBBY_OK;
 }

@@ -25,9 +25,10 @@ from subby_gb300 import synth, models, _lib  # noqa: E402
 KERNELS = {"auto": 0, "thread": 1, "tree_smem": 2, "tree_global": 3, "tree_tmem": 4}
 
 
-@pytest.fixture(params=["auto", "thread"])
+@pytest.fixture(params=["auto", "thread", "tree_smem"])
 def big_kernel(request):
-    """Large alphabets: walk + staged accumulation (auto) or warp per column."""
+    """Large alphabets: tree walk + staged accumulation (auto: tensor cores
+    at A = 64), warp per column (thread), FP32 CUDA-core walk (tree_smem)."""
     _lib.load().subby_debug_set_kernel(KERNELS[request.param])
     yield request.param
     _lib.load().subby_debug_set_kernel(0)

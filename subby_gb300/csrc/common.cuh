@@ -88,9 +88,9 @@ struct KParams {
   int nsteps;
   int nslots;
   int smem_words;         // sofs of the slot words (k_tree, shared-memory slots)
-  // tensor-core walk (A = 64): BF16 hi/lo operand tiles in the canonical
-  // K-major layout; per node n at n*16384: [M hi | M lo | M^T hi | M^T lo]
-  // (4096 elements each), then [Vd^T hi | lo | Vu^T hi | lo] at R*16384
+  // tensor-core walk (A = 64): three-term BF16 operand tiles in the
+  // canonical K-major layout; per node n at n*24576: [M 1|2|3 | M^T 1|2|3]
+  // (4096 elements each), then [Vd^T 1|2|3 | Vu^T 1|2|3] at R*24576
   const uint16_t *tab16;
   int *err;               // device status: bounded waits that gave up (tensor-core walk)
 };

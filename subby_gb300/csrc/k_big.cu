@@ -81,8 +81,8 @@ __device__ __forceinline__ bool mbar_wait(uint32_t mb, uint32_t phase) {
 
 struct TcState {
   uint32_t tmem;    // accumulator: 128 lanes x 64 fp32 columns
-  uint32_t sA;      // A operand hi (16 KB) then lo (16 KB), shared address
-  uint32_t sB;      // B operand hi (8 KB) then lo (8 KB)
+  uint32_t sA;      // A operand: three BF16 terms of 16 KB each, shared address
+  uint32_t sB;      // B operand: three BF16 terms of 8 KB each
   uint32_t mbB, mbM;
   uint32_t nmv;     // matvecs issued (mbarrier phase)
   int *err;         // shared: set when a bounded wait gives up
@@ -99,38 +99,47 @@ struct Walk {
   bool use_tc;
 
   // y = (B x) on the tensor cores for the 128 columns of the tile at once:
-  // D[c][b] = sum_j X[c][j] B[b][j] with X, B split into BF16 hi + lo and
-  // three MMAs (hi.hi + hi.lo + lo.hi) accumulating in FP32 in TMEM.
-  // Bg: the B tile (hi block, lo block 4096 elements later) in the canonical
-  // layout in global memory, brought in by one bulk copy per half.
+  // D[c][b] = sum_j X[c][j] B[b][j].  X and B are each split into three
+  // BF16 terms (v = v1 + v2 + v3, v2 = bf16(v - v1), v3 = bf16(v - v1 - v2))
+  // and the six products with combined order <= 4 (1.1, 1.2, 2.1, 1.3, 2.2,
+  // 3.1) accumulate in FP32 in TMEM, which keeps FP32-level accuracy (the
+  // two-term split measured 1.5e-4 column-wise counts error at A = 64).
+  // Bg: the B tile's three terms (4096 elements each) in the canonical
+  // layout in global memory, brought in by bulk copies.
   __device__ __forceinline__ void matvec_tc(BV<A> &y, const BV<A> &x, const uint16_t *Bg) {
     static_assert(A == 64, "tensor-core walk is A = 64");
     TcState &T = tcs;
     const uint32_t phase = T.nmv & 1;
     if (threadIdx.x == 0) {
-      asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(T.mbB), "r"(16384) : "memory");
-      asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
-                   ::"r"(T.sB), "l"(Bg), "r"(8192), "r"(T.mbB) : "memory");
-      asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
-                   ::"r"(T.sB + 8192), "l"(Bg + 4096), "r"(8192), "r"(T.mbB) : "memory");
+      asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(T.mbB), "r"(3 * 8192) : "memory");
+#pragma unroll
+      for (int part = 0; part < 3; ++part)
+        asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                     ::"r"(T.sB + part * 8192), "l"(Bg + part * 4096), "r"(8192), "r"(T.mbB) : "memory");
     }
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
-      uint32_t hi[4], lo[4];
+      uint32_t t1[4], t2[4], t3[4];
 #pragma unroll
       for (int pp = 0; pp < 4; ++pp) {
         const float a0 = x.v[8 * q + 2 * pp], a1 = x.v[8 * q + 2 * pp + 1];
-        const __nv_bfloat162 hh = __floats2bfloat162_rn(a0, a1);
-        const float2 hf = __bfloat1622float2(hh);
-        const __nv_bfloat162 ll = __floats2bfloat162_rn(a0 - hf.x, a1 - hf.y);
-        hi[pp] = *reinterpret_cast<const uint32_t *>(&hh);
-        lo[pp] = *reinterpret_cast<const uint32_t *>(&ll);
+        const __nv_bfloat162 b1 = __floats2bfloat162_rn(a0, a1);
+        const float2 f1 = __bfloat1622float2(b1);
+        const float r0 = a0 - f1.x, r1 = a1 - f1.y;
+        const __nv_bfloat162 b2 = __floats2bfloat162_rn(r0, r1);
+        const float2 f2 = __bfloat1622float2(b2);
+        const __nv_bfloat162 b3 = __floats2bfloat162_rn(r0 - f2.x, r1 - f2.y);
+        t1[pp] = *reinterpret_cast<const uint32_t *>(&b1);
+        t2[pp] = *reinterpret_cast<const uint32_t *>(&b2);
+        t3[pp] = *reinterpret_cast<const uint32_t *>(&b3);
       }
       const uint32_t off = kmaj_off(c, 32 * h + 8 * q);
-      asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};" ::"r"(T.sA + off), "r"(hi[0]), "r"(hi[1]), "r"(hi[2]),
-                   "r"(hi[3]) : "memory");
-      asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};" ::"r"(T.sA + 16384 + off), "r"(lo[0]), "r"(lo[1]),
-                   "r"(lo[2]), "r"(lo[3]) : "memory");
+      asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};" ::"r"(T.sA + off), "r"(t1[0]), "r"(t1[1]), "r"(t1[2]),
+                   "r"(t1[3]) : "memory");
+      asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};" ::"r"(T.sA + 16384 + off), "r"(t2[0]), "r"(t2[1]),
+                   "r"(t2[2]), "r"(t2[3]) : "memory");
+      asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};" ::"r"(T.sA + 32768 + off), "r"(t3[0]), "r"(t3[1]),
+                   "r"(t3[2]), "r"(t3[3]) : "memory");
     }
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -138,12 +147,14 @@ struct Walk {
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     if (threadIdx.x == 0) {
       if (!mbar_wait(T.mbB, phase)) *T.err = 1;
+      // (A term, B term) pairs with combined order <= 4
+      constexpr int pa[6] = {0, 0, 1, 0, 1, 2}, pb[6] = {0, 1, 0, 2, 1, 0};
 #pragma unroll
       for (int ks = 0; ks < 4; ++ks) {
 #pragma unroll
-        for (int prod = 0; prod < 3; ++prod) {
-          const uint32_t a = T.sA + (prod == 2 ? 16384 : 0) + ks * 256;
-          const uint32_t b = T.sB + (prod == 1 ? 8192 : 0) + ks * 256;
+        for (int prod = 0; prod < 6; ++prod) {
+          const uint32_t a = T.sA + pa[prod] * 16384 + ks * 256;
+          const uint32_t b = T.sB + pb[prod] * 8192 + ks * 256;
           const uint32_t accum = (ks | prod) != 0;
           asm volatile("{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
                        " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}"
@@ -291,7 +302,7 @@ __global__ void __launch_bounds__(128 * Geo<A>::H, 1) k_walk(const KParams P, fl
   __shared__ __align__(8) uint64_t s_mbar[2];
   __shared__ uint32_t s_taddr;
   __shared__ int s_err;
-  extern __shared__ __align__(1024) unsigned char s_dyn[];  // TC: A (32 KB) + B (16 KB) operands
+  extern __shared__ __align__(1024) unsigned char s_dyn[];  // TC: A (48 KB) + B (24 KB) operands
   if constexpr (TC) {
     if ((threadIdx.x >> 5) == 0) {
       const uint32_t dst = (uint32_t)__cvta_generic_to_shared(&s_taddr);
@@ -313,7 +324,7 @@ __global__ void __launch_bounds__(128 * Geo<A>::H, 1) k_walk(const KParams P, fl
     if (threadIdx.x == 0) {
       s_tc.tmem = s_taddr;
       s_tc.sA = (uint32_t)__cvta_generic_to_shared(s_dyn);
-      s_tc.sB = s_tc.sA + 32768;
+      s_tc.sB = s_tc.sA + 49152;
       s_tc.mbB = (uint32_t)__cvta_generic_to_shared(&s_mbar[0]);
       s_tc.mbM = (uint32_t)__cvta_generic_to_shared(&s_mbar[1]);
       s_tc.nmv = 0;
@@ -381,7 +392,7 @@ __global__ void __launch_bounds__(128 * Geo<A>::H, 1) k_walk(const KParams P, fl
       o.hh = k0.hh | k1.hh;
       o.init = k0.hh & k1.hh;
       o.code = -1;
-      wk.matvec(o.cc, u, MT + (size_t)n * (A + 1) * A, P.tab16 + (size_t)n * 16384);
+      wk.matvec(o.cc, u, MT + (size_t)n * (A + 1) * A, P.tab16 + (size_t)n * 24576);
     };
 
     // ---------------------------------------------------------------- inside
@@ -415,7 +426,7 @@ __global__ void __launch_bounds__(128 * Geo<A>::H, 1) k_walk(const KParams P, fl
         iRoot = init;
       } else {
         BV<A> cc;
-        wk.matvec(cc, u, MT + (size_t)s0.x * (A + 1) * A, P.tab16 + (size_t)s0.x * 16384);
+        wk.matvec(cc, u, MT + (size_t)s0.x * (A + 1) * A, P.tab16 + (size_t)s0.x * 24576);
         wk.st(slotv(s0.y), cc);
         if (h == 0) slotw(s0.y) = (eU << 2) | (hh << 1) | init;
       }
@@ -460,9 +471,9 @@ __global__ void __launch_bounds__(128 * Geo<A>::H, 1) k_walk(const KParams P, fl
       BV<A> Ds, dt, ut;
 #pragma unroll
       for (int q = 0; q < S; ++q) Ds.v[q] = D.v[q] * s;
-      wk.matvec(dt, Ds, Vd, P.tab16 + (size_t)P.R * 16384);
+      wk.matvec(dt, Ds, Vd, P.tab16 + (size_t)P.R * 24576);
       if (leafcode >= 0) wk.ld(ut, Ut + leafcode * A + 32 * h);
-      else wk.matvec(ut, U, Vu, P.tab16 + (size_t)P.R * 16384 + 8192);
+      else wk.matvec(ut, U, Vu, P.tab16 + (size_t)P.R * 24576 + 12288);
       if (valid) {
         wk.st(pa, dt);
         wk.st(pb, ut);
@@ -507,7 +518,7 @@ __global__ void __launch_bounds__(128 * Geo<A>::H, 1) k_walk(const KParams P, fl
         wk.obs(U, codep);
         const int eUp = nl.e + nr.e + wk.rescale(U);
         emit(s0.x, D, U, -1, eD + eUp, actp);
-        wk.matvec(O, D, MN + (size_t)s0.x * A * A, P.tab16 + (size_t)s0.x * 16384 + 8192);
+        wk.matvec(O, D, MN + (size_t)s0.x * A * A, P.tab16 + (size_t)s0.x * 24576 + 12288);
         wk.obs(O, codep);
         eO = eD + wk.rescale(O);
       }
@@ -547,7 +558,7 @@ __global__ void __launch_bounds__(128 * Geo<A>::H, 1) k_walk(const KParams P, fl
             emit(sc.x, Dc, du, -1, eDc + me.e, actc);
           }
           BV<A> Oc;
-          wk.matvec(Oc, Dc, MN + (size_t)sc.x * A * A, P.tab16 + (size_t)sc.x * 16384 + 8192);
+          wk.matvec(Oc, Dc, MN + (size_t)sc.x * A * A, P.tab16 + (size_t)sc.x * 24576 + 12288);
           wk.obs(Oc, dcode);
           const int eOc = eDc + wk.rescale(Oc);
 #pragma unroll
@@ -844,7 +855,7 @@ __global__ void __launch_bounds__(256, 1) k_acc(const KParams P, const float *__
 template <int A, int MODE, bool TC>
 int walk_launch1(const KParams &p, float *sa, float *sb, int c_base, int c_count, int grid, cudaStream_t s) {
   const int threads = 128 * Geo<A>::H;
-  const size_t dyn = TC ? 48 * 1024 + 1024 : 0;
+  const size_t dyn = TC ? 72 * 1024 + 1024 : 0;
   if (TC) {
     cudaError_t e = cudaFuncSetAttribute(k_walk<A, MODE, TC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
     if (e != cudaSuccess) return (int)e;

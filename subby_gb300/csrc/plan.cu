@@ -108,7 +108,8 @@ __global__ void k_compute_M(const double *__restrict__ V, const double *__restri
 // canonical K-major layout without swizzle (element (r, k) at byte
 // (r&7)*16 + (r>>3)*1024 + (k&7)*2 + (k>>3)*128 of a 64 x 64 tile):
 // per node n, B = M_n (rows b, K = j) and B = M_n^T (rows a, K = i); then
-// Vd^T and Vu^T.  hi = bf16(v), lo = bf16(v - hi).
+// Vd^T and Vu^T, each as three BF16 terms v1 = bf16(v), v2 = bf16(v - v1),
+// v3 = bf16(v - v1 - v2).
 __global__ void k_pack16(const float *__restrict__ MN, const float *__restrict__ Vd, const float *__restrict__ Vu,
                          int R, uint16_t *__restrict__ out) {
   const int ntiles = 2 * R + 2;
@@ -123,12 +124,15 @@ __global__ void k_pack16(const float *__restrict__ MN, const float *__restrict__
       const float *Vt = (tile == 2 * R) ? Vd : Vu;
       v = Vt[k * 64 + r];  // B[r][k] = V[k][r]
     }
-    const __nv_bfloat16 hi = __float2bfloat16_rn(v);
-    const __nv_bfloat16 lo = __float2bfloat16_rn(v - __bfloat162float(hi));
-    const size_t base = (size_t)tile * 8192;  // elements: hi 4096 then lo 4096
+    const __nv_bfloat16 t1 = __float2bfloat16_rn(v);
+    const float r1 = v - __bfloat162float(t1);
+    const __nv_bfloat16 t2 = __float2bfloat16_rn(r1);
+    const __nv_bfloat16 t3 = __float2bfloat16_rn(r1 - __bfloat162float(t2));
+    const size_t base = (size_t)tile * 12288;  // elements: three terms of 4096
     const int off = ((r & 7) * 16 + (r >> 3) * 1024 + (k & 7) * 2 + (k >> 3) * 128) / 2;
-    out[base + off] = __bfloat16_as_ushort(hi);
-    out[base + 4096 + off] = __bfloat16_as_ushort(lo);
+    out[base + off] = __bfloat16_as_ushort(t1);
+    out[base + 4096 + off] = __bfloat16_as_ushort(t2);
+    out[base + 8192 + off] = __bfloat16_as_ushort(t3);
   }
 }
 
@@ -485,7 +489,7 @@ int subby_plan_create(const int32_t *parent, const double *dist, const double *e
       e = cudaGetLastError();
     }
     if (e == cudaSuccess && A == 64) {
-      e = cudaMalloc(&P->d_tab16, sizeof(uint16_t) * (size_t)(2 * R + 2) * 8192);
+      e = cudaMalloc(&P->d_tab16, sizeof(uint16_t) * (size_t)(2 * R + 2) * 12288);
       if (e == cudaSuccess) {
         const int tt = (2 * R + 2) * 4096;
         k_pack16<<<std::max(1, std::min((tt + 255) / 256, 8192)), 256>>>(P->d_tab + o.MN, P->d_tab + o.Vd,

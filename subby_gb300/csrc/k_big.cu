@@ -629,12 +629,16 @@ __global__ void __launch_bounds__(256, 1) k_acc(const KParams P, const float *__
   for (int gi = blockIdx.x; gi < ngroups; gi += gridDim.x) {
     const int g0 = gi * G;                       // first column (chunk-relative)
     const int gcols = min(G, c_count - g0);
-    float acc[16][8];
+    // accumulators: ac2[a][p][q] = (C[k0+a][l0+2p], C[k0+a][l0+2p+1]) of column q
+    float2 ac2[4][2][8];
+#define ACC(a, b, q) (((b) & 1) ? ac2[a][(b) >> 1][q].y : ac2[a][(b) >> 1][q].x)
     float hv[4][8], gv[4][8], zv[8];
 #pragma unroll
-    for (int a = 0; a < 16; ++a)
+    for (int a = 0; a < 4; ++a)
 #pragma unroll
-      for (int q = 0; q < 8; ++q) acc[a][q] = 0.f;
+      for (int pp = 0; pp < 2; ++pp)
+#pragma unroll
+        for (int q = 0; q < 8; ++q) ac2[a][pp][q] = make_float2(0.f, 0.f);
     if (F81) {
 #pragma unroll
       for (int a = 0; a < 4; ++a)
@@ -689,22 +693,28 @@ __global__ void __launch_bounds__(256, 1) k_acc(const KParams P, const float *__
       if (active) {
         const float *da = cur + A * A, *db = cur + A * A + G * A;
         if (!F81) {
-          float jb[4][4];
+          // packed FP32x2: (d_k J_kl) for two l at once, then fma with (u_l, u_l+1)
+          float2 jp[4][2];
 #pragma unroll
           for (int a = 0; a < 4; ++a) {
             const float4 r = *reinterpret_cast<const float4 *>(cur + (k0 + a) * A + l0);
-            jb[a][0] = r.x, jb[a][1] = r.y, jb[a][2] = r.z, jb[a][3] = r.w;
+            jp[a][0] = make_float2(r.x, r.y);
+            jp[a][1] = make_float2(r.z, r.w);
           }
 #pragma unroll
           for (int q = 0; q < 8; ++q) {
             const int cc = grp * 8 + q;
             const float4 d = *reinterpret_cast<const float4 *>(da + cc * A + k0);
             const float4 u = *reinterpret_cast<const float4 *>(db + cc * A + l0);
-            const float dk[4] = {d.x, d.y, d.z, d.w}, ul[4] = {u.x, u.y, u.z, u.w};
+            const float dk[4] = {d.x, d.y, d.z, d.w};
+            const float2 up[2] = {make_float2(u.x, u.y), make_float2(u.z, u.w)};
 #pragma unroll
-            for (int a = 0; a < 4; ++a)
+            for (int a = 0; a < 4; ++a) {
+              const float2 dd = make_float2(dk[a], dk[a]);
 #pragma unroll
-              for (int b = 0; b < 4; ++b) acc[a * 4 + b][q] = fmaf(dk[a] * jb[a][b], ul[b], acc[a * 4 + b][q]);
+              for (int pp = 0; pp < 2; ++pp)
+                ac2[a][pp][q] = __ffma2_rn(__fmul2_rn(dd, jp[a][pp]), up[pp], ac2[a][pp][q]);
+            }
           }
         } else {
           const float4 abg = __ldg(reinterpret_cast<const float4 *>(F8) + n + 1);
@@ -716,10 +726,13 @@ __global__ void __launch_bounds__(256, 1) k_acc(const KParams P, const float *__
             const float4 d = *reinterpret_cast<const float4 *>(Ds + k0);
             const float4 u = *reinterpret_cast<const float4 *>(U + l0);
             const float dk[4] = {d.x, d.y, d.z, d.w}, ul[4] = {u.x, u.y, u.z, u.w};
+            const float2 up[2] = {make_float2(ul[0], ul[1]), make_float2(ul[2], ul[3])};
 #pragma unroll
             for (int a = 0; a < 4; ++a) {
+              const float ad = abg.x * dk[a];
+              const float2 dd = make_float2(ad, ad);
 #pragma unroll
-              for (int b = 0; b < 4; ++b) acc[a * 4 + b][q] = fmaf(abg.x * dk[a], ul[b], acc[a * 4 + b][q]);
+              for (int pp = 0; pp < 2; ++pp) ac2[a][pp][q] = __ffma2_rn(dd, up[pp], ac2[a][pp][q]);
               hv[a][q] = fmaf(abg.y * piU, dk[a], hv[a][q]);
               gv[a][q] = fmaf(abg.y * dsum, ul[a], gv[a][q]);
             }
@@ -749,7 +762,7 @@ __global__ void __launch_bounds__(256, 1) k_acc(const KParams P, const float *__
               const float pi_i = __ldg(pig + i);
               // h (row i) and g (column j): recomputed per block from its own
               // accumulators — hv[a] holds h_i, gv[b] holds g_j
-              const float I = acc[a * 4 + b][q] + hv[a][q] + pi_i * (gv[b][q] + zv[q]);
+              const float I = ACC(a, b, q) + hv[a][q] + pi_i * (gv[b][q] + zv[q]);
               out[(size_t)(i * A + j) * C + col] = (i == j) ? I : mu * __ldg(pig + j) * I;
             }
         }
@@ -768,22 +781,28 @@ __global__ void __launch_bounds__(256, 1) k_acc(const KParams P, const float *__
 #pragma unroll
         for (int a = 0; a < 4; ++a)
           *reinterpret_cast<float4 *>(Cs + ((size_t)cc * A + k0 + a) * A + l0) =
-              make_float4(acc[a * 4][q], acc[a * 4 + 1][q], acc[a * 4 + 2][q], acc[a * 4 + 3][q]);
+              make_float4(ac2[a][0][q].x, ac2[a][0][q].y, ac2[a][1][q].x, ac2[a][1][q].y);
       }
     }
     __syncthreads();
     // T[c][k][j] = sum_l C[c][k][l] V[j][l]   (block (k0.., j0 = l0..))
     if (active) {
 #pragma unroll
-      for (int a = 0; a < 16; ++a)
+      for (int a = 0; a < 4; ++a)
 #pragma unroll
-        for (int q = 0; q < 8; ++q) acc[a][q] = 0.f;
+        for (int pp = 0; pp < 2; ++pp)
+#pragma unroll
+          for (int q = 0; q < 8; ++q) ac2[a][pp][q] = make_float2(0.f, 0.f);
       for (int l = 0; l < A; l += 4) {
-        float vj[4][4];
+        float2 vjp[2][4];  // (V[j][l+m], V[j+1][l+m]) for the two j pairs of this block
 #pragma unroll
-        for (int b = 0; b < 4; ++b) {
-          const float4 r = __ldg(reinterpret_cast<const float4 *>(V + (l0 + b) * A + l));
-          vj[b][0] = r.x, vj[b][1] = r.y, vj[b][2] = r.z, vj[b][3] = r.w;
+        for (int pp = 0; pp < 2; ++pp) {
+          const float4 r0 = __ldg(reinterpret_cast<const float4 *>(V + (l0 + 2 * pp) * A + l));
+          const float4 r1 = __ldg(reinterpret_cast<const float4 *>(V + (l0 + 2 * pp + 1) * A + l));
+          vjp[pp][0] = make_float2(r0.x, r1.x);
+          vjp[pp][1] = make_float2(r0.y, r1.y);
+          vjp[pp][2] = make_float2(r0.z, r1.z);
+          vjp[pp][3] = make_float2(r0.w, r1.w);
         }
 #pragma unroll
         for (int q = 0; q < 8; ++q) {
@@ -793,9 +812,11 @@ __global__ void __launch_bounds__(256, 1) k_acc(const KParams P, const float *__
             const float4 cr = *reinterpret_cast<const float4 *>(Cs + ((size_t)cc * A + k0 + a) * A + l);
             const float cv[4] = {cr.x, cr.y, cr.z, cr.w};
 #pragma unroll
-            for (int b = 0; b < 4; ++b)
+            for (int m = 0; m < 4; ++m) {
+              const float2 cc2 = make_float2(cv[m], cv[m]);
 #pragma unroll
-              for (int m = 0; m < 4; ++m) acc[a * 4 + b][q] = fmaf(cv[m], vj[b][m], acc[a * 4 + b][q]);
+              for (int pp = 0; pp < 2; ++pp) ac2[a][pp][q] = __ffma2_rn(cc2, vjp[pp][m], ac2[a][pp][q]);
+            }
           }
         }
       }
@@ -808,29 +829,34 @@ __global__ void __launch_bounds__(256, 1) k_acc(const KParams P, const float *__
 #pragma unroll
         for (int a = 0; a < 4; ++a)
           *reinterpret_cast<float4 *>(Cs + ((size_t)cc * A + k0 + a) * A + l0) =
-              make_float4(acc[a * 4][q], acc[a * 4 + 1][q], acc[a * 4 + 2][q], acc[a * 4 + 3][q]);
+              make_float4(ac2[a][0][q].x, ac2[a][0][q].y, ac2[a][1][q].x, ac2[a][1][q].y);
       }
     }
     __syncthreads();
     // VCV[c][i][j] = sum_k V[i][k] T[c][k][j]   (block (i0 = k0.., j0 = l0..))
     if (active) {
 #pragma unroll
-      for (int a = 0; a < 16; ++a)
+      for (int a = 0; a < 4; ++a)
 #pragma unroll
-        for (int q = 0; q < 8; ++q) acc[a][q] = 0.f;
+        for (int pp = 0; pp < 2; ++pp)
+#pragma unroll
+          for (int q = 0; q < 8; ++q) ac2[a][pp][q] = make_float2(0.f, 0.f);
       for (int k = 0; k < A; ++k) {
-        float vi[4];
+        float2 vi2[4];
 #pragma unroll
-        for (int a = 0; a < 4; ++a) vi[a] = __ldg(V + (k0 + a) * A + k);
+        for (int a = 0; a < 4; ++a) {
+          const float v = __ldg(V + (k0 + a) * A + k);
+          vi2[a] = make_float2(v, v);
+        }
 #pragma unroll
         for (int q = 0; q < 8; ++q) {
           const int cc = grp * 8 + q;
           const float4 tr = *reinterpret_cast<const float4 *>(Cs + ((size_t)cc * A + k) * A + l0);
-          const float tv[4] = {tr.x, tr.y, tr.z, tr.w};
+          const float2 tp[2] = {make_float2(tr.x, tr.y), make_float2(tr.z, tr.w)};
 #pragma unroll
           for (int a = 0; a < 4; ++a)
 #pragma unroll
-            for (int b = 0; b < 4; ++b) acc[a * 4 + b][q] = fmaf(vi[a], tv[b], acc[a * 4 + b][q]);
+            for (int pp = 0; pp < 2; ++pp) ac2[a][pp][q] = __ffma2_rn(vi2[a], tp[pp], ac2[a][pp][q]);
         }
       }
 #pragma unroll
@@ -843,7 +869,7 @@ __global__ void __launch_bounds__(256, 1) k_acc(const KParams P, const float *__
 #pragma unroll
           for (int b = 0; b < 4; ++b) {
             const int i = k0 + a, j = l0 + b;
-            const float v = acc[a * 4 + b][q];
+            const float v = ACC(a, b, q);
             out[(size_t)(i * A + j) * C + col] = (i == j) ? v : __ldg(Sm + i * A + j) * v;
           }
       }
@@ -851,6 +877,7 @@ __global__ void __launch_bounds__(256, 1) k_acc(const KParams P, const float *__
     __syncthreads();
   }
 }
+#undef ACC
 
 template <int A, int MODE, bool TC>
 int walk_launch1(const KParams &p, float *sa, float *sb, int c_base, int c_count, int grid, cudaStream_t s) {

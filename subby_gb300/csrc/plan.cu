@@ -205,6 +205,9 @@ struct subby_plan {
   size_t tab_bytes = 0;
   DevBuf work;     // scratch + gradient partials
   DevBuf io;       // staging of alignment/mask/outputs in host-pointer mode
+  // host-pointer mode: copy queues of the column-chunk pipeline and its events
+  cudaStream_t s_in = nullptr, s_out = nullptr;
+  std::vector<cudaEvent_t> ev;
   std::mutex lock;
 };
 
@@ -517,6 +520,9 @@ int subby_plan_destroy(subby_plan *P) {
   if (P->d_err) cudaFree(P->d_err);
   P->work.release();
   P->io.release();
+  for (cudaEvent_t e : P->ev) cudaEventDestroy(e);
+  if (P->s_in) cudaStreamDestroy(P->s_in);
+  if (P->s_out) cudaStreamDestroy(P->s_out);
   delete P;
   return SUBBY_OK;
 }
@@ -812,6 +818,28 @@ int run_big(subby_plan *P, const int32_t *d_aln, int C, float *d_logL, float *d_
   return 0;
 }
 
+// Columns per chunk of the host-pointer pipeline: whole waves of the
+// one-CTA-per-SM kernels (nsm x 256 columns), about eight chunks for large C,
+// a single chunk below two waves (nothing to overlap).
+int host_chunk_columns(const subby_plan *P, int C) {
+  const long long wave = (long long)std::max(P->nsm, 1) * 256;
+  if (C < 2 * wave) return std::max(C, 1);
+  const long long waves = (C + wave - 1) / wave;
+  const long long per = std::max(1LL, (waves + 7) / 8);
+  return (int)std::min<long long>(C, per * wave);
+}
+
+int ensure_pipeline(subby_plan *P, int nev) {
+  if (!P->s_in) CU(cudaStreamCreateWithFlags(&P->s_in, cudaStreamNonBlocking));
+  if (!P->s_out) CU(cudaStreamCreateWithFlags(&P->s_out, cudaStreamNonBlocking));
+  while ((int)P->ev.size() < nev) {
+    cudaEvent_t e;
+    CU(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    P->ev.push_back(e);
+  }
+  return 0;
+}
+
 int run_common(subby_plan *P, const int32_t *d_aln, int C, float *d_logL, float *d_counts,
                float *d_root, int mode, int mask_mode, const uint8_t *d_mask, const float *d_g,
                double *d_gt, double *d_gC, int *grid_out, cudaStream_t stream) {
@@ -908,7 +936,13 @@ int subby_plan_run(subby_plan *P, const int32_t *aln, int C, float *logL, float 
     if (rc == 0 && dev != P->device) cudaSetDevice(dev);
     return rc;
   }
-  // host pointers: stage through device buffers on `stream`
+  // host pointers: column chunks flow through three queues — host-to-device
+  // copies on P->s_in, kernels on `stream`, device-to-host copies on
+  // P->s_out — so the copies of one chunk overlap the kernels of its
+  // neighbours.  Chunk c0..c0+cc is staged compactly ((R, cc) tokens at
+  // R*c0, (A*A, cc) counts at A*A*c0, ...), so no device region is reused
+  // within a call and the only ordering needed is copy-in -> kernel ->
+  // copy-out per chunk.
   const size_t b_aln = (size_t)R * C * sizeof(int32_t);
   const size_t b_mask = (mask_mode == SUBBY_MASK_GIVEN) ? (size_t)R * C : 0;
   const size_t b_ll = logL ? (size_t)C * 4 : 0;
@@ -927,15 +961,56 @@ int subby_plan_run(subby_plan *P, const int32_t *aln, int C, float *logL, float 
   float *d_ct = b_ct ? (float *)base : nullptr;
   base += al(b_ct);
   float *d_rp = b_rp ? (float *)base : nullptr;
-  CU(cudaMemcpyAsync(d_aln, aln, b_aln, cudaMemcpyHostToDevice, stream));
-  if (b_mask) CU(cudaMemcpyAsync(d_mask, mask, b_mask, cudaMemcpyHostToDevice, stream));
-  rc = run_common(P, d_aln, C, d_ll, d_ct, d_rp, mode, mask_mode, d_mask, nullptr, nullptr,
-                  nullptr, nullptr, stream);
-  if (rc) return rc;
-  if (b_ll) CU(cudaMemcpyAsync(logL, d_ll, b_ll, cudaMemcpyDeviceToHost, stream));
-  if (b_ct) CU(cudaMemcpyAsync(counts, d_ct, b_ct, cudaMemcpyDeviceToHost, stream));
-  if (b_rp) CU(cudaMemcpyAsync(rootProb, d_rp, b_rp, cudaMemcpyDeviceToHost, stream));
-  CU(cudaStreamSynchronize(stream));
+  const int chunk = host_chunk_columns(P, C);
+  const int nch = (C + chunk - 1) / chunk;
+  if ((rc = ensure_pipeline(P, 2 * nch + 2))) return rc;
+  cudaEvent_t *ev = P->ev.data();
+  // drains both copy queues before any return, so P->io is idle afterwards
+  auto finish = [&](int code) {
+    cudaStreamSynchronize(P->s_in);
+    cudaStreamSynchronize(P->s_out);
+    cudaStreamSynchronize(stream);
+    return code;
+  };
+  CU(cudaEventRecord(ev[0], stream));
+  CU(cudaStreamWaitEvent(P->s_in, ev[0], 0));
+  for (int i = 0; i < nch; ++i) {
+    const int c0 = i * chunk, cc = std::min(chunk, C - c0);
+    cudaError_t e = cudaMemcpy2DAsync(d_aln + (size_t)R * c0, (size_t)cc * 4, aln + c0, (size_t)C * 4,
+                                      (size_t)cc * 4, R, cudaMemcpyHostToDevice, P->s_in);
+    if (e == cudaSuccess && b_mask)
+      e = cudaMemcpy2DAsync(d_mask + (size_t)R * c0, (size_t)cc, mask + c0, (size_t)C, (size_t)cc, R,
+                            cudaMemcpyHostToDevice, P->s_in);
+    if (e == cudaSuccess) e = cudaEventRecord(ev[2 + 2 * i], P->s_in);
+    if (e != cudaSuccess) return finish(cuda_fail(e, "chunk copy-in"));
+  }
+  for (int i = 0; i < nch; ++i) {
+    const int c0 = i * chunk, cc = std::min(chunk, C - c0);
+    cudaError_t e = cudaStreamWaitEvent(stream, ev[2 + 2 * i], 0);
+    if (e != cudaSuccess) return finish(cuda_fail(e, "cudaStreamWaitEvent"));
+    rc = run_common(P, d_aln + (size_t)R * c0, cc, d_ll ? d_ll + c0 : nullptr,
+                    d_ct ? d_ct + (size_t)A * A * c0 : nullptr, d_rp ? d_rp + (size_t)A * c0 : nullptr,
+                    mode, mask_mode, d_mask ? d_mask + (size_t)R * c0 : nullptr, nullptr, nullptr, nullptr,
+                    nullptr, stream);
+    if (rc) return finish(rc);
+    e = cudaEventRecord(ev[3 + 2 * i], stream);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(P->s_out, ev[3 + 2 * i], 0);
+    if (e == cudaSuccess && b_ll)
+      e = cudaMemcpyAsync(logL + c0, d_ll + c0, (size_t)cc * 4, cudaMemcpyDeviceToHost, P->s_out);
+    if (e == cudaSuccess && b_ct)
+      e = cudaMemcpy2DAsync(counts + c0, (size_t)C * 4, d_ct + (size_t)A * A * c0, (size_t)cc * 4,
+                            (size_t)cc * 4, (size_t)A * A, cudaMemcpyDeviceToHost, P->s_out);
+    if (e == cudaSuccess && b_rp)
+      e = cudaMemcpy2DAsync(rootProb + c0, (size_t)C * 4, d_rp + (size_t)A * c0, (size_t)cc * 4,
+                            (size_t)cc * 4, (size_t)A, cudaMemcpyDeviceToHost, P->s_out);
+    if (e != cudaSuccess) return finish(cuda_fail(e, "chunk copy-out"));
+  }
+  {
+    cudaError_t e = cudaEventRecord(ev[1], P->s_out);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(stream, ev[1], 0);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
+    if (e != cudaSuccess) return finish(cuda_fail(e, "chunk pipeline"));
+  }
   if (P->d_err) {
     int dev_err = 0;
     CU(cudaMemcpy(&dev_err, P->d_err, sizeof(int), cudaMemcpyDeviceToHost));

@@ -607,14 +607,30 @@ struct AccGeo {
   static constexpr int THREADS = NB * GROUPS;
 };
 
+// Stages of the k_acc ring: as many (J_n, a, b) buffers as fit in the
+// G x A x A floats of the back-transform buffer, at most 8.
+template <int A>
+struct AccRing {
+  static constexpr int STAGE = A * A + 2 * AccGeo<A>::G * A;       // floats per stage
+  static constexpr int CBUF = AccGeo<A>::G * A * A;                // back-transform buffer
+  static constexpr int S = (CBUF / STAGE) < 8 ? (CBUF / STAGE) : 8;
+  static constexpr int SCAL = (S * STAGE > CBUF ? S * STAGE : CBUF);  // F81 scalars after both
+  static_assert(S >= 3, "ring too short");
+};
+
 template <int A, bool F81>
 __global__ void __launch_bounds__(256, 1) k_acc(const KParams P, const float *__restrict__ stage_a,
                                                  const float *__restrict__ stage_b, int c_base, int c_count) {
   using Gm = AccGeo<A>;
+  using Rg = AccRing<A>;
   constexpr int G = Gm::G;
-  extern __shared__ __align__(16) float sm[];
-  // double-buffered stage: J_n (A*A) + a (G*A) + b (G*A); later reused for C / T
-  float *buf[2] = {sm, sm + A * A + 2 * G * A};
+  constexpr int S = Rg::S;
+  extern __shared__ __align__(128) float sm[];
+  // ring of S stages, each J_n (A*A, eigen path) + a (G*A) + b (G*A), filled
+  // by bulk copies that complete on one mbarrier per stage; the space is
+  // reused for C / T by the back-transform.
+  __shared__ __align__(8) uint64_t mbar[S];
+  __shared__ int s_err;
   const int t = threadIdx.x;
   const bool active = t < Gm::THREADS;
   const int blk = t % Gm::NB, grp = t / Gm::NB;
@@ -625,6 +641,38 @@ __global__ void __launch_bounds__(256, 1) k_acc(const KParams P, const float *__
   const int C = P.C;
   const int nbr = P.R - 1;
   const int ngroups = (c_count + G - 1) / G;
+  // V, S (eigen path) and pi, copied once per CTA behind the F81 scalars
+  float *Vs = sm + Rg::SCAL + 2 * G, *Ss = Vs + A * A, *pis = Ss + A * A;
+  if (!F81)
+    for (int i = t; i < A * A; i += blockDim.x) {
+      Vs[i] = __ldg(P.tab + P.off.V + i);
+      Ss[i] = __ldg(P.tab + P.off.S + i);
+    }
+  for (int i = t; i < A; i += blockDim.x) pis[i] = __ldg(pig + i);
+  // output row r, the 8 columns col0.. of this thread's group: two 16-byte
+  // stores when the rows are 16-byte aligned and all 8 columns exist
+  const bool vec_out = (C & 3) == 0 && (c_base & 3) == 0;
+  auto store8 = [&](size_t r, const float (&v)[8], int col0, int ncols) {
+    float *o = P.counts + r * C + col0;
+    if (vec_out && ncols >= 8) {
+      *reinterpret_cast<float4 *>(o) = make_float4(v[0], v[1], v[2], v[3]);
+      *reinterpret_cast<float4 *>(o + 4) = make_float4(v[4], v[5], v[6], v[7]);
+    } else {
+#pragma unroll
+      for (int q = 0; q < 8; ++q)
+        if (q < ncols) o[q] = v[q];
+    }
+  };
+  if (t == 0) {
+    s_err = 0;
+    for (int i = 0; i < S; ++i) {
+      const uint32_t mb = (uint32_t)__cvta_generic_to_shared(&mbar[i]);
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mb) : "memory");
+    }
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  uint32_t it = 0;  // ring position of the next branch to consume (all groups)
 
   for (int gi = blockIdx.x; gi < ngroups; gi += gridDim.x) {
     const int g0 = gi * G;                       // first column (chunk-relative)
@@ -647,39 +695,53 @@ __global__ void __launch_bounds__(256, 1) k_acc(const KParams P, const float *__
 #pragma unroll
       for (int q = 0; q < 8; ++q) zv[q] = 0.f;
     }
-    // J_n (eigen) and the staged vectors of branch n for this group's columns,
-    // copied asynchronously (cp.async, 16 B; out-of-range columns zero-filled)
-    auto cp16 = [](float *dst, const float *src, bool in) {
-      const uint32_t d = (uint32_t)__cvta_generic_to_shared(dst);
-      asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(d), "l"(src), "r"(in ? 16 : 0)
-                   : "memory");
-    };
-    auto load = [&](int n, float *dst) {
-      if (!F81)
-        for (int i = t; i < A * A / 4; i += blockDim.x) cp16(dst + 4 * i, J + (size_t)(n + 1) * A * A + 4 * i, true);
-      const size_t off = ((size_t)n * c_count + g0) * A;
-      float *da = dst + A * A, *db = dst + A * A + G * A;
-      for (int i = t; i < G * A / 4; i += blockDim.x) {
-        const bool in = i * 4 < gcols * A;
-        cp16(da + 4 * i, stage_a + off + (in ? 4 * i : 0), in);
-        cp16(db + 4 * i, stage_b + off + (in ? 4 * i : 0), in);
-      }
-      asm volatile("cp.async.commit_group;" ::: "memory");
-    };
-    load(0, buf[0]);
-    float *scal = sm + 2 * (A * A + 2 * G * A);  // F81: piU, Dsum per column
-    for (int n = 0; n < nbr; ++n) {
-      float *cur = buf[n & 1];
-      if (n + 1 < nbr) {
-        load(n + 1, buf[(n + 1) & 1]);
-        asm volatile("cp.async.wait_group 1;" ::: "memory");
-      } else {
-        asm volatile("cp.async.wait_group 0;" ::: "memory");
+    // a short last group: zero the unused column rows of every stage once
+    // (the copies below fill only gcols rows)
+    if (gcols < G) {
+      for (int i = t; i < S * 2 * (G - gcols) * A; i += blockDim.x) {
+        const int st = i / (2 * (G - gcols) * A), r = i % (2 * (G - gcols) * A);
+        const int half = r / ((G - gcols) * A), e = r % ((G - gcols) * A);
+        sm[st * Rg::STAGE + (F81 ? 0 : A * A) + half * G * A + gcols * A + e] = 0.f;
       }
       __syncthreads();
+    }
+    // J_n (eigen path) and the staged vectors of branch n for this group's
+    // columns: three bulk copies issued by one thread, completing on the
+    // stage's mbarrier
+    const uint32_t vbytes = (uint32_t)gcols * A * 4;
+    auto load = [&](int n, uint32_t pos) {
+      const int st = (int)(pos % S);
+      float *dst = sm + st * Rg::STAGE;
+      const uint32_t mb = (uint32_t)__cvta_generic_to_shared(&mbar[st]);
+      const uint32_t jb = F81 ? 0u : (uint32_t)(A * A * 4);
+      asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(mb), "r"(jb + 2 * vbytes)
+                   : "memory");
+      if (!F81)
+        asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                     ::"r"((uint32_t)__cvta_generic_to_shared(dst)), "l"(J + (size_t)(n + 1) * A * A), "r"(jb),
+                     "r"(mb) : "memory");
+      const size_t off = ((size_t)n * c_count + g0) * A;
+      float *da = dst + (F81 ? 0 : A * A), *db = da + G * A;
+      asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                   ::"r"((uint32_t)__cvta_generic_to_shared(da)), "l"(stage_a + off), "r"(vbytes), "r"(mb)
+                   : "memory");
+      asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                   ::"r"((uint32_t)__cvta_generic_to_shared(db)), "l"(stage_b + off), "r"(vbytes), "r"(mb)
+                   : "memory");
+    };
+    if (t == 0)
+      for (int n = 0; n < S - 1 && n < nbr; ++n) load(n, it + n);
+    float *scal = sm + Rg::SCAL;  // F81: piU, Dsum per column
+    for (int n = 0; n < nbr; ++n, ++it) {
+      // every thread is done with the stage of branch n - 1: refill it
+      __syncthreads();
+      if (t == 0 && n + S - 1 < nbr) load(n + S - 1, it + S - 1);
+      const int st = (int)(it % S);
+      const float *cur = sm + st * Rg::STAGE;
+      if (!mbar_wait((uint32_t)__cvta_generic_to_shared(&mbar[st]), (it / S) & 1)) s_err = 1;
       if (F81) {
         if (t < G) {
-          const float *Ds = cur + A * A + t * A, *U = cur + A * A + G * A + t * A;
+          const float *Ds = cur + t * A, *U = cur + G * A + t * A;
           float piU = 0.f, dsum = 0.f;
           for (int a = 0; a < A; ++a) {
             piU = fmaf(__ldg(pig + a), U[a], piU);
@@ -691,7 +753,7 @@ __global__ void __launch_bounds__(256, 1) k_acc(const KParams P, const float *__
         __syncthreads();
       }
       if (active) {
-        const float *da = cur + A * A, *db = cur + A * A + G * A;
+        const float *da = cur + (F81 ? 0 : A * A), *db = da + G * A;
         if (!F81) {
           // packed FP32x2: (d_k J_kl) for two l at once, then fma with (u_l, u_l+1)
           float2 jp[4][2];
@@ -740,40 +802,32 @@ __global__ void __launch_bounds__(256, 1) k_acc(const KParams P, const float *__
           }
         }
       }
-      __syncthreads();
     }
+    __syncthreads();
     // ------------------------------------------------------------- epilogue
-    float *out = P.counts;
+    const int col0 = c_base + g0 + grp * 8, ncols = gcols - grp * 8;
     if (F81) {
-      // h_i lives with l0 == 0 blocks' rows? Every block owns h for its k rows
-      // and g for its l columns; all blocks computed both, use them directly.
-      if (active) {
+      // every (k, l) block accumulated h for its rows and g for its columns
+      if (active && ncols > 0) {
         const float mu = P.f81_mu;
 #pragma unroll
-        for (int q = 0; q < 8; ++q) {
-          const int cc = grp * 8 + q;
-          if (cc >= gcols) continue;
-          const int col = c_base + g0 + cc;
+        for (int a = 0; a < 4; ++a)
 #pragma unroll
-          for (int a = 0; a < 4; ++a)
+          for (int b = 0; b < 4; ++b) {
+            const int i = k0 + a, j = l0 + b;
+            const float pi_i = pis[i], f = (i == j) ? 1.f : mu * pis[j];
+            float v[8];
 #pragma unroll
-            for (int b = 0; b < 4; ++b) {
-              const int i = k0 + a, j = l0 + b;
-              const float pi_i = __ldg(pig + i);
-              // h (row i) and g (column j): recomputed per block from its own
-              // accumulators — hv[a] holds h_i, gv[b] holds g_j
-              const float I = ACC(a, b, q) + hv[a][q] + pi_i * (gv[b][q] + zv[q]);
-              out[(size_t)(i * A + j) * C + col] = (i == j) ? I : mu * __ldg(pig + j) * I;
-            }
-        }
+            for (int q = 0; q < 8; ++q) v[q] = f * (ACC(a, b, q) + hv[a][q] + pi_i * (gv[b][q] + zv[q]));
+            store8((size_t)(i * A + j), v, col0, ncols);
+          }
       }
       __syncthreads();
       continue;
     }
     // back-transform: C -> T = C V^T -> VCV = V T, through shared memory [c][k][l]
     float *Cs = sm;  // G * A * A floats
-    const float *V = P.tab + P.off.V;
-    const float *Sm = P.tab + P.off.S;
+    const float *V = Vs;
     if (active) {
 #pragma unroll
       for (int q = 0; q < 8; ++q) {
@@ -797,8 +851,8 @@ __global__ void __launch_bounds__(256, 1) k_acc(const KParams P, const float *__
         float2 vjp[2][4];  // (V[j][l+m], V[j+1][l+m]) for the two j pairs of this block
 #pragma unroll
         for (int pp = 0; pp < 2; ++pp) {
-          const float4 r0 = __ldg(reinterpret_cast<const float4 *>(V + (l0 + 2 * pp) * A + l));
-          const float4 r1 = __ldg(reinterpret_cast<const float4 *>(V + (l0 + 2 * pp + 1) * A + l));
+          const float4 r0 = *reinterpret_cast<const float4 *>(V + (l0 + 2 * pp) * A + l);
+          const float4 r1 = *reinterpret_cast<const float4 *>(V + (l0 + 2 * pp + 1) * A + l);
           vjp[pp][0] = make_float2(r0.x, r1.x);
           vjp[pp][1] = make_float2(r0.y, r1.y);
           vjp[pp][2] = make_float2(r0.z, r1.z);
@@ -845,7 +899,7 @@ __global__ void __launch_bounds__(256, 1) k_acc(const KParams P, const float *__
         float2 vi2[4];
 #pragma unroll
         for (int a = 0; a < 4; ++a) {
-          const float v = __ldg(V + (k0 + a) * A + k);
+          const float v = V[(k0 + a) * A + k];
           vi2[a] = make_float2(v, v);
         }
 #pragma unroll
@@ -859,23 +913,23 @@ __global__ void __launch_bounds__(256, 1) k_acc(const KParams P, const float *__
             for (int pp = 0; pp < 2; ++pp) ac2[a][pp][q] = __ffma2_rn(vi2[a], tp[pp], ac2[a][pp][q]);
         }
       }
-#pragma unroll
-      for (int q = 0; q < 8; ++q) {
-        const int cc = grp * 8 + q;
-        if (cc >= gcols) continue;
-        const int col = c_base + g0 + cc;
+      if (ncols > 0) {
 #pragma unroll
         for (int a = 0; a < 4; ++a)
 #pragma unroll
           for (int b = 0; b < 4; ++b) {
             const int i = k0 + a, j = l0 + b;
-            const float v = ACC(a, b, q);
-            out[(size_t)(i * A + j) * C + col] = (i == j) ? v : __ldg(Sm + i * A + j) * v;
+            const float f = (i == j) ? 1.f : Ss[i * A + j];
+            float v[8];
+#pragma unroll
+            for (int q = 0; q < 8; ++q) v[q] = f * ACC(a, b, q);
+            store8((size_t)(i * A + j), v, col0, ncols);
           }
       }
     }
     __syncthreads();
   }
+  if (t == 0 && s_err && P.err) atomicAdd(P.err, 1);
 }
 #undef ACC
 
@@ -910,9 +964,7 @@ template <int A>
 int acc_launch(const KParams &p, bool f81, const float *sa, const float *sb, int c_base, int c_count, int grid,
                cudaStream_t s) {
   using Gm = AccGeo<A>;
-  const size_t stage = (size_t)(A * A + 2 * Gm::G * A) * 2 * sizeof(float);
-  const size_t cbuf = (size_t)Gm::G * A * A * sizeof(float);
-  const size_t smem = (stage + 2 * Gm::G * sizeof(float)) > cbuf ? (stage + 2 * Gm::G * sizeof(float)) : cbuf;
+  const size_t smem = (size_t)(AccRing<A>::SCAL + 2 * Gm::G + 2 * A * A + A) * sizeof(float);
   cudaError_t e;
   if (f81) {
     e = cudaFuncSetAttribute(k_acc<A, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);

@@ -153,19 +153,57 @@ __global__ void k_compute_K(const float *__restrict__ J, const float *__restrict
   }
 }
 
+// Device memory of plans comes from one library-owned stream-ordered pool per
+// device: allocations and frees are ordered on CUDA streams (no implicit
+// device-wide synchronisation, so creating or evicting a plan never stalls
+// kernels of other streams), and up to kPoolKeep bytes of freed blocks stay
+// cached in the pool for the next plan.
+constexpr uint64_t kPoolKeep = 2ull << 30;
+
+cudaMemPool_t lib_pool(int dev) {
+  static std::mutex m;
+  static cudaMemPool_t pools[64] = {};
+  if (dev < 0 || dev >= 64) return nullptr;
+  std::lock_guard<std::mutex> g(m);
+  if (!pools[dev]) {
+    cudaMemPoolProps pr{};
+    pr.allocType = cudaMemAllocationTypePinned;
+    pr.location.type = cudaMemLocationTypeDevice;
+    pr.location.id = dev;
+    if (cudaMemPoolCreate(&pools[dev], &pr) != cudaSuccess) {
+      cudaGetLastError();
+      pools[dev] = nullptr;
+      return nullptr;
+    }
+    uint64_t keep = kPoolKeep;
+    cudaMemPoolSetAttribute(pools[dev], cudaMemPoolAttrReleaseThreshold, &keep);
+  }
+  return pools[dev];
+}
+
+cudaError_t pool_alloc(void **p, size_t bytes, cudaMemPool_t pool, cudaStream_t s) {
+  return pool ? cudaMallocFromPoolAsync(p, bytes, pool, s) : cudaMallocAsync(p, bytes, s);
+}
+
 struct DevBuf {
   void *p = nullptr;
   size_t bytes = 0;
-  int grow(size_t need) {
+  // Grow to `need` bytes in stream order on `s`; the old block is freed on
+  // `s` once `after` (the plan's last use, possibly on another stream) has
+  // completed.
+  int grow(size_t need, cudaStream_t s, cudaMemPool_t pool, cudaEvent_t after) {
     if (need <= bytes) return 0;
-    if (p) cudaFree(p);
+    if (p) {
+      if (after) cudaStreamWaitEvent(s, after, 0);
+      cudaFreeAsync(p, s);
+    }
     p = nullptr;
     bytes = 0;
     size_t want = need + need / 4;
-    cudaError_t e = cudaMalloc(&p, want);
+    cudaError_t e = pool_alloc(&p, want, pool, s);
     if (e != cudaSuccess) {
       cudaGetLastError();
-      e = cudaMalloc(&p, need);
+      e = pool_alloc(&p, need, pool, s);
       if (e != cudaSuccess) {
         cudaGetLastError();
         p = nullptr;
@@ -176,8 +214,8 @@ struct DevBuf {
     bytes = want;
     return 0;
   }
-  void release() {
-    if (p) cudaFree(p);
+  void release(cudaStream_t s) {
+    if (p) cudaFreeAsync(p, s);
     p = nullptr;
     bytes = 0;
   }
@@ -207,6 +245,15 @@ struct subby_plan {
   DevBuf io;       // staging of alignment/mask/outputs in host-pointer mode
   // host-pointer mode: copy queues of the column-chunk pipeline and its events
   cudaStream_t s_in = nullptr, s_out = nullptr;
+  // stream-ordered lifetime: tables are built on s_prep; last_use marks the
+  // end of the latest enqueued kernel, after which buffers may be freed
+  cudaStream_t s_prep = nullptr;
+  cudaEvent_t last_use = nullptr;
+  bool used = false;
+  cudaMemPool_t pool = nullptr;
+  int grow(DevBuf &b, size_t need, cudaStream_t s) {
+    return b.grow(need, s, pool, used ? last_use : nullptr);
+  }
   std::vector<cudaEvent_t> ev;
   std::mutex lock;
 };
@@ -286,6 +333,15 @@ int subby_plan_create(const int32_t *parent, const double *dist, const double *e
   cudaGetDevice(&P->device);
   cudaDeviceGetAttribute(&P->nsm, cudaDevAttrMultiProcessorCount, P->device);
   P->root_is_leaf = (R == 1);
+  P->pool = lib_pool(P->device);
+  {
+    cudaError_t e0 = cudaStreamCreateWithFlags(&P->s_prep, cudaStreamNonBlocking);
+    if (e0 == cudaSuccess) e0 = cudaEventCreateWithFlags(&P->last_use, cudaEventDisableTiming);
+    if (e0 != cudaSuccess) {
+      subby_plan_destroy(P);
+      return cuda_fail(e0, "plan stream");
+    }
+  }
 
   // DFS postorder of the internal nodes (children before parents).
   std::vector<int> order;
@@ -444,65 +500,66 @@ int subby_plan_create(const int32_t *parent, const double *dist, const double *e
     return rc;
   };
   P->tab_bytes = (size_t)o.total * sizeof(float);
-  cudaError_t e = cudaMalloc(&P->d_tab, P->tab_bytes);
-  if (e != cudaSuccess) return cleanup(cuda_fail(e, "cudaMalloc(tables)"));
-  e = cudaMemcpy(P->d_tab, tab.data(), P->tab_bytes, cudaMemcpyHostToDevice);
-  if (e != cudaSuccess) return cleanup(cuda_fail(e, "cudaMemcpy(tables)"));
-  e = cudaMalloc(&P->d_tab64, sizeof(double) * (2 * A * A + A + R + A));
-  if (e != cudaSuccess) return cleanup(cuda_fail(e, "cudaMalloc(tables64)"));
+  cudaStream_t qs = P->s_prep;
+  cudaError_t e = pool_alloc((void **)&P->d_tab, P->tab_bytes, P->pool, qs);
+  if (e != cudaSuccess) return cleanup(cuda_fail(e, "table allocation"));
+  e = cudaMemcpyAsync(P->d_tab, tab.data(), P->tab_bytes, cudaMemcpyHostToDevice, qs);
+  if (e != cudaSuccess) return cleanup(cuda_fail(e, "table upload"));
+  e = pool_alloc((void **)&P->d_tab64, sizeof(double) * (2 * A * A + A + R + A), P->pool, qs);
+  if (e != cudaSuccess) return cleanup(cuda_fail(e, "FP64 table allocation"));
   std::vector<double> t64((size_t)2 * A * A + A + R + A);
   std::copy(evecs, evecs + A * A, t64.begin());
   std::copy(S64.begin(), S64.end(), t64.begin() + A * A);
   std::copy(evals, evals + A, t64.begin() + 2 * A * A);
   std::copy(dist, dist + R, t64.begin() + 2 * A * A + A);
   std::copy(pi, pi + A, t64.begin() + 2 * A * A + A + R);
-  e = cudaMemcpy(P->d_tab64, t64.data(), sizeof(double) * t64.size(), cudaMemcpyHostToDevice);
-  if (e != cudaSuccess) return cleanup(cuda_fail(e, "cudaMemcpy(tables64)"));
+  e = cudaMemcpyAsync(P->d_tab64, t64.data(), sizeof(double) * t64.size(), cudaMemcpyHostToDevice, qs);
+  if (e != cudaSuccess) return cleanup(cuda_fail(e, "FP64 table upload"));
   if (P->nInt > 0) {
-    e = cudaMalloc(&P->d_steps, sizeof(int4) * P->nInt);
-    if (e == cudaSuccess) e = cudaMalloc(&P->d_slots, sizeof(int4) * P->nInt);
+    e = pool_alloc((void **)&P->d_steps, sizeof(int4) * P->nInt, P->pool, qs);
+    if (e == cudaSuccess) e = pool_alloc((void **)&P->d_slots, sizeof(int4) * P->nInt, P->pool, qs);
     if (e == cudaSuccess)
-      e = cudaMemcpy(P->d_steps, P->steps.data(), sizeof(int4) * P->nInt, cudaMemcpyHostToDevice);
+      e = cudaMemcpyAsync(P->d_steps, P->steps.data(), sizeof(int4) * P->nInt, cudaMemcpyHostToDevice, qs);
     if (e == cudaSuccess)
-      e = cudaMemcpy(P->d_slots, P->slots.data(), sizeof(int4) * P->nInt, cudaMemcpyHostToDevice);
+      e = cudaMemcpyAsync(P->d_slots, P->slots.data(), sizeof(int4) * P->nInt, cudaMemcpyHostToDevice, qs);
     if (e != cudaSuccess) return cleanup(cuda_fail(e, "schedule upload"));
   }
   if (P->prog_steps > 0) {
-    e = cudaMalloc(&P->d_prog, sizeof(int4) * P->prog.size());
+    e = pool_alloc((void **)&P->d_prog, sizeof(int4) * P->prog.size(), P->pool, qs);
     if (e == cudaSuccess)
-      e = cudaMemcpy(P->d_prog, P->prog.data(), sizeof(int4) * P->prog.size(), cudaMemcpyHostToDevice);
+      e = cudaMemcpyAsync(P->d_prog, P->prog.data(), sizeof(int4) * P->prog.size(), cudaMemcpyHostToDevice, qs);
     if (e != cudaSuccess) return cleanup(cuda_fail(e, "program upload"));
   }
   {
     const int tm = R * A;
-    k_compute_M<<<std::max(1, std::min((tm + 127) / 128, 4096)), 128>>>(
+    k_compute_M<<<std::max(1, std::min((tm + 127) / 128, 4096)), 128, 0, qs>>>(
         P->d_tab64, P->d_tab64 + 2 * A * A, P->d_tab64 + 2 * A * A + A, P->d_tab64 + 2 * A * A + A + R, R, A,
         P->d_tab + o.MT, P->d_tab + o.MN);
     e = cudaGetLastError();
     if (e != cudaSuccess) return cleanup(cuda_fail(e, "M(t) prologue"));
     const int total = R * A * A;
     const int blk = 256, grd = std::max(1, std::min((total + blk - 1) / blk, 4096));
-    k_compute_J<<<grd, blk>>>(P->d_tab64 + 2 * A * A, P->d_tab64 + 2 * A * A + A, R, A,
+    k_compute_J<<<grd, blk, 0, qs>>>(P->d_tab64 + 2 * A * A, P->d_tab64 + 2 * A * A + A, R, A,
                               P->d_tab + o.J, P->d_tab + o.JT);
     e = cudaGetLastError();
     if (e == cudaSuccess && A <= 8) {
       const int tk = R * (A + 1) * A * A;
-      k_compute_K<<<std::max(1, std::min((tk + 255) / 256, 4096)), 256>>>(P->d_tab + o.J, P->d_tab + o.Ut, R, A,
+      k_compute_K<<<std::max(1, std::min((tk + 255) / 256, 4096)), 256, 0, qs>>>(P->d_tab + o.J, P->d_tab + o.Ut, R, A,
                                                                          P->d_tab + o.K);
       e = cudaGetLastError();
     }
     if (e == cudaSuccess && A == 64) {
-      e = cudaMalloc(&P->d_tab16, sizeof(uint16_t) * (size_t)(2 * R + 2) * 12288);
+      e = pool_alloc((void **)&P->d_tab16, sizeof(uint16_t) * (size_t)(2 * R + 2) * 12288, P->pool, qs);
       if (e == cudaSuccess) {
         const int tt = (2 * R + 2) * 4096;
-        k_pack16<<<std::max(1, std::min((tt + 255) / 256, 8192)), 256>>>(P->d_tab + o.MN, P->d_tab + o.Vd,
+        k_pack16<<<std::max(1, std::min((tt + 255) / 256, 8192)), 256, 0, qs>>>(P->d_tab + o.MN, P->d_tab + o.Vd,
                                                                          P->d_tab + o.Vu, R, P->d_tab16);
         e = cudaGetLastError();
       }
     }
-    if (e == cudaSuccess) e = cudaMalloc(&P->d_err, sizeof(int));
-    if (e == cudaSuccess) e = cudaMemset(P->d_err, 0, sizeof(int));
-    if (e == cudaSuccess) e = cudaDeviceSynchronize();
+    if (e == cudaSuccess) e = pool_alloc((void **)&P->d_err, sizeof(int), P->pool, qs);
+    if (e == cudaSuccess) e = cudaMemsetAsync(P->d_err, 0, sizeof(int), qs);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(qs);
     if (e != cudaSuccess) return cleanup(cuda_fail(e, "J(t) prologue"));
   }
   *out = P;
@@ -511,18 +568,26 @@ int subby_plan_create(const int32_t *parent, const double *dist, const double *e
 
 int subby_plan_destroy(subby_plan *P) {
   if (!P) return SUBBY_OK;
-  if (P->d_tab) cudaFree(P->d_tab);
-  if (P->d_tab64) cudaFree(P->d_tab64);
-  if (P->d_steps) cudaFree(P->d_steps);
-  if (P->d_slots) cudaFree(P->d_slots);
-  if (P->d_prog) cudaFree(P->d_prog);
-  if (P->d_tab16) cudaFree(P->d_tab16);
-  if (P->d_err) cudaFree(P->d_err);
-  P->work.release();
-  P->io.release();
+  int cur = 0;
+  cudaGetDevice(&cur);
+  if (cur != P->device) cudaSetDevice(P->device);
+  // frees are ordered after the plan's last enqueued kernel; nothing here
+  // waits for the device
+  cudaStream_t s = P->s_prep;
+  if (s && P->used) cudaStreamWaitEvent(s, P->last_use, 0);
+  if (P->s_in) cudaStreamSynchronize(P->s_in);
+  if (P->s_out) cudaStreamSynchronize(P->s_out);
+  void *bufs[] = {P->d_tab, P->d_tab64, P->d_steps, P->d_slots, P->d_prog, P->d_tab16, P->d_err};
+  for (void *b : bufs)
+    if (b) cudaFreeAsync(b, s);
+  P->work.release(s);
+  P->io.release(s);
   for (cudaEvent_t e : P->ev) cudaEventDestroy(e);
+  if (P->last_use) cudaEventDestroy(P->last_use);
   if (P->s_in) cudaStreamDestroy(P->s_in);
   if (P->s_out) cudaStreamDestroy(P->s_out);
+  if (s) cudaStreamDestroy(s);
+  if (cur != P->device) cudaSetDevice(cur);
   delete P;
   return SUBBY_OK;
 }
@@ -744,6 +809,13 @@ int plan_tree4(subby_plan *P, int mode, int C, Launch &L) {
 // staging (2 (R-1) A floats per column) stays within kStageBudget bytes.
 constexpr size_t kStageBudget = size_t(1) << 30;
 
+// Marks the end of the work just enqueued on `stream` as the plan's last use.
+int mark_use(subby_plan *P, cudaStream_t stream) {
+  CU(cudaEventRecord(P->last_use, stream));
+  P->used = true;
+  return 0;
+}
+
 int run_big(subby_plan *P, const int32_t *d_aln, int C, float *d_logL, float *d_counts, float *d_root,
             int mode, int mask_mode, const uint8_t *d_mask, cudaStream_t stream) {
   const int A = P->A, R = P->R;
@@ -787,7 +859,8 @@ int run_big(subby_plan *P, const int32_t *d_aln, int C, float *d_logL, float *d_
   const size_t stage_floats = counts ? (size_t)(R - 1) * chunk * A : 0;
   auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
   int rc;
-  if ((rc = P->work.grow(al(slot_floats * 4) + al(slot_ints * 4) + 2 * al(stage_floats * 4) + 256))) return rc;
+  if ((rc = P->grow(P->work, al(slot_floats * 4) + al(slot_ints * 4) + 2 * al(stage_floats * 4) + 256, stream)))
+    return rc;
   char *base = (char *)P->work.p;
   k.scrV = (float *)base;
   base += al(slot_floats * 4);
@@ -815,7 +888,7 @@ int run_big(subby_plan *P, const int32_t *d_aln, int C, float *d_logL, float *d_
       g_launches += 1;
     }
   }
-  return 0;
+  return mark_use(P, stream);
 }
 
 // Columns per chunk of the host-pointer pipeline: whole waves of the
@@ -885,7 +958,7 @@ int run_common(subby_plan *P, const int32_t *d_aln, int C, float *d_logL, float 
   const size_t vbytes = (tree && !L.global_slots) ? 0 : nsl * L.nworkers * P->A * sizeof(float);
   const size_t wbytes = (tree && !L.global_slots) ? 0 : nsl * L.nworkers * 2 * sizeof(int);
   const size_t vb_al = (vbytes + 255) & ~(size_t)255;
-  if ((rc = P->work.grow(vb_al + wbytes + 256))) return rc;
+  if ((rc = P->grow(P->work, vb_al + wbytes + 256, stream))) return rc;
   k.scrV = (float *)P->work.p;
   k.scrW = (int *)((char *)P->work.p + vb_al);
   if (grid_out) *grid_out = L.grid;
@@ -896,7 +969,7 @@ int run_common(subby_plan *P, const int32_t *d_aln, int C, float *d_logL, float 
   if (lr != 0) return fail(SUBBY_ERR_CUDA, std::string("kernel launch failed: ") +
                                                cudaGetErrorString((cudaError_t)lr));
   g_launches += 1;
-  return 0;
+  return mark_use(P, stream);
 }
 
 }  // namespace
@@ -950,7 +1023,7 @@ int subby_plan_run(subby_plan *P, const int32_t *aln, int C, float *logL, float 
   const size_t b_rp = rootProb ? (size_t)A * C * 4 : 0;
   auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
   const size_t total = al(b_aln) + al(b_mask) + al(b_ll) + al(b_ct) + al(b_rp);
-  if ((rc = P->io.grow(total))) return rc;
+  if ((rc = P->grow(P->io, total, stream))) return rc;
   char *base = (char *)P->io.p;
   int32_t *d_aln = (int32_t *)base;
   base += al(b_aln);
@@ -1013,9 +1086,11 @@ int subby_plan_run(subby_plan *P, const int32_t *aln, int C, float *logL, float 
   }
   if (P->d_err) {
     int dev_err = 0;
-    CU(cudaMemcpy(&dev_err, P->d_err, sizeof(int), cudaMemcpyDeviceToHost));
+    CU(cudaMemcpyAsync(&dev_err, P->d_err, sizeof(int), cudaMemcpyDeviceToHost, stream));
+    CU(cudaStreamSynchronize(stream));
     if (dev_err) {
-      cudaMemset(P->d_err, 0, sizeof(int));
+      cudaMemsetAsync(P->d_err, 0, sizeof(int), stream);
+      cudaStreamSynchronize(stream);
       return fail(SUBBY_ERR_TIMEOUT, "a bounded device wait gave up (tensor-core walk)");
     }
   }
@@ -1041,7 +1116,7 @@ int subby_plan_grad(subby_plan *P, const int32_t *aln, int C, const float *g, fl
   int rc = 0;
   if (!dev) {
     const size_t b_aln = (size_t)R * C * 4, b_g = g ? (size_t)C * 4 : 0, b_ll = logL ? (size_t)C * 4 : 0;
-    if ((rc = P->io.grow(al(b_aln) + al(b_g) + al(b_ll)))) return rc;
+    if ((rc = P->grow(P->io, al(b_aln) + al(b_g) + al(b_ll), stream))) return rc;
     char *base = (char *)P->io.p;
     int32_t *a = (int32_t *)base;
     base += al(b_aln);
@@ -1062,21 +1137,22 @@ int subby_plan_grad(subby_plan *P, const int32_t *aln, int C, const float *g, fl
   const size_t nb = (size_t)L.grid;
   double *d_part = nullptr;
   const size_t pbytes = nb * ((size_t)R + (size_t)A * A) * sizeof(double);
-  CU(cudaMalloc(&d_part, pbytes));
+  CU(pool_alloc((void **)&d_part, pbytes, P->pool, stream));
   CU(cudaMemsetAsync(d_part, 0, pbytes, stream));
   int grid = 0;
   rc = run_common(P, d_aln, C, d_ll, nullptr, nullptr, mode, SUBBY_MASK_NONE, nullptr, d_g, d_part,
                   d_part + nb * R, &grid, stream);
   if (rc) {
-    cudaFree(d_part);
+    cudaFreeAsync(d_part, stream);
+    cudaStreamSynchronize(stream);
     return rc;
   }
   std::vector<double> part(nb * ((size_t)R + (size_t)A * A));
   cudaError_t e = cudaMemcpyAsync(part.data(), d_part, pbytes, cudaMemcpyDeviceToHost, stream);
   if (e == cudaSuccess && logL && !dev)
     e = cudaMemcpyAsync(logL, d_ll, (size_t)C * 4, cudaMemcpyDeviceToHost, stream);
+  if (e == cudaSuccess) e = cudaFreeAsync(d_part, stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
-  cudaFree(d_part);
   if (e != cudaSuccess) return cuda_fail(e, "gradient readback");
   if ((size_t)grid != nb) return fail(SUBBY_ERR_CUDA, "grid mismatch");
   for (int n = 0; n < R; ++n) {

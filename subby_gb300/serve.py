@@ -57,6 +57,11 @@ class Job:
     def latency(self):
         return self.finish - self.arrival
 
+    def release(self):
+        """Drop the results (pinned host buffers go back to the host cache)."""
+        self.result = {}
+        self._pinned = None
+
     @property
     def RC(self):
         return tuple(self.shape) if self.shape is not None else tuple(self.alignment.shape)
@@ -96,6 +101,7 @@ class Server:
         self.inflight = []           # (job, slot, event, bytes, bufs)
         self.used_bytes = 0
         self.completed = []
+        self.on_done = None
         self.lock = threading.Lock()
 
     # ------------------------------------------------------------------ plans
@@ -171,21 +177,28 @@ class Server:
         for job, slot, ev, nbytes, bufs in self.inflight:
             if ev.query():
                 job.finish = now_fn()
+                # numpy views of the pinned result buffers; Job.release()
+                # hands the buffers back to the host allocator's cache
                 job.result = {k: v.numpy() for k, v in bufs[3].items()}
+                job._pinned = bufs[3]
                 self.free_slots.append(slot)
                 self.used_bytes -= nbytes
                 self.completed.append(job)
                 done += 1
+                if self.on_done is not None:
+                    self.on_done(job)
             else:
                 keep.append((job, slot, ev, nbytes, bufs))
         self.inflight = keep
         return done
 
     # ------------------------------------------------------------------- run
-    def run(self, jobs, realtime: bool = True, on_admit=None):
+    def run(self, jobs, realtime: bool = True, on_admit=None, on_done=None):
         """Serve ``jobs`` (sorted by ``arrival``).  With ``realtime`` the loop
         admits a job only once the wall clock reaches its arrival time;
-        otherwise all jobs are available at t=0.  Returns the completed jobs."""
+        otherwise all jobs are available at t=0.  ``on_done(job)`` runs as
+        each job's results land in host memory.  Returns the completed jobs."""
+        self.on_done = on_done
         t0 = time.perf_counter()
         now = lambda: time.perf_counter() - t0  # noqa: E731
         pending = collections.deque(sorted(jobs, key=lambda j: j.arrival))

@@ -807,7 +807,7 @@ int plan_tree4(subby_plan *P, int mode, int C, Launch &L) {
 // CTA, stored-node slots in global memory) then, for Counts, k_acc over the
 // staged per-branch vectors.  Columns are processed in chunks so that the
 // staging (2 (R-1) A floats per column) stays within kStageBudget bytes.
-constexpr size_t kStageBudget = size_t(1) << 30;
+constexpr size_t kStageBudget = size_t(4) << 30;
 
 // Marks the end of the work just enqueued on `stream` as the plan's last use.
 int mark_use(subby_plan *P, cudaStream_t stream) {
@@ -851,7 +851,10 @@ int run_big(subby_plan *P, const int32_t *d_aln, int C, float *d_logL, float *d_
     const size_t per_col = (size_t)2 * (R - 1) * A * sizeof(float);
     size_t cmax = std::max<size_t>(tile, kStageBudget / per_col);
     cmax = cmax / tile * tile;
-    chunk = (int)std::min<size_t>((size_t)C, cmax);
+    // equal chunks (whole tiles), so the last one is not a sliver
+    const size_t nch = ((size_t)C + cmax - 1) / cmax;
+    const size_t even = ((size_t)C + nch - 1) / nch;
+    chunk = (int)std::min<size_t>((size_t)C, (even + tile - 1) / tile * tile);
   }
   const int walk_grid = std::max(1, std::min((chunk + tile - 1) / tile, P->nsm * (H == 2 ? 1 : 2)));
   const size_t slot_floats = (size_t)walk_grid * k.nslots * tile * A;

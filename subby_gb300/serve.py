@@ -16,7 +16,12 @@ Jobs (alignment, tree, model, options) arrive over time.  The loop
 * never runs two jobs of the same plan at once (a plan's workspace is
   per-plan), so such a job waits for its twin to finish;
 * completes jobs in whatever order their streams finish and records, per job,
-  the latency from arrival to results-in-host-memory.
+  the latency from arrival to results-in-host-memory;
+* estimates each job's device time from its shape (``job_cost_ms``): short
+  jobs go to high-priority streams, so the block scheduler starts their
+  kernels ahead of queued work of long jobs, and long jobs are cut into
+  column slices of about ``slice_ms`` each (whole 128-column tiles), so a
+  short job waits for at most one slice rather than a whole long job.
 
 Results of a job do not depend on what else is in flight: every job runs the
 same kernel on the same inputs as it would alone (``tests/test_gpu_serving``
@@ -75,12 +80,31 @@ def _plan_key(tree, model):
     return h.hexdigest()
 
 
+STAGE_CAP = 4 << 30   # per-plan staging cap of the large-alphabet path (bytes)
+
+# Device time per (column x tree node), ns, by path (GB300, Counts): used only
+# to order and slice work, never to skip any.
+_NS_PER_COL_NODE = {("4", False): 0.012, ("4", True): 0.011, ("16", False): 0.20, ("16", True): 0.05,
+                    ("64", False): 1.6, ("64", True): 0.30}
+
+
+def job_cost_ms(R: int, C: int, A: int, f81: bool = False) -> float:
+    """Estimated device time of one job's Counts call (ms)."""
+    key = ("4" if A <= 8 else "16" if A <= 20 else "64", bool(f81))
+    return _NS_PER_COL_NODE[key] * R * C * 1e-6
+
+
 def job_device_bytes(R: int, C: int, A: int) -> int:
-    """Device footprint estimate of one in-flight job (bytes)."""
+    """Device footprint estimate of one in-flight job (bytes): plan tables,
+    tokens, outputs and the plan's scratch (per-branch staging of the
+    large-alphabet Counts path, capped per plan; slot scratch otherwise)."""
     tables = 4 * R * (A + 1) * A * 6 + 4 * R * (A + 1) * (A * A + 4) * (A <= 8)
     tokens = 4 * R * C
     outputs = 4 * C * (A * A + A + 1)
-    scratch = 4 * R * (A + 2) * min(C, 152 * 256)
+    if A >= 16:
+        scratch = min(STAGE_CAP, 8 * (R - 1) * A * C) + 4 * R * (A + 1) * min(C, 152 * 128)
+    else:
+        scratch = 4 * R * (A + 2) * min(C, 152 * 256)
     return tables + tokens + outputs + scratch
 
 
@@ -88,13 +112,17 @@ class Server:
     """Continuous batching over CUDA streams with memory-budget admission."""
 
     def __init__(self, max_inflight: int = 8, device_budget: int = 16 << 30, plan_cache: int = 64,
-                 device=None):
+                 device=None, short_ms: float = 5.0, slice_ms: float = 8.0):
         import torch
         self.torch = torch
         self.device = torch.device("cuda", torch.cuda.current_device() if device is None else device)
         self.max_inflight = max_inflight
         self.budget = device_budget
+        self.short_ms = short_ms
+        self.slice_ms = slice_ms
+        # one normal- and one high-priority stream per slot
         self.streams = [torch.cuda.Stream(device=self.device) for _ in range(max_inflight)]
+        self.hi_streams = [torch.cuda.Stream(device=self.device, priority=-8) for _ in range(max_inflight)]
         self.free_slots = list(range(max_inflight))
         self.plans = collections.OrderedDict()
         self.plan_cache = plan_cache
@@ -132,9 +160,12 @@ class Server:
         A = len(ensure_diag(job.model).pi)
         nbytes = job_device_bytes(R, C, A)
         slot = self.free_slots.pop()
-        stream = self.streams[slot]
+        cost = job_cost_ms(R, C, A, job.f81)
+        stream = (self.hi_streams if cost <= self.short_ms else self.streams)[slot]
         plan = self.plan_for(job.tree, job.model, self._key(job))
         h_aln = None
+        kw = dict(loglike="logLike" in job.want, counts="counts" in job.want,
+                  rootprob="rootProb" in job.want, f81=job.f81, branch_mask=job.branch_mask)
         with torch.cuda.stream(stream):
             if callable(job.alignment):
                 d_aln = job.alignment(stream, self.device)
@@ -145,9 +176,23 @@ class Server:
                 if not h_aln.is_pinned():
                     h_aln = h_aln.pin_memory()
                 d_aln = h_aln.to(self.device, non_blocking=True)
-            res = plan.run(d_aln, loglike="logLike" in job.want, counts="counts" in job.want,
-                           rootprob="rootProb" in job.want, f81=job.f81,
-                           branch_mask=job.branch_mask, stream=stream)
+            nsl = max(1, min(int(np.ceil(cost / self.slice_ms)), (C + 127) // 128))
+            if nsl == 1 or not isinstance(job.branch_mask, str):
+                res = plan.run(d_aln, stream=stream, **kw)
+            else:
+                # long job: column slices of whole 128-column tiles, each its
+                # own launch sequence, results gathered on the device
+                edges = [min(C, ((C * i // nsl) + 127) // 128 * 128) for i in range(nsl)] + [C]
+                res = None
+                for c0, c1 in zip(edges[:-1], edges[1:]):
+                    if c1 <= c0:
+                        continue
+                    part = plan.run(d_aln[:, c0:c1].contiguous(), stream=stream, **kw)
+                    if res is None:
+                        res = {k: torch.empty(v.shape[:-1] + (C,), dtype=v.dtype, device=v.device)
+                               for k, v in part.items()}
+                    for k, v in part.items():
+                        res[k][..., c0:c1].copy_(v)
             host = {}
             for k, v in res.items():
                 hv = torch.empty(v.shape, dtype=v.dtype, pin_memory=True)

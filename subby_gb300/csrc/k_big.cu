@@ -680,7 +680,9 @@ __global__ void __launch_bounds__(256, 1) k_acc(const KParams P, const float *__
     // accumulators: ac2[a][p][q] = (C[k0+a][l0+2p], C[k0+a][l0+2p+1]) of column q
     float2 ac2[4][2][8];
 #define ACC(a, b, q) (((b) & 1) ? ac2[a][(b) >> 1][q].y : ac2[a][(b) >> 1][q].x)
-    float hv[4][8], gv[4][8], zv[8];
+    // F81: per-column h (rows), g (columns) and z, one element set per thread
+    constexpr int NE = (G * A + 255) / 256;
+    float hreg[NE], greg[NE], zreg = 0.f;
 #pragma unroll
     for (int a = 0; a < 4; ++a)
 #pragma unroll
@@ -689,11 +691,7 @@ __global__ void __launch_bounds__(256, 1) k_acc(const KParams P, const float *__
         for (int q = 0; q < 8; ++q) ac2[a][pp][q] = make_float2(0.f, 0.f);
     if (F81) {
 #pragma unroll
-      for (int a = 0; a < 4; ++a)
-#pragma unroll
-        for (int q = 0; q < 8; ++q) hv[a][q] = gv[a][q] = 0.f;
-#pragma unroll
-      for (int q = 0; q < 8; ++q) zv[q] = 0.f;
+      for (int r = 0; r < NE; ++r) hreg[r] = greg[r] = 0.f;
     }
     // a short last group: zero the unused column rows of every stage once
     // (the copies below fill only gcols rows)
@@ -740,17 +738,38 @@ __global__ void __launch_bounds__(256, 1) k_acc(const KParams P, const float *__
       const float *cur = sm + st * Rg::STAGE;
       if (!mbar_wait((uint32_t)__cvta_generic_to_shared(&mbar[st]), (it / S) & 1)) s_err = 1;
       if (F81) {
-        if (t < G) {
-          const float *Ds = cur + t * A, *U = cur + G * A + t * A;
+        // pi . U and sum(s D) per column: one warp per column, shuffle sums
+        const int warp = t >> 5, lane = t & 31;
+        for (int c = warp; c < G; c += 8) {
+          const float *Ds = cur + c * A, *U = cur + G * A + c * A;
           float piU = 0.f, dsum = 0.f;
-          for (int a = 0; a < A; ++a) {
-            piU = fmaf(__ldg(pig + a), U[a], piU);
+          for (int a = lane; a < A; a += 32) {
+            piU = fmaf(pis[a], U[a], piU);
             dsum += Ds[a];
           }
-          scal[2 * t] = piU;
-          scal[2 * t + 1] = dsum;
+#pragma unroll
+          for (int o = 16; o > 0; o >>= 1) {
+            piU += __shfl_xor_sync(0xffffffffu, piU, o);
+            dsum += __shfl_xor_sync(0xffffffffu, dsum, o);
+          }
+          if (lane == 0) {
+            scal[2 * c] = piU;
+            scal[2 * c + 1] = dsum;
+          }
         }
         __syncthreads();
+        // h_i += beta piU (s D)_i, g_j += beta sum(s D) U_j, z += gamma sum(s D) piU
+        const float4 abg = __ldg(reinterpret_cast<const float4 *>(F8) + n + 1);
+#pragma unroll
+        for (int r = 0; r < NE; ++r) {
+          const int e = t + 256 * r;
+          if (NE * 256 == G * A || e < G * A) {
+            const int c = e / A;
+            hreg[r] = fmaf(abg.y * scal[2 * c], cur[e], hreg[r]);
+            greg[r] = fmaf(abg.y * scal[2 * c + 1], cur[G * A + e], greg[r]);
+          }
+        }
+        if (t < G) zreg = fmaf(abg.z * scal[2 * t + 1], scal[2 * t], zreg);
       }
       if (active) {
         const float *da = cur + (F81 ? 0 : A * A), *db = da + G * A;
@@ -783,22 +802,17 @@ __global__ void __launch_bounds__(256, 1) k_acc(const KParams P, const float *__
 #pragma unroll
           for (int q = 0; q < 8; ++q) {
             const int cc = grp * 8 + q;
-            const float *Ds = da + cc * A, *U = db + cc * A;
-            const float piU = scal[2 * cc], dsum = scal[2 * cc + 1];
-            const float4 d = *reinterpret_cast<const float4 *>(Ds + k0);
-            const float4 u = *reinterpret_cast<const float4 *>(U + l0);
-            const float dk[4] = {d.x, d.y, d.z, d.w}, ul[4] = {u.x, u.y, u.z, u.w};
-            const float2 up[2] = {make_float2(ul[0], ul[1]), make_float2(ul[2], ul[3])};
+            const float4 d = *reinterpret_cast<const float4 *>(da + cc * A + k0);
+            const float4 u = *reinterpret_cast<const float4 *>(db + cc * A + l0);
+            const float dk[4] = {d.x, d.y, d.z, d.w};
+            const float2 up[2] = {make_float2(u.x, u.y), make_float2(u.z, u.w)};
 #pragma unroll
             for (int a = 0; a < 4; ++a) {
               const float ad = abg.x * dk[a];
               const float2 dd = make_float2(ad, ad);
 #pragma unroll
               for (int pp = 0; pp < 2; ++pp) ac2[a][pp][q] = __ffma2_rn(dd, up[pp], ac2[a][pp][q]);
-              hv[a][q] = fmaf(abg.y * piU, dk[a], hv[a][q]);
-              gv[a][q] = fmaf(abg.y * dsum, ul[a], gv[a][q]);
             }
-            zv[q] = fmaf(abg.z * dsum, piU, zv[q]);
           }
         }
       }
@@ -807,7 +821,18 @@ __global__ void __launch_bounds__(256, 1) k_acc(const KParams P, const float *__
     // ------------------------------------------------------------- epilogue
     const int col0 = c_base + g0 + grp * 8, ncols = gcols - grp * 8;
     if (F81) {
-      // every (k, l) block accumulated h for its rows and g for its columns
+      // h, g, z of every column through shared memory to the (k, l) blocks
+      float *Hs = pis + A, *Gs = Hs + G * A, *Zs = Gs + G * A;
+#pragma unroll
+      for (int r = 0; r < NE; ++r) {
+        const int e = t + 256 * r;
+        if (NE * 256 == G * A || e < G * A) {
+          Hs[e] = hreg[r];
+          Gs[e] = greg[r];
+        }
+      }
+      if (t < G) Zs[t] = zreg;
+      __syncthreads();
       if (active && ncols > 0) {
         const float mu = P.f81_mu;
 #pragma unroll
@@ -818,7 +843,10 @@ __global__ void __launch_bounds__(256, 1) k_acc(const KParams P, const float *__
             const float pi_i = pis[i], f = (i == j) ? 1.f : mu * pis[j];
             float v[8];
 #pragma unroll
-            for (int q = 0; q < 8; ++q) v[q] = f * (ACC(a, b, q) + hv[a][q] + pi_i * (gv[b][q] + zv[q]));
+            for (int q = 0; q < 8; ++q) {
+              const int cc = grp * 8 + q;
+              v[q] = f * (ACC(a, b, q) + Hs[cc * A + i] + pi_i * (Gs[cc * A + j] + Zs[cc]));
+            }
             store8((size_t)(i * A + j), v, col0, ncols);
           }
       }
@@ -964,7 +992,7 @@ template <int A>
 int acc_launch(const KParams &p, bool f81, const float *sa, const float *sb, int c_base, int c_count, int grid,
                cudaStream_t s) {
   using Gm = AccGeo<A>;
-  const size_t smem = (size_t)(AccRing<A>::SCAL + 2 * Gm::G + 2 * A * A + A) * sizeof(float);
+  const size_t smem = (size_t)(AccRing<A>::SCAL + 2 * Gm::G + 2 * A * A + A + 2 * Gm::G * A + Gm::G) * sizeof(float);
   cudaError_t e;
   if (f81) {
     e = cudaFuncSetAttribute(k_acc<A, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);

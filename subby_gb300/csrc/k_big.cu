@@ -65,6 +65,8 @@ __device__ __forceinline__ uint64_t umma_desc(uint32_t saddr) {
 // kind::f16, BF16 x BF16 -> F32, K-major A and B, M = 128, N = 64
 constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(64 >> 3) << 17) |
                             ((uint32_t)(128 >> 4) << 24);
+constexpr uint32_t kIdesc128 = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(128 >> 3) << 17) |
+                               ((uint32_t)(128 >> 4) << 24);
 constexpr int kWaitLimit = 1 << 24;  // bounded mbarrier waits
 
 __device__ __forceinline__ bool mbar_wait(uint32_t mb, uint32_t phase) {
@@ -79,12 +81,19 @@ __device__ __forceinline__ bool mbar_wait(uint32_t mb, uint32_t phase) {
   return false;
 }
 
+// Shared-memory operand layout of the tensor-core walk (dynamic, 168 KB):
+//   sA   [0,   48K)  A operand 0: three BF16 terms of 16 KB (128 columns x 64)
+//   sA1  [48K, 96K)  A operand 1 (the U of an outside-pass product)
+//   sB2  [96K,144K)  three terms of 16 KB, each [per-node matrix 8 KB | Vd 8 KB]:
+//                    a stacked 128 x 64 B operand [MN_n ; Vd^T-tile] (N = 128)
+//   sBu  [144K,168K) Vu tile, three terms of 8 KB
+// Vd and Vu are loaded once per CTA; per-node matrices per product.
+constexpr uint32_t kSA1 = 49152, kSB2 = 98304, kSBu = 147456, kTcDyn = 172032;
 struct TcState {
-  uint32_t tmem;    // accumulator: 128 lanes x 64 fp32 columns
-  uint32_t sA;      // A operand: three BF16 terms of 16 KB each, shared address
-  uint32_t sB;      // B operand: three BF16 terms of 8 KB each
+  uint32_t tmem;    // accumulators: 128 lanes x 192 fp32 columns (O | dt | ut)
+  uint32_t sA;      // shared address of the operand area
   uint32_t mbB, mbM;
-  uint32_t nmv;     // matvecs issued (mbarrier phase)
+  uint32_t nB, nM;  // completed phases of the copy and MMA mbarriers
   int *err;         // shared: set when a bounded wait gives up
 };
 
@@ -106,17 +115,9 @@ struct Walk {
   // two-term split measured 1.5e-4 column-wise counts error at A = 64).
   // Bg: the B tile's three terms (4096 elements each) in the canonical
   // layout in global memory, brought in by bulk copies.
-  __device__ __forceinline__ void matvec_tc(BV<A> &y, const BV<A> &x, const uint16_t *Bg) {
-    static_assert(A == 64, "tensor-core walk is A = 64");
-    TcState &T = tcs;
-    const uint32_t phase = T.nmv & 1;
-    if (threadIdx.x == 0) {
-      asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(T.mbB), "r"(3 * 8192) : "memory");
-#pragma unroll
-      for (int part = 0; part < 3; ++part)
-        asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
-                     ::"r"(T.sB + part * 8192), "l"(Bg + part * 4096), "r"(8192), "r"(T.mbB) : "memory");
-    }
+  // x (this thread's 32 states of column c) as three BF16 terms into the
+  // canonical K-major A tile at shared address base
+  __device__ __forceinline__ void stage_x(const BV<A> &x, uint32_t base) const {
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
       uint32_t t1[4], t2[4], t3[4];
@@ -134,40 +135,59 @@ struct Walk {
         t3[pp] = *reinterpret_cast<const uint32_t *>(&b3);
       }
       const uint32_t off = kmaj_off(c, 32 * h + 8 * q);
-      asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};" ::"r"(T.sA + off), "r"(t1[0]), "r"(t1[1]), "r"(t1[2]),
+      asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};" ::"r"(base + off), "r"(t1[0]), "r"(t1[1]), "r"(t1[2]),
                    "r"(t1[3]) : "memory");
-      asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};" ::"r"(T.sA + 16384 + off), "r"(t2[0]), "r"(t2[1]),
+      asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};" ::"r"(base + 16384 + off), "r"(t2[0]), "r"(t2[1]),
                    "r"(t2[2]), "r"(t2[3]) : "memory");
-      asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};" ::"r"(T.sA + 32768 + off), "r"(t3[0]), "r"(t3[1]),
+      asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};" ::"r"(base + 32768 + off), "r"(t3[0]), "r"(t3[1]),
                    "r"(t3[2]), "r"(t3[3]) : "memory");
     }
+  }
+  // bring a per-node B tile (three terms) into the matrix slots of sB2
+  __device__ __forceinline__ void load_node_B(const uint16_t *Bg) {
+    TcState &T = tcs;
+    if (threadIdx.x == 0) {
+      asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(T.mbB), "r"(3 * 8192) : "memory");
+#pragma unroll
+      for (int part = 0; part < 3; ++part)
+        asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                     ::"r"(T.sA + kSB2 + part * 16384), "l"(Bg + part * 4096), "r"(8192), "r"(T.mbB) : "memory");
+    }
+  }
+  // A-tile stores visible to the tensor cores, then every thread past the barrier
+  __device__ __forceinline__ void tc_sync() const {
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-    if (threadIdx.x == 0) {
-      if (!mbar_wait(T.mbB, phase)) *T.err = 1;
-      // (A term, B term) pairs with combined order <= 4
-      constexpr int pa[6] = {0, 0, 1, 0, 1, 2}, pb[6] = {0, 1, 0, 2, 1, 0};
+  }
+  // the six (A term, B term) products with combined order <= 4 over K = 64
+  __device__ __forceinline__ static void mma6(uint32_t d, uint32_t a, uint32_t astride, uint32_t b,
+                                              uint32_t bstride, uint32_t idesc) {
+    constexpr int pa[6] = {0, 0, 1, 0, 1, 2}, pb[6] = {0, 1, 0, 2, 1, 0};
 #pragma unroll
-      for (int ks = 0; ks < 4; ++ks) {
+    for (int ks = 0; ks < 4; ++ks) {
 #pragma unroll
-        for (int prod = 0; prod < 6; ++prod) {
-          const uint32_t a = T.sA + pa[prod] * 16384 + ks * 256;
-          const uint32_t b = T.sB + pb[prod] * 8192 + ks * 256;
-          const uint32_t accum = (ks | prod) != 0;
-          asm volatile("{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
-                       " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}"
-                       ::"r"(T.tmem), "l"(umma_desc(a)), "l"(umma_desc(b)), "r"(kIdesc), "r"(accum) : "memory");
-        }
+      for (int prod = 0; prod < 6; ++prod) {
+        const uint32_t accum = (ks | prod) != 0;
+        asm volatile("{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+                     " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}"
+                     ::"r"(d), "l"(umma_desc(a + pa[prod] * astride + ks * 256)),
+                     "l"(umma_desc(b + pb[prod] * bstride + ks * 256)), "r"(idesc), "r"(accum) : "memory");
       }
-      asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(T.mbM)
-                   : "memory");
     }
-    if (!mbar_wait(T.mbM, phase)) *T.err = 1;
+  }
+  // wait for the MMAs of this round trip
+  __device__ __forceinline__ void mma_wait() {
+    TcState &T = tcs;
+    if (!mbar_wait(T.mbM, T.nM & 1)) *T.err = 1;
+    T.nM += 1;
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  }
+  // this thread's 32 FP32 accumulator columns [col, col + 32) of its lane
+  __device__ __forceinline__ void tm_ld32(BV<A> &y, uint32_t col) const {
     uint32_t r[32];
-    const uint32_t ta = T.tmem + ((uint32_t)(32 * (warp & 3)) << 16) + 32u * h;
+    const uint32_t ta = tcs.tmem + ((uint32_t)(32 * (warp & 3)) << 16) + col;
     asm volatile("tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
                  "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
                  : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
@@ -180,7 +200,71 @@ struct Walk {
     asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
     for (int i = 0; i < 32; ++i) y.v[i] = __uint_as_float(r[i]);
-    T.nmv += 1;
+  }
+
+  // y = (B x) on the tensor cores for the 128 columns of the tile at once:
+  // D[c][b] = sum_j X[c][j] B[b][j].  X and B are each split into three
+  // BF16 terms (v = v1 + v2 + v3, v2 = bf16(v - v1), v3 = bf16(v - v1 - v2))
+  // and the six products with combined order <= 4 (1.1, 1.2, 2.1, 1.3, 2.2,
+  // 3.1) accumulate in FP32 in TMEM, which keeps FP32-level accuracy (the
+  // two-term split measured 1.5e-4 column-wise counts error at A = 64).
+  // Bg: the B tile's three terms (4096 elements each) in the canonical
+  // layout in global memory, brought in by bulk copies.
+  __device__ __forceinline__ void matvec_tc(BV<A> &y, const BV<A> &x, const uint16_t *Bg) {
+    static_assert(A == 64, "tensor-core walk is A = 64");
+    TcState &T = tcs;
+    load_node_B(Bg);
+    stage_x(x, T.sA);
+    tc_sync();
+    if (threadIdx.x == 0) {
+      if (!mbar_wait(T.mbB, T.nB & 1)) *T.err = 1;
+      mma6(T.tmem, T.sA, 16384, T.sA + kSB2, 16384, kIdesc);
+      asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(T.mbM)
+                   : "memory");
+    }
+    T.nB += 1;
+    mma_wait();
+    tm_ld32(y, 32u * h);
+  }
+
+  // Outside-pass products of one branch in a single round trip:
+  //   O = MN_n-product of D and dt = Vd-product of D (stacked, N = 128) when
+  //   MNg is given, dt alone (N = 64) otherwise; ut = Vu-product of U when U
+  //   is given.  dt is scaled by s and stored to pa, ut to pb (when store).
+  __device__ __forceinline__ void outside_tc(BV<A> &O, const BV<A> &D, const BV<A> *U, const uint16_t *MNg,
+                                             float s, float *pa, float *pb, bool store) {
+    TcState &T = tcs;
+    const bool wantO = MNg != nullptr, wantU = U != nullptr;
+    if (wantO) load_node_B(MNg);
+    stage_x(D, T.sA);
+    if (wantU) stage_x(*U, T.sA + kSA1);
+    tc_sync();
+    if (threadIdx.x == 0) {
+      if (wantO) {
+        if (!mbar_wait(T.mbB, T.nB & 1)) *T.err = 1;
+        mma6(T.tmem, T.sA, 16384, T.sA + kSB2, 16384, kIdesc128);
+      } else {
+        mma6(T.tmem + 64, T.sA, 16384, T.sA + kSB2 + 8192, 16384, kIdesc);
+      }
+      if (wantU) mma6(T.tmem + 128, T.sA + kSA1, 16384, T.sA + kSBu, 8192, kIdesc);
+      asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(T.mbM)
+                   : "memory");
+    }
+    if (wantO) T.nB += 1;
+    mma_wait();
+    {
+      BV<A> t;
+      tm_ld32(t, 64u + 32u * h);
+#pragma unroll
+      for (int i = 0; i < 32; ++i) t.v[i] *= s;
+      if (store) st(pa, t);
+    }
+    if (wantU) {
+      BV<A> t;
+      tm_ld32(t, 128u + 32u * h);
+      if (store) st(pb, t);
+    }
+    if (wantO) tm_ld32(O, 32u * h);
   }
 
   __device__ __forceinline__ void ld(BV<A> &o, const float *p) const {  // S contiguous floats
@@ -302,11 +386,11 @@ __global__ void __launch_bounds__(128 * Geo<A>::H, 1) k_walk(const KParams P, fl
   __shared__ __align__(8) uint64_t s_mbar[2];
   __shared__ uint32_t s_taddr;
   __shared__ int s_err;
-  extern __shared__ __align__(1024) unsigned char s_dyn[];  // TC: A (48 KB) + B (24 KB) operands
+  extern __shared__ __align__(1024) unsigned char s_dyn[];  // TC: operand tiles (layout at TcState)
   if constexpr (TC) {
     if ((threadIdx.x >> 5) == 0) {
       const uint32_t dst = (uint32_t)__cvta_generic_to_shared(&s_taddr);
-      asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(dst), "r"(64)
+      asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(dst), "r"(256)
                    : "memory");
       asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     }
@@ -324,11 +408,27 @@ __global__ void __launch_bounds__(128 * Geo<A>::H, 1) k_walk(const KParams P, fl
     if (threadIdx.x == 0) {
       s_tc.tmem = s_taddr;
       s_tc.sA = (uint32_t)__cvta_generic_to_shared(s_dyn);
-      s_tc.sB = s_tc.sA + 49152;
       s_tc.mbB = (uint32_t)__cvta_generic_to_shared(&s_mbar[0]);
       s_tc.mbM = (uint32_t)__cvta_generic_to_shared(&s_mbar[1]);
-      s_tc.nmv = 0;
+      s_tc.nB = 0;
+      s_tc.nM = 0;
       s_tc.err = &s_err;
+      if (MODE == 1) {
+        // Vd (stacked behind the per-node matrix slots) and Vu, once per CTA
+        const uint16_t *Vg = P.tab16 + (size_t)P.R * 24576;
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(s_tc.mbB), "r"(6 * 8192)
+                     : "memory");
+        for (int part = 0; part < 3; ++part) {
+          asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                       ::"r"(s_tc.sA + kSB2 + part * 16384 + 8192), "l"(Vg + part * 4096), "r"(8192),
+                       "r"(s_tc.mbB) : "memory");
+          asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                       ::"r"(s_tc.sA + kSBu + part * 8192), "l"(Vg + 12288 + part * 4096), "r"(8192),
+                       "r"(s_tc.mbB) : "memory");
+        }
+        if (!mbar_wait(s_tc.mbB, 0)) s_err = 1;
+        s_tc.nB = 1;
+      }
     }
     __syncthreads();
     wk.tcs = s_tc;
@@ -479,6 +579,23 @@ __global__ void __launch_bounds__(128 * Geo<A>::H, 1) k_walk(const KParams P, fl
         wk.st(pb, ut);
       }
     };
+    // tensor-core walk, eigen staging: the branch's products in one round
+    // trip (Walk::outside_tc); O receives the MN product when MNg is given
+    BV<A> Onone;
+    auto emit_tc = [&](int n, const BV<A> &D, const BV<A> *U, int leafcode, int eDU, int active, BV<A> &O,
+                       const uint16_t *MNg) {
+      float s = invP * __int_as_float((max(-127, min(127, eDU - eRoot)) + 127) << 23);
+      s = active ? s : 0.f;
+      float *pa = stage_a + ((size_t)(n - 1) * c_count + (valid ? cc0 : c_count - 1)) * A + 32 * h;
+      float *pb = stage_b + ((size_t)(n - 1) * c_count + (valid ? cc0 : c_count - 1)) * A + 32 * h;
+      wk.outside_tc(O, D, leafcode >= 0 ? nullptr : U, MNg, s, pa, pb, valid);
+      if (leafcode >= 0 && valid) {
+        BV<A> ut;
+        wk.ld(ut, Ut + leafcode * A + 32 * h);
+        wk.st(pb, ut);
+      }
+    };
+    constexpr bool kFuse = TC && MODE == 1;
     auto act_of = [&](int n, int stn, int stpar) -> int {
       if (P.mask_mode == kMaskAuto) return stn & stpar;
       if (P.mask_mode == kMaskGiven) return P.mask[(size_t)n * C + col] != 0;
@@ -517,8 +634,12 @@ __global__ void __launch_bounds__(128 * Geo<A>::H, 1) k_walk(const KParams P, fl
         for (int q = 0; q < S; ++q) U.v[q] = nl.cc.v[q] * nr.cc.v[q];
         wk.obs(U, codep);
         const int eUp = nl.e + nr.e + wk.rescale(U);
-        emit(s0.x, D, U, -1, eD + eUp, actp);
-        wk.matvec(O, D, MN + (size_t)s0.x * A * A, P.tab16 + (size_t)s0.x * 24576 + 12288);
+        if constexpr (kFuse) {
+          emit_tc(s0.x, D, &U, -1, eD + eUp, actp, O, P.tab16 + (size_t)s0.x * 24576 + 12288);
+        } else {
+          emit(s0.x, D, U, -1, eD + eUp, actp);
+          wk.matvec(O, D, MN + (size_t)s0.x * A * A, P.tab16 + (size_t)s0.x * 24576 + 12288);
+        }
         wk.obs(O, codep);
         eO = eD + wk.rescale(O);
       }
@@ -534,10 +655,14 @@ __global__ void __launch_bounds__(128 * Geo<A>::H, 1) k_walk(const KParams P, fl
         const int stc = me.init | (stp & me.hh);
         const int actc = act_of(sc.x, stc, stp);
         if (sc.y == -1) {
-          BV<A> U;
-          wk.fill(U, 1.f);
-          wk.obs(U, me.code);
-          emit(sc.x, Dc, U, me.code, eDc, actc);
+          if constexpr (kFuse) {
+            emit_tc(sc.x, Dc, nullptr, me.code, eDc, actc, Onone, nullptr);
+          } else {
+            BV<A> U;
+            wk.fill(U, 1.f);
+            wk.obs(U, me.code);
+            emit(sc.x, Dc, U, me.code, eDc, actc);
+          }
         } else if (sc.y >= 0) {
           __syncwarp();
           wk.st(slotv(sc.y), Dc);
@@ -549,16 +674,21 @@ __global__ void __launch_bounds__(128 * Geo<A>::H, 1) k_walk(const KParams P, fl
           basic(kk[0], gn[0], gks[0]);
           basic(kk[1], gn[1], gks[1]);
           const int dcode = btcode(tok(sc.x), A);
+          BV<A> Oc;
           {
             BV<A> du;
 #pragma unroll
             for (int q = 0; q < S; ++q) du.v[q] = kk[0].cc.v[q] * kk[1].cc.v[q];
             wk.obs(du, dcode);
             wk.rescale(du);  // same exponent as in the gather: eU_c = me.e
-            emit(sc.x, Dc, du, -1, eDc + me.e, actc);
+            if constexpr (kFuse) {
+              emit_tc(sc.x, Dc, &du, -1, eDc + me.e, actc, Oc, P.tab16 + (size_t)sc.x * 24576 + 12288);
+            } else {
+              emit(sc.x, Dc, du, -1, eDc + me.e, actc);
+            }
           }
-          BV<A> Oc;
-          wk.matvec(Oc, Dc, MN + (size_t)sc.x * A * A, P.tab16 + (size_t)sc.x * 24576 + 12288);
+          if constexpr (!kFuse)
+            wk.matvec(Oc, Dc, MN + (size_t)sc.x * A * A, P.tab16 + (size_t)sc.x * 24576 + 12288);
           wk.obs(Oc, dcode);
           const int eOc = eDc + wk.rescale(Oc);
 #pragma unroll
@@ -572,10 +702,14 @@ __global__ void __launch_bounds__(128 * Geo<A>::H, 1) k_walk(const KParams P, fl
             const int stg = g.init | (stc & g.hh);
             const int actg = act_of(gn[gs], stg, stc);
             if (gks[gs] == -1) {
-              BV<A> U;
-              wk.fill(U, 1.f);
-              wk.obs(U, g.code);
-              emit(gn[gs], Dg, U, g.code, eDg, actg);
+              if constexpr (kFuse) {
+                emit_tc(gn[gs], Dg, nullptr, g.code, eDg, actg, Onone, nullptr);
+              } else {
+                BV<A> U;
+                wk.fill(U, 1.f);
+                wk.obs(U, g.code);
+                emit(gn[gs], Dg, U, g.code, eDg, actg);
+              }
             } else {
               wk.st(slotv(gks[gs]), Dg);
               if (h == 0) slotw(gks[gs]) = (eDg << 2) | (stg << 1) | actg;
@@ -590,7 +724,7 @@ __global__ void __launch_bounds__(128 * Geo<A>::H, 1) k_walk(const KParams P, fl
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     if ((threadIdx.x >> 5) == 0)
-      asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(wk.tcs.tmem), "r"(64) : "memory");
+      asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(wk.tcs.tmem), "r"(256) : "memory");
     if (threadIdx.x == 0 && s_err && P.err) atomicAdd(P.err, 1);
   }
 }
@@ -964,7 +1098,7 @@ __global__ void __launch_bounds__(256, 1) k_acc(const KParams P, const float *__
 template <int A, int MODE, bool TC>
 int walk_launch1(const KParams &p, float *sa, float *sb, int c_base, int c_count, int grid, cudaStream_t s) {
   const int threads = 128 * Geo<A>::H;
-  const size_t dyn = TC ? 72 * 1024 + 1024 : 0;
+  const size_t dyn = TC ? kTcDyn + 1024 : 0;
   if (TC) {
     cudaError_t e = cudaFuncSetAttribute(k_walk<A, MODE, TC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
     if (e != cudaSuccess) return (int)e;

@@ -376,11 +376,22 @@ def precision64_bench(args):
         res[name]["loglike_only_columns_per_s"] = C / (ms_ll / 1e3)
     lib.subby_debug_set_kernel(0)
     tc, fp = res["split_bf16_tensor_core"], res["fp32_cuda_core"]
+    # tensor-core roofline of the step: the tree walk's matrix products,
+    # 8 A^2 FLOP per branch (inside M, outside M^T, Vd and Vu products)
+    R = len(w['tree'].parentIndex)
+    flop_col = 8 * 64 * 64 * (R - 1)
+    _, bf16, peak_kind = _peaks()
+    achieved = flop_col * tc["value"] / 1e12
     print(json.dumps({"metric": "Counts columns/s (A=64 reversible, R=127, C=65536)", "value": tc["value"],
                       "unit": UNIT, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
                       "dtype": "fp32 (split-bf16 tensor-core products)", "forced_near_degenerate_pairs": w['forced_pairs'],
                       "tensor_core_vs_fp32_speedup": tc["value"] / fp["value"],
                       "loglike_tensor_core_vs_fp32_speedup": tc["loglike_only_columns_per_s"] / fp["loglike_only_columns_per_s"],
+                      "roofline": {"bound": "tensor", "achieved": achieved, "peak": bf16, "unit": "TFLOP/s",
+                                   "frac": achieved / bf16, "peak_kind": peak_kind, "traffic": None,
+                                   "flop_per_column": flop_col,
+                                   "note": "useful walk FLOP over the whole Counts step; split-BF16 issues 6 "
+                                           "MMAs per product"},
                       "variants": res}))
     return 0
 
@@ -462,6 +473,7 @@ def serving_bench(args):
                       "p99_ms": st['p99_ms'], "max_ms": st['max_ms'], "jobs": st['jobs'],
                       "columns_per_s": st['columns_per_s'], "span_s": st['span_s'], "rate_jobs_per_s": args.rate,
                       "by_kind": by_kind,
+                      "host_s": {k: round(v, 3) for k, v in srv.host_s.items()},
                       "data": "synthetic: per-job random tree and model, uniform device-generated tokens"}))
     return 0
 

@@ -41,6 +41,7 @@ struct TableOffsets {
   int S;     // A x A         : S[i][j] = sum_k V_ik mu_k V_jk
   int ME;    // R x A         : mu_k e^{mu_k t_n} (distance gradient)
   int K;     // R x (A+1) x A x A (A <= 8 only): K[n][code][k][l] = J[n][k][l] Ut[code][l]
+  int EF;    // R x 2         : e^{-mu t_n}, 1 - e^{-mu t_n} (F81 closed form of M(t))
   int total;
 };
 
@@ -93,6 +94,9 @@ struct KParams {
   // (4096 elements each), then [Vd^T 1|2|3 | Vu^T 1|2|3] at R*24576
   const uint16_t *tab16;
   int *err;               // device status: bounded waits that gave up (tensor-core walk)
+  // the model is F81 / JC: M_n = e_n I + (1 - e_n) 1 pi^T, so the walk's
+  // products take the closed form (tables EF) instead of A x A products
+  int f81_model;
 };
 
 // launchers (k_small.cu / k_warp.cu)

@@ -311,6 +311,25 @@ struct Walk {
     for (int i = 0; i < S; ++i) x.v[i] *= s;
     return E - 127;
   }
+  // F81 / JC closed form of the two products with M = e I + (1 - e) 1 pi^T:
+  //   M u     : y_a = e u_a + (1 - e) (pi . u)
+  //   D^T M   : y_b = e D_b + (1 - e) pi_b (sum_a D_a)        (trans)
+  // The column's dot product is combined over its H threads.
+  __device__ __forceinline__ void f81prod(BV<A> &y, const BV<A> &x, float e, float ome, bool trans,
+                                          const BV<A> &piv) const {
+    float sd = 0.f;
+#pragma unroll
+    for (int i = 0; i < S; ++i) sd = trans ? sd + x.v[i] : fmaf(piv.v[i], x.v[i], sd);
+    if constexpr (H == 2) {
+      xch[h * kTile + c] = sd;
+      pair_sync(warp);
+      sd += xch[(1 - h) * kTile + c];
+      pair_sync(warp);
+    }
+    const float q = ome * sd;
+#pragma unroll
+    for (int i = 0; i < S; ++i) y.v[i] = fmaf(e, x.v[i], trans ? q * piv.v[i] : q);
+  }
   // y_b = sum_j T[j][b] x_j over all A inputs j (T rows contiguous, stride A);
   // on the tensor cores when enabled, with Bg the same product's B tile.
   __device__ __forceinline__ void matvec(BV<A> &y, const BV<A> &x, const float *__restrict__ T,
@@ -373,7 +392,9 @@ struct BN {
   int e, hh, init, code;
 };
 
-template <int A, int MODE, bool TC>  // MODE: 0 inside only, 1 eigen staging, 2 F81 staging
+// MODE: 0 inside only, 1 eigen staging, 2 F81 staging; F81M: the model is
+// F81 / JC and the M products take the closed form
+template <int A, int MODE, bool TC, bool F81M>
 __global__ void __launch_bounds__(128 * Geo<A>::H, 1) k_walk(const KParams P, float *__restrict__ stage_a,
                                                               float *__restrict__ stage_b, int c_base,
                                                               int c_count) {
@@ -454,6 +475,18 @@ __global__ void __launch_bounds__(128 * Geo<A>::H, 1) k_walk(const KParams P, fl
   int *sword = P.scrW + (size_t)blockIdx.x * tile_slots;       // [slot][c]
   BV<A> piv;
   wk.ld(piv, pig + 32 * h);
+  const float *EF = P.tab + P.off.EF;
+  constexpr bool f81m = F81M;
+  // the walk's M products: y = M_n x (inside) or y = x^T M_n (outside, trans)
+  auto mprod = [&](BV<A> &y, const BV<A> &x, int n, bool trans) {
+    if constexpr (f81m) {
+      wk.f81prod(y, x, __ldg(EF + 2 * n), __ldg(EF + 2 * n + 1), trans, piv);
+    } else if (trans) {
+      wk.matvec(y, x, MN + (size_t)n * A * A, P.tab16 + (size_t)n * 24576 + 12288);
+    } else {
+      wk.matvec(y, x, MT + (size_t)n * (A + 1) * A, P.tab16 + (size_t)n * 24576);
+    }
+  };
 
   const int ntiles = (c_count + kTile - 1) / kTile;
   for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
@@ -492,7 +525,7 @@ __global__ void __launch_bounds__(128 * Geo<A>::H, 1) k_walk(const KParams P, fl
       o.hh = k0.hh | k1.hh;
       o.init = k0.hh & k1.hh;
       o.code = -1;
-      wk.matvec(o.cc, u, MT + (size_t)n * (A + 1) * A, P.tab16 + (size_t)n * 24576);
+      mprod(o.cc, u, n, false);
     };
 
     // ---------------------------------------------------------------- inside
@@ -526,7 +559,7 @@ __global__ void __launch_bounds__(128 * Geo<A>::H, 1) k_walk(const KParams P, fl
         iRoot = init;
       } else {
         BV<A> cc;
-        wk.matvec(cc, u, MT + (size_t)s0.x * (A + 1) * A, P.tab16 + (size_t)s0.x * 24576);
+        mprod(cc, u, s0.x, false);
         wk.st(slotv(s0.y), cc);
         if (h == 0) slotw(s0.y) = (eU << 2) | (hh << 1) | init;
       }
@@ -635,10 +668,15 @@ __global__ void __launch_bounds__(128 * Geo<A>::H, 1) k_walk(const KParams P, fl
         wk.obs(U, codep);
         const int eUp = nl.e + nr.e + wk.rescale(U);
         if constexpr (kFuse) {
-          emit_tc(s0.x, D, &U, -1, eD + eUp, actp, O, P.tab16 + (size_t)s0.x * 24576 + 12288);
+          if constexpr (f81m) {
+            mprod(O, D, s0.x, true);
+            emit_tc(s0.x, D, &U, -1, eD + eUp, actp, Onone, nullptr);
+          } else {
+            emit_tc(s0.x, D, &U, -1, eD + eUp, actp, O, P.tab16 + (size_t)s0.x * 24576 + 12288);
+          }
         } else {
           emit(s0.x, D, U, -1, eD + eUp, actp);
-          wk.matvec(O, D, MN + (size_t)s0.x * A * A, P.tab16 + (size_t)s0.x * 24576 + 12288);
+          mprod(O, D, s0.x, true);
         }
         wk.obs(O, codep);
         eO = eD + wk.rescale(O);
@@ -682,13 +720,13 @@ __global__ void __launch_bounds__(128 * Geo<A>::H, 1) k_walk(const KParams P, fl
             wk.obs(du, dcode);
             wk.rescale(du);  // same exponent as in the gather: eU_c = me.e
             if constexpr (kFuse) {
-              emit_tc(sc.x, Dc, &du, -1, eDc + me.e, actc, Oc, P.tab16 + (size_t)sc.x * 24576 + 12288);
+              if constexpr (f81m) emit_tc(sc.x, Dc, &du, -1, eDc + me.e, actc, Onone, nullptr);
+              else emit_tc(sc.x, Dc, &du, -1, eDc + me.e, actc, Oc, P.tab16 + (size_t)sc.x * 24576 + 12288);
             } else {
               emit(sc.x, Dc, du, -1, eDc + me.e, actc);
             }
           }
-          if constexpr (!kFuse)
-            wk.matvec(Oc, Dc, MN + (size_t)sc.x * A * A, P.tab16 + (size_t)sc.x * 24576 + 12288);
+          if constexpr (!kFuse || f81m) mprod(Oc, Dc, sc.x, true);
           wk.obs(Oc, dcode);
           const int eOc = eDc + wk.rescale(Oc);
 #pragma unroll
@@ -1095,31 +1133,42 @@ __global__ void __launch_bounds__(256, 1) k_acc(const KParams P, const float *__
 }
 #undef ACC
 
-template <int A, int MODE, bool TC>
+template <int A, int MODE, bool TC, bool F81M>
 int walk_launch1(const KParams &p, float *sa, float *sb, int c_base, int c_count, int grid, cudaStream_t s) {
   const int threads = 128 * Geo<A>::H;
   const size_t dyn = TC ? kTcDyn + 1024 : 0;
   if (TC) {
-    cudaError_t e = cudaFuncSetAttribute(k_walk<A, MODE, TC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
+    cudaError_t e =
+        cudaFuncSetAttribute(k_walk<A, MODE, TC, F81M>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
     if (e != cudaSuccess) return (int)e;
   }
-  k_walk<A, MODE, TC><<<grid, threads, dyn, s>>>(p, sa, sb, c_base, c_count);
+  k_walk<A, MODE, TC, F81M><<<grid, threads, dyn, s>>>(p, sa, sb, c_base, c_count);
   return (int)cudaGetLastError();
+}
+
+// The closed-form F81 walk serves the inside-only and F81-staging modes;
+// eigen staging of an F81 model keeps the general products.
+template <int A, bool TC>
+int walk_launch_tc(const KParams &p, int mode, float *sa, float *sb, int c_base, int c_count, int grid,
+                   cudaStream_t s) {
+  const bool f = !TC && p.f81_model != 0;   // (the tensor-core walk is never F81-specialised)
+  constexpr bool kF = !TC;
+  if (mode == 0)
+    return f ? walk_launch1<A, 0, TC, kF>(p, sa, sb, c_base, c_count, grid, s)
+             : walk_launch1<A, 0, TC, false>(p, sa, sb, c_base, c_count, grid, s);
+  if (mode == 1) return walk_launch1<A, 1, TC, false>(p, sa, sb, c_base, c_count, grid, s);
+  return f ? walk_launch1<A, 2, TC, kF>(p, sa, sb, c_base, c_count, grid, s)
+           : walk_launch1<A, 2, TC, false>(p, sa, sb, c_base, c_count, grid, s);
 }
 
 template <int A>
 int walk_launch(const KParams &p, int mode, bool tc, float *sa, float *sb, int c_base, int c_count, int grid,
                 cudaStream_t s) {
   if constexpr (A == 64) {
-    if (tc) {
-      if (mode == 0) return walk_launch1<A, 0, true>(p, sa, sb, c_base, c_count, grid, s);
-      if (mode == 1) return walk_launch1<A, 1, true>(p, sa, sb, c_base, c_count, grid, s);
-      return walk_launch1<A, 2, true>(p, sa, sb, c_base, c_count, grid, s);
-    }
+    // the closed-form F81 walk has no matrix products for the tensor cores
+    if (tc && !(p.f81_model && mode != 1)) return walk_launch_tc<A, true>(p, mode, sa, sb, c_base, c_count, grid, s);
   }
-  if (mode == 0) return walk_launch1<A, 0, false>(p, sa, sb, c_base, c_count, grid, s);
-  if (mode == 1) return walk_launch1<A, 1, false>(p, sa, sb, c_base, c_count, grid, s);
-  return walk_launch1<A, 2, false>(p, sa, sb, c_base, c_count, grid, s);
+  return walk_launch_tc<A, false>(p, mode, sa, sb, c_base, c_count, grid, s);
 }
 
 template <int A>

@@ -234,6 +234,7 @@ struct subby_plan {
   int4 *d_prog = nullptr;
   std::vector<double> V, mu, pi;
   float f81_mu = 0.f;
+  int f81_model = 0;   // M(t) has the F81 / JC closed form (checked on the host)
   TableOffsets off{};
   float *d_tab = nullptr;
   double *d_tab64 = nullptr;
@@ -432,6 +433,23 @@ int subby_plan_create(const int32_t *parent, const double *dist, const double *e
   }
   const double mu81 = 1.0 / (1.0 - pi2);
   P->f81_mu = (float)mu81;
+  {
+    // Is M(t) = e I + (1 - e) 1 pi^T, e = exp(-mu81 t)?  Checked in FP64 at
+    // two branch lengths; then the large-alphabet walk uses the closed form.
+    double worst = 0.0;
+    for (double t : {0.3, 2.0}) {
+      const double e = std::exp(-mu81 * t);
+      for (int i = 0; i < A; ++i)
+        for (int j = 0; j < A; ++j) {
+          double m = 0.0;
+          for (int k = 0; k < A; ++k) m += evecs[i * A + k] * std::exp(evals[k] * t) * evecs[j * A + k];
+          m *= std::sqrt(pi[j] / pi[i]);
+          const double f = (i == j ? e : 0.0) + (1.0 - e) * pi[j];
+          worst = std::max(worst, std::fabs(m - f));
+        }
+    }
+    P->f81_model = std::isfinite(mu81) && worst < 1e-9;
+  }
 
   TableOffsets &o = P->off;
   int cur = 0;
@@ -455,8 +473,12 @@ int subby_plan_create(const int32_t *parent, const double *dist, const double *e
   o.F81 = take(R * 4);
   o.ME = take(R * A);
   o.K = (A <= 8) ? take(R * (A + 1) * (A * A + 4)) : 0;
+  o.EF = take(R * 2);
   o.total = cur;
-  std::vector<float> tab((size_t)o.total, 0.f);
+  // Host-computed parts only: the small block and the F81 / ME tables (MT,
+  // MN, J, JT and K are written on the device by the prologue kernels).
+  std::vector<float> hsm((size_t)small_n, 0.f), hfm((size_t)(o.ME + R * A - o.F81), 0.f), hef((size_t)R * 2);
+  auto at = [&](int off) -> float & { return off >= o.F81 ? hfm[off - o.F81] : hsm[off - o.Vu]; };
   std::vector<double> E(A);
   // M(t) itself (MT / MN tables) is formed by k_compute_M on the device, in
   // FP64, right after the upload below.
@@ -465,12 +487,14 @@ int subby_plan_create(const int32_t *parent, const double *dist, const double *e
     for (int k = 0; k < A; ++k) E[k] = std::exp(evals[k] * t);
     // F81 branch coefficients (subby/oracle/oracle.py:1226-1233)
     const double e = std::exp(-mu81 * t), pp = 1.0 - e;
-    float *f = tab.data() + o.F81 + (size_t)n * 4;
+    float *f = &at(o.F81 + n * 4);
     f[0] = (float)(t * e);
     f[1] = (float)(pp / mu81 - t * e);
     f[2] = (float)(t * (1.0 + e) - 2.0 * pp / mu81);
     f[3] = (float)t;
-    for (int k = 0; k < A; ++k) tab[o.ME + (size_t)n * A + k] = (float)(evals[k] * E[k]);
+    hef[2 * n] = (float)e;
+    hef[2 * n + 1] = (float)(-std::expm1(-mu81 * t));
+    for (int k = 0; k < A; ++k) at(o.ME + n * A + k) = (float)(evals[k] * E[k]);
   }
   std::vector<double> S64((size_t)A * A);
   for (int i = 0; i < A; ++i)
@@ -481,18 +505,18 @@ int subby_plan_create(const int32_t *parent, const double *dist, const double *e
     }
   for (int b = 0; b < A; ++b)
     for (int l = 0; l < A; ++l) {
-      tab[o.Vu + b * A + l] = (float)(sp[b] * evecs[b * A + l]);
-      tab[o.Vd + b * A + l] = (float)(isp[b] * evecs[b * A + l]);
-      tab[o.Ut + b * A + l] = (float)(sp[b] * evecs[b * A + l]);
-      tab[o.S + b * A + l] = (float)S64[b * A + l];
-      tab[o.V + b * A + l] = (float)evecs[b * A + l];
+      at(o.Vu + b * A + l) = (float)(sp[b] * evecs[b * A + l]);
+      at(o.Vd + b * A + l) = (float)(isp[b] * evecs[b * A + l]);
+      at(o.Ut + b * A + l) = (float)(sp[b] * evecs[b * A + l]);
+      at(o.S + b * A + l) = (float)S64[b * A + l];
+      at(o.V + b * A + l) = (float)evecs[b * A + l];
     }
   for (int l = 0; l < A; ++l) {
     double s = 0.0;
     for (int b = 0; b < A; ++b) s += sp[b] * evecs[b * A + l];
-    tab[o.Ut + A * A + l] = (float)s;
+    at(o.Ut + A * A + l) = (float)s;
   }
-  for (int a = 0; a < A; ++a) tab[o.pi + a] = (float)pi[a];
+  for (int a = 0; a < A; ++a) at(o.pi + a) = (float)pi[a];
 
   // ---- device upload
   auto cleanup = [&](int rc) {
@@ -503,7 +527,11 @@ int subby_plan_create(const int32_t *parent, const double *dist, const double *e
   cudaStream_t qs = P->s_prep;
   cudaError_t e = pool_alloc((void **)&P->d_tab, P->tab_bytes, P->pool, qs);
   if (e != cudaSuccess) return cleanup(cuda_fail(e, "table allocation"));
-  e = cudaMemcpyAsync(P->d_tab, tab.data(), P->tab_bytes, cudaMemcpyHostToDevice, qs);
+  e = cudaMemcpyAsync(P->d_tab + o.Vu, hsm.data(), hsm.size() * sizeof(float), cudaMemcpyHostToDevice, qs);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(P->d_tab + o.F81, hfm.data(), hfm.size() * sizeof(float), cudaMemcpyHostToDevice, qs);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(P->d_tab + o.EF, hef.data(), hef.size() * sizeof(float), cudaMemcpyHostToDevice, qs);
   if (e != cudaSuccess) return cleanup(cuda_fail(e, "table upload"));
   e = pool_alloc((void **)&P->d_tab64, sizeof(double) * (2 * A * A + A + R + A), P->pool, qs);
   if (e != cudaSuccess) return cleanup(cuda_fail(e, "FP64 table allocation"));
@@ -833,6 +861,7 @@ int run_big(subby_plan *P, const int32_t *d_aln, int C, float *d_logL, float *d_
   k.off = P->off;
   k.root_is_leaf = P->root_is_leaf;
   k.f81_mu = P->f81_mu;
+  k.f81_model = P->f81_model;
   k.logL = d_logL;
   k.counts = d_counts;
   k.rootp = d_root;

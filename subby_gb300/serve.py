@@ -130,6 +130,8 @@ class Server:
         self.used_bytes = 0
         self.completed = []
         self.on_done = None
+        # host seconds spent preparing plans, enqueueing jobs and polling
+        self.host_s = {"plan": 0.0, "launch": 0.0, "poll": 0.0}
         self.lock = threading.Lock()
 
     # ------------------------------------------------------------------ plans
@@ -147,7 +149,9 @@ class Server:
         if p is not None:
             self.plans.move_to_end(k)
             return p
+        t0 = time.perf_counter()
         p = Plan(tree, model, device=self.device)
+        self.host_s["plan"] += time.perf_counter() - t0
         self.plans[k] = p
         while len(self.plans) > self.plan_cache:
             self.plans.popitem(last=False)[1].close()
@@ -257,10 +261,15 @@ class Server:
                 waiting.append(j)
             while waiting and self.fits(waiting[0]):
                 j = waiting.popleft()
+                t1 = time.perf_counter()
                 self._launch(j, now())
+                self.host_s["launch"] += time.perf_counter() - t1
                 if on_admit:
                     on_admit(j)
-            if self.poll(now) == 0:
+            t1 = time.perf_counter()
+            ndone = self.poll(now)
+            self.host_s["poll"] += time.perf_counter() - t1
+            if ndone == 0:
                 if self.inflight:
                     time.sleep(0.0002)
                 elif pending and realtime:

@@ -137,11 +137,21 @@ def test_small_alphabets(A, kernel):
 
 
 def test_jc_and_f81_fast_paths_large_alphabet(big_kernel):
+    """F81 / JC models: the large-alphabet walk detects the closed form of
+    M(t) and uses it for LogLike-only and F81-count runs (general products
+    for eigen counts); every output against the oracle."""
     rng = np.random.default_rng(7)
     tree = synth.random_tree(14, 0.1, rng)
-    for m in (models.jukes_cantor_model(64), models.f81_model(rng.dirichlet(np.ones(20)))):
+    otree = oracle.Tree(tree.parentIndex, tree.distanceToParent)
+    for m in (models.jukes_cantor_model(64), models.f81_model(rng.dirichlet(np.ones(20))),
+              models.f81_model(rng.dirichlet(np.ones(64))), models.jukes_cantor_model(16),
+              models.f81_model(rng.dirichlet(np.ones(32)))):
         aln = synth.simulated_alignment(tree, m, 19, 0.1, rng)
         _check_all(aln, tree, m, f81=True)
+        plan = sg.Plan(tree, m)
+        ll = plan.run(aln, loglike=True)['logLike']
+        assert_loglike(ll, oracle.LogLike(aln, otree, _model_dict(m)))
+        plan.close()
 
 
 def test_edge_cases(kernel):

@@ -437,12 +437,14 @@ int subby_plan_create(const int32_t *parent, const double *dist, const double *e
     // Is M(t) = e I + (1 - e) 1 pi^T, e = exp(-mu81 t)?  Checked in FP64 at
     // two branch lengths; then the large-alphabet walk uses the closed form.
     double worst = 0.0;
+    std::vector<double> ek(A);
     for (double t : {0.3, 2.0}) {
       const double e = std::exp(-mu81 * t);
+      for (int k = 0; k < A; ++k) ek[k] = std::exp(evals[k] * t);
       for (int i = 0; i < A; ++i)
         for (int j = 0; j < A; ++j) {
           double m = 0.0;
-          for (int k = 0; k < A; ++k) m += evecs[i * A + k] * std::exp(evals[k] * t) * evecs[j * A + k];
+          for (int k = 0; k < A; ++k) m += evecs[i * A + k] * ek[k] * evecs[j * A + k];
           m *= std::sqrt(pi[j] / pi[i]);
           const double f = (i == j ? e : 0.0) + (1.0 - e) * pi[j];
           worst = std::max(worst, std::fabs(m - f));

@@ -97,6 +97,8 @@ struct KParams {
   // the model is F81 / JC: M_n = e_n I + (1 - e_n) 1 pi^T, so the walk's
   // products take the closed form (tables EF) instead of A x A products
   int f81_model;
+  // F81 staging (k_walk MODE 2): per branch and column (pi . U, sum s D), or null
+  float2 *stage_c;
 };
 
 // launchers (k_small.cu / k_warp.cu)
@@ -117,6 +119,9 @@ int launch_acc(const KParams &p, int A, bool f81, const float *sa, const float *
                int grid, cudaStream_t s);
 int launch_tree4(const KParams &p, bool f81, int mask_mode, int grid, int block, size_t smem,
                  cudaStream_t s);
+// A = 64 F81 accumulation on the tensor cores (k_acctc.cu); groups of 8 columns
+int launch_acc_f81_tc(const KParams &p, const float *sa, const float *sb, const float2 *sc, int c_base,
+                      int c_count, int grid, cudaStream_t s);
 bool small_supported(int A);
 bool warp_supported(int A);
 int small_block();

@@ -599,6 +599,26 @@ __global__ void __launch_bounds__(128 * Geo<A>::H, 1) k_walk(const KParams P, fl
           wk.st(pa, Ds);
           wk.st(pb, U);
         }
+        if (P.stage_c) {
+          // the branch's scalars pi . U and sum(s D), combined over the pair
+          float pu = 0.f, ds = 0.f;
+#pragma unroll
+          for (int q = 0; q < S; ++q) {
+            pu = fmaf(piv.v[q], U.v[q], pu);
+            ds += Ds.v[q];
+          }
+          if constexpr (Geo<A>::H == 2) {
+            s_xch[h * kTile + cl] = pu;
+            pair_sync(wk.warp);
+            pu += s_xch[(1 - h) * kTile + cl];
+            pair_sync(wk.warp);
+            s_xch[h * kTile + cl] = ds;
+            pair_sync(wk.warp);
+            ds += s_xch[(1 - h) * kTile + cl];
+            pair_sync(wk.warp);
+          }
+          if (valid && h == 0) P.stage_c[(size_t)(n - 1) * c_count + cc0] = make_float2(pu, ds);
+        }
         return;
       }
       BV<A> Ds, dt, ut;

@@ -5,6 +5,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstdio>
 #include <cstring>
 #include <mutex>
@@ -156,9 +157,13 @@ __global__ void k_compute_K(const float *__restrict__ J, const float *__restrict
 // Device memory of plans comes from one library-owned stream-ordered pool per
 // device: allocations and frees are ordered on CUDA streams (no implicit
 // device-wide synchronisation, so creating or evicting a plan never stalls
-// kernels of other streams), and up to kPoolKeep bytes of freed blocks stay
-// cached in the pool for the next plan.
-constexpr uint64_t kPoolKeep = 2ull << 30;
+// kernels of other streams), and freed blocks stay cached in the pool for
+// the next plan up to SUBBY_POOL_KEEP_MB megabytes (default 2048).
+uint64_t pool_keep_bytes() {
+  const char *v = std::getenv("SUBBY_POOL_KEEP_MB");
+  const long long mb = v ? std::atoll(v) : 2048;
+  return (uint64_t)(mb > 0 ? mb : 0) << 20;
+}
 
 cudaMemPool_t lib_pool(int dev) {
   static std::mutex m;
@@ -175,7 +180,7 @@ cudaMemPool_t lib_pool(int dev) {
       pools[dev] = nullptr;
       return nullptr;
     }
-    uint64_t keep = kPoolKeep;
+    uint64_t keep = pool_keep_bytes();
     cudaMemPoolSetAttribute(pools[dev], cudaMemPoolAttrReleaseThreshold, &keep);
   }
   return pools[dev];
@@ -250,6 +255,7 @@ struct subby_plan {
   // end of the latest enqueued kernel, after which buffers may be freed
   cudaStream_t s_prep = nullptr;
   cudaEvent_t last_use = nullptr;
+  cudaEvent_t ready = nullptr;   // end of the table preparation on s_prep
   bool used = false;
   cudaMemPool_t pool = nullptr;
   int grow(DevBuf &b, size_t need, cudaStream_t s) {
@@ -336,8 +342,13 @@ int subby_plan_create(const int32_t *parent, const double *dist, const double *e
   P->root_is_leaf = (R == 1);
   P->pool = lib_pool(P->device);
   {
-    cudaError_t e0 = cudaStreamCreateWithFlags(&P->s_prep, cudaStreamNonBlocking);
+    // the preparation stream has the highest priority, so the prologue
+    // kernels start as soon as SMs free up when other work fills the device
+    int lo = 0, hi = 0;
+    cudaDeviceGetStreamPriorityRange(&lo, &hi);
+    cudaError_t e0 = cudaStreamCreateWithPriority(&P->s_prep, cudaStreamNonBlocking, hi);
     if (e0 == cudaSuccess) e0 = cudaEventCreateWithFlags(&P->last_use, cudaEventDisableTiming);
+    if (e0 == cudaSuccess) e0 = cudaEventCreateWithFlags(&P->ready, cudaEventDisableTiming);
     if (e0 != cudaSuccess) {
       subby_plan_destroy(P);
       return cuda_fail(e0, "plan stream");
@@ -589,7 +600,8 @@ int subby_plan_create(const int32_t *parent, const double *dist, const double *e
     }
     if (e == cudaSuccess) e = pool_alloc((void **)&P->d_err, sizeof(int), P->pool, qs);
     if (e == cudaSuccess) e = cudaMemsetAsync(P->d_err, 0, sizeof(int), qs);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(qs);
+    // no host wait: runs order themselves after `ready` on their own streams
+    if (e == cudaSuccess) e = cudaEventRecord(P->ready, qs);
     if (e != cudaSuccess) return cleanup(cuda_fail(e, "J(t) prologue"));
   }
   *out = P;
@@ -614,6 +626,7 @@ int subby_plan_destroy(subby_plan *P) {
   P->io.release(s);
   for (cudaEvent_t e : P->ev) cudaEventDestroy(e);
   if (P->last_use) cudaEventDestroy(P->last_use);
+  if (P->ready) cudaEventDestroy(P->ready);
   if (P->s_in) cudaStreamDestroy(P->s_in);
   if (P->s_out) cudaStreamDestroy(P->s_out);
   if (s) cudaStreamDestroy(s);
@@ -891,9 +904,14 @@ int run_big(subby_plan *P, const int32_t *d_aln, int C, float *d_logL, float *d_
   const size_t slot_floats = (size_t)walk_grid * k.nslots * tile * A;
   const size_t slot_ints = (size_t)walk_grid * k.nslots * tile;
   const size_t stage_floats = counts ? (size_t)(R - 1) * chunk * A : 0;
+  // A = 64 F81 counts on the tensor cores: per-branch scalars staged too
+  const bool f81tc = counts && (mode & kModeF81) && tc;
+  const size_t stage_c_floats = f81tc ? (size_t)(R - 1) * chunk * 2 : 0;
   auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
   int rc;
-  if ((rc = P->grow(P->work, al(slot_floats * 4) + al(slot_ints * 4) + 2 * al(stage_floats * 4) + 256, stream)))
+  if ((rc = P->grow(P->work,
+                    al(slot_floats * 4) + al(slot_ints * 4) + 2 * al(stage_floats * 4) + al(stage_c_floats * 4) + 256,
+                    stream)))
     return rc;
   char *base = (char *)P->work.p;
   k.scrV = (float *)base;
@@ -903,6 +921,8 @@ int run_big(subby_plan *P, const int32_t *d_aln, int C, float *d_logL, float *d_
   float *sa = (float *)base;
   base += al(stage_floats * 4);
   float *sb = (float *)base;
+  base += al(stage_floats * 4);
+  k.stage_c = f81tc ? (float2 *)base : nullptr;
   const int wmode = counts ? ((mode & kModeF81) ? 2 : 1) : 0;
   if (!counts && (mode & kModeCounts)) {
     // a single-node tree has no branch: counts are zero
@@ -917,7 +937,8 @@ int run_big(subby_plan *P, const int32_t *d_aln, int C, float *d_logL, float *d_
     if (counts) {
       const int G = big_acc_group(A);
       const int agrid = std::max(1, std::min((cc + G - 1) / G, P->nsm));
-      lr = launch_acc(k, A, (mode & kModeF81) != 0, sa, sb, c0, cc, agrid, stream);
+      lr = f81tc ? launch_acc_f81_tc(k, sa, sb, k.stage_c, c0, cc, agrid, stream)
+                 : launch_acc(k, A, (mode & kModeF81) != 0, sa, sb, c0, cc, agrid, stream);
       if (lr != 0) return fail(SUBBY_ERR_CUDA, std::string("accumulate launch failed: ") + cudaGetErrorString((cudaError_t)lr));
       g_launches += 1;
     }
@@ -1028,6 +1049,7 @@ int subby_plan_run(subby_plan *P, const int32_t *aln, int C, float *logL, float 
   cudaGetDevice(&dev);
   if (dev != P->device) CU(cudaSetDevice(P->device));
   const int A = P->A, R = P->R;
+  CU(cudaStreamWaitEvent(stream, P->ready, 0));
   int mode = 0;
   if (logL) mode |= kModeLogLike;
   if (rootProb) mode |= kModeRootProb;
@@ -1141,6 +1163,7 @@ int subby_plan_grad(subby_plan *P, const int32_t *aln, int C, const float *g, fl
   std::lock_guard<std::mutex> lk(P->lock);
   cudaStream_t stream = (cudaStream_t)stream_;
   const int A = P->A, R = P->R;
+  CU(cudaStreamWaitEvent(stream, P->ready, 0));
   const bool dev = (flags & SUBBY_DEVICE_PTRS) != 0;
   // staging for host pointers
   const int32_t *d_aln = aln;

@@ -134,6 +134,22 @@ class Server:
         self.host_s = {"plan": 0.0, "launch": 0.0, "poll": 0.0}
         self.lock = threading.Lock()
 
+    def prewarm(self, host_bytes: int = 0, device_bytes: int = 0, per_class: int = 2):
+        """Fill the allocators' caches before serving: one device block of
+        ``device_bytes`` for torch's caching allocator to split, and
+        ``per_class`` pinned host blocks of every power-of-two size up to
+        ``host_bytes`` (page pinning costs milliseconds per large block, which
+        would otherwise land on the first jobs of each size)."""
+        torch = self.torch
+        if device_bytes > 0:
+            x = torch.empty(int(device_bytes), dtype=torch.uint8, device=self.device)
+            del x
+        size, keep = 1 << 20, []
+        while size <= host_bytes:
+            keep += [torch.empty(size, dtype=torch.uint8, pin_memory=True) for _ in range(per_class)]
+            size <<= 1
+        del keep
+
     # ------------------------------------------------------------------ plans
     @staticmethod
     def _key(job):

@@ -127,6 +127,26 @@ def test_precision64_subset(big_kernel):
     _check_all(w['alignment'], w['tree'], w['model'], masked=False)
 
 
+def test_f81_counts_general_model_large_alphabet(big_kernel):
+    """F81 counts requested with a general reversible model (the reference
+    applies the F81 formulas to the model's own inside/outside vectors): the
+    tensor-core walk stages F81 vectors and, at A = 64, the tensor-core F81
+    accumulation runs; vs the oracle, masked and unmasked, with ragged
+    column counts (last group short)."""
+    rng = np.random.default_rng(17)
+    for A, C in ((64, 37), (20, 29)):
+        m, _, _ = models.random_reversible(A, rng, 0.5, 2.0)
+        tree = synth.random_tree(21, 0.1, rng)
+        aln = synth.simulated_alignment(tree, m, C, 0.1, rng)
+        otree = oracle.Tree(tree.parentIndex, tree.distanceToParent)
+        plan = sg.Plan(tree, m)
+        for bm in (None, "auto"):
+            got = plan.run(aln, loglike=False, counts=True, f81=True, branch_mask=bm)['counts']
+            ref = oracle.Counts(aln, otree, _model_dict(m), f81_fast=True, branch_mask=bm)
+            assert_cols(got, ref, COUNTS_RTOL, f"A={A} f81 counts mask={bm}")
+        plan.close()
+
+
 @pytest.mark.parametrize("A", [2, 3, 4, 5, 6, 8])
 def test_small_alphabets(A, kernel):
     rng = np.random.default_rng(200 + A)

@@ -92,6 +92,12 @@ int subby_plan_create(const int32_t *parent_index, const double *distances,
 int subby_plan_destroy(subby_plan *plan);
 /* Bytes of device memory the plan currently holds (tables + workspace). */
 size_t subby_plan_device_bytes(const subby_plan *plan);
+/* Release the plan's workspace (staging, scratch, host-call buffers) in
+ * stream order after its last enqueued kernel; the tables stay.  The next
+ * run allocates again (from the library pool).  For servers that keep many
+ * plans resident.  No counterpart in the reference (it holds no device
+ * state between calls). */
+int subby_plan_trim(subby_plan *plan);
 
 /*
  * Run the hot path of a prepared plan on a (R, C) alignment.

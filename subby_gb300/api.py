@@ -192,6 +192,11 @@ class Plan:
     def device_bytes(self) -> int:
         return int(_lib.load().subby_plan_device_bytes(self._handle))
 
+    def trim(self):
+        """Release the workspace (kept tables); the next run allocates again."""
+        with self._lock:
+            _lib.check(_lib.load().subby_plan_trim(self._handle), "subby_plan_trim")
+
     def close(self):
         if getattr(self, "_handle", None) and self._handle.value:
             _lib.load().subby_plan_destroy(self._handle)

@@ -635,6 +635,19 @@ int subby_plan_destroy(subby_plan *P) {
   return SUBBY_OK;
 }
 
+int subby_plan_trim(subby_plan *P) {
+  if (!P) return fail(SUBBY_ERR_ARG, "null plan");
+  std::lock_guard<std::mutex> g(P->lock);
+  int cur = 0;
+  cudaGetDevice(&cur);
+  if (cur != P->device) cudaSetDevice(P->device);
+  if (P->used) cudaStreamWaitEvent(P->s_prep, P->last_use, 0);
+  P->work.release(P->s_prep);
+  P->io.release(P->s_prep);
+  if (cur != P->device) cudaSetDevice(cur);
+  return SUBBY_OK;
+}
+
 size_t subby_plan_device_bytes(const subby_plan *P) {
   if (!P) return 0;
   return P->tab_bytes + P->work.bytes + P->io.bytes + sizeof(int4) * 2 * P->nInt;

@@ -246,6 +246,10 @@ class Server:
                 # hands the buffers back to the host allocator's cache
                 job.result = {k: v.numpy() for k, v in bufs[3].items()}
                 job._pinned = bufs[3]
+                # the plan stays cached; its workspace goes back to the pool
+                plan = self.plans.get(self._key(job))
+                if plan is not None:
+                    plan.trim()
                 self.free_slots.append(slot)
                 self.used_bytes -= nbytes
                 self.completed.append(job)

@@ -80,3 +80,19 @@ def test_sliced_long_jobs_and_priority_streams_give_identical_results():
             np.testing.assert_array_equal(j.result['counts'], ref[j.id]['counts'])
             np.testing.assert_array_equal(j.result['logLike'], ref[j.id]['logLike'])
         srv.close()
+
+
+def test_plan_trim_releases_workspace_and_keeps_results():
+    rng = np.random.default_rng(3)
+    m = sg.models.random_reversible(20, rng, 0.5, 2.0)[0]
+    tree = synth.random_tree(12, 0.1, rng)
+    aln = synth.simulated_alignment(tree, m, 300, 0.1, rng)
+    plan = sg.Plan(tree, m)
+    a = plan.run(aln, loglike=True, counts=True)
+    held = plan.device_bytes()
+    plan.trim()
+    assert plan.device_bytes() < held
+    b = plan.run(aln, loglike=True, counts=True)
+    for k in a:
+        np.testing.assert_array_equal(a[k], b[k])
+    plan.close()

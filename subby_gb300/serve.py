@@ -63,9 +63,12 @@ class Job:
         return self.finish - self.arrival
 
     def release(self):
-        """Drop the results (pinned host buffers go back to the host cache)."""
+        """Drop the results; their pinned host buffers go back to the server."""
         self.result = {}
-        self._pinned = None
+        blocks, self._pinned = getattr(self, "_pinned", None), None
+        cb = getattr(self, "_give_back", None)
+        if blocks and cb is not None:
+            cb(blocks)
 
     @property
     def RC(self):
@@ -130,25 +133,37 @@ class Server:
         self.used_bytes = 0
         self.completed = []
         self.on_done = None
+        self.pinned_free = {}    # size class -> free pinned blocks
         # host seconds spent preparing plans, enqueueing jobs and polling
-        self.host_s = {"plan": 0.0, "launch": 0.0, "poll": 0.0}
+        self.host_s = {"plan": 0.0, "launch": 0.0, "poll": 0.0, "tokens": 0.0, "run": 0.0, "result": 0.0}
         self.lock = threading.Lock()
 
+    # ------------------------------------------------------- pinned buffers
+    # Result buffers come from a server-owned pool of pinned host blocks in
+    # power-of-two size classes: page pinning costs milliseconds per large
+    # block, so blocks are reused instead of allocated per job.
+    def _pinned(self, nbytes: int):
+        cls = max(1 << 16, 1 << (max(int(nbytes), 1) - 1).bit_length())
+        free = self.pinned_free.setdefault(cls, [])
+        return free.pop() if free else self.torch.empty(cls, dtype=self.torch.uint8, pin_memory=True)
+
+    def _give_back(self, blocks):
+        for b in blocks:
+            self.pinned_free.setdefault(b.numel(), []).append(b)
+
     def prewarm(self, host_bytes: int = 0, device_bytes: int = 0, per_class: int = 2):
-        """Fill the allocators' caches before serving: one device block of
+        """Fill the caches before serving: one device block of
         ``device_bytes`` for torch's caching allocator to split, and
         ``per_class`` pinned host blocks of every power-of-two size up to
-        ``host_bytes`` (page pinning costs milliseconds per large block, which
-        would otherwise land on the first jobs of each size)."""
+        ``host_bytes`` in the server's pool."""
         torch = self.torch
         if device_bytes > 0:
             x = torch.empty(int(device_bytes), dtype=torch.uint8, device=self.device)
             del x
-        size, keep = 1 << 20, []
+        size = 1 << 16
         while size <= host_bytes:
-            keep += [torch.empty(size, dtype=torch.uint8, pin_memory=True) for _ in range(per_class)]
+            self._give_back([torch.empty(size, dtype=torch.uint8, pin_memory=True) for _ in range(per_class)])
             size <<= 1
-        del keep
 
     # ------------------------------------------------------------------ plans
     @staticmethod
@@ -186,6 +201,7 @@ class Server:
         h_aln = None
         kw = dict(loglike="logLike" in job.want, counts="counts" in job.want,
                   rootprob="rootProb" in job.want, f81=job.f81, branch_mask=job.branch_mask)
+        t_tok = time.perf_counter()
         with torch.cuda.stream(stream):
             if callable(job.alignment):
                 d_aln = job.alignment(stream, self.device)
@@ -196,6 +212,8 @@ class Server:
                 if not h_aln.is_pinned():
                     h_aln = h_aln.pin_memory()
                 d_aln = h_aln.to(self.device, non_blocking=True)
+            t_run = time.perf_counter()
+            self.host_s["tokens"] += t_run - t_tok
             nsl = max(1, min(int(np.ceil(cost / self.slice_ms)), (C + 127) // 128))
             if nsl == 1 or not isinstance(job.branch_mask, str):
                 res = plan.run(d_aln, stream=stream, **kw)
@@ -213,16 +231,21 @@ class Server:
                                for k, v in part.items()}
                     for k, v in part.items():
                         res[k][..., c0:c1].copy_(v)
-            host = {}
+            t_pin = time.perf_counter()
+            self.host_s["run"] += t_pin - t_run
+            host, blocks = {}, []
             for k, v in res.items():
-                hv = torch.empty(v.shape, dtype=v.dtype, pin_memory=True)
+                blk = self._pinned(v.numel() * v.element_size())
+                blocks.append(blk)
+                hv = blk[:v.numel() * v.element_size()].view(v.dtype).view(v.shape)
                 hv.copy_(v, non_blocking=True)
                 host[k] = hv
+            self.host_s["result"] += time.perf_counter() - t_pin
             ev = torch.cuda.Event()
             ev.record(stream)
         job.start = now
         self.used_bytes += nbytes
-        self.inflight.append((job, slot, ev, nbytes, (h_aln, d_aln, res, host)))
+        self.inflight.append((job, slot, ev, nbytes, (h_aln, d_aln, res, host, blocks)))
 
     def fits(self, job: Job) -> bool:
         R, C = job.RC
@@ -245,7 +268,8 @@ class Server:
                 # numpy views of the pinned result buffers; Job.release()
                 # hands the buffers back to the host allocator's cache
                 job.result = {k: v.numpy() for k, v in bufs[3].items()}
-                job._pinned = bufs[3]
+                job._pinned = bufs[4]
+                job._give_back = self._give_back
                 # the plan stays cached; its workspace goes back to the pool
                 plan = self.plans.get(self._key(job))
                 if plan is not None:

@@ -45,7 +45,8 @@ from .models import ensure_diag
 class Job:
     id: int
     alignment: object              # (R, C) int32: host array, CUDA tensor, or a
-    #                                callable(stream, device) -> CUDA tensor
+    #                                callable(stream, device, out) that fills
+    #                                the (R, C) int32 CUDA tensor ``out``
     tree: object
     model: object
     f81: bool = False
@@ -126,6 +127,7 @@ class Server:
         # one normal- and one high-priority stream per slot
         self.streams = [torch.cuda.Stream(device=self.device) for _ in range(max_inflight)]
         self.hi_streams = [torch.cuda.Stream(device=self.device, priority=-8) for _ in range(max_inflight)]
+        self.arenas = [None] * max_inflight
         self.free_slots = list(range(max_inflight))
         self.plans = collections.OrderedDict()
         self.plan_cache = plan_cache
@@ -189,6 +191,31 @@ class Server:
         return p
 
     # ---------------------------------------------------------------- submit
+    # ----------------------------------------------------------- slot arenas
+    # Each slot owns one device arena that grows to the largest job it has
+    # served; a job's tokens, outputs and slice temporaries are carved from
+    # it, so enqueueing a job allocates nothing (allocation calls can stall
+    # the host while the device is busy).
+    def _arena(self, slot: int, nbytes: int):
+        torch = self.torch
+        a = self.arenas[slot]
+        if a is None or a.numel() < nbytes:
+            self.arenas[slot] = None
+            a = torch.empty(1 << (max(int(nbytes), 1 << 20) - 1).bit_length(), dtype=torch.uint8,
+                            device=self.device)
+            self.arenas[slot] = a
+        return a
+
+    @staticmethod
+    def _carve(buf, plan_list):
+        """Views of ``buf`` for [(name, shape, dtype), ...] at 256-byte offsets."""
+        out, off = {}, 0
+        for name, shape, dtype in plan_list:
+            n = int(np.prod(shape)) * dtype.itemsize
+            out[name] = buf[off:off + n].view(dtype).view(shape)
+            off = (off + n + 255) & ~255
+        return out
+
     def _launch(self, job: Job, now: float):
         torch = self.torch
         R, C = job.RC
@@ -198,54 +225,71 @@ class Server:
         cost = job_cost_ms(R, C, A, job.f81)
         stream = (self.hi_streams if cost <= self.short_ms else self.streams)[slot]
         plan = self.plan_for(job.tree, job.model, self._key(job))
-        h_aln = None
         kw = dict(loglike="logLike" in job.want, counts="counts" in job.want,
                   rootprob="rootProb" in job.want, f81=job.f81, branch_mask=job.branch_mask)
+        nsl = max(1, min(int(np.ceil(cost / self.slice_ms)), (C + 127) // 128))
+        if not isinstance(job.branch_mask, str):
+            nsl = 1
+        cmax = C if nsl == 1 else ((C + nsl - 1) // nsl + 127) // 128 * 128
+        f32, i32 = torch.float32, torch.int32
+        shapes = {"logLike": (C,), "counts": (A, A, C), "rootProb": (A, C)}
+        want = [k for k in ("logLike", "counts", "rootProb") if k in job.want]
+        layout = [("aln", (R, C), i32)] + [(k, shapes[k], f32) for k in want]
+        if nsl > 1:
+            layout += [("s_aln", (R * cmax,), i32)] + [("s_" + k, (int(np.prod(shapes[k][:-1])) * cmax,), f32)
+                                                       for k in want]
+        need = sum((int(np.prod(sh)) * dt.itemsize + 255) & ~255 for _, sh, dt in layout)
+        v = self._carve(self._arena(slot, need), layout)
+        res = {k: v[k] for k in want}
         t_tok = time.perf_counter()
+        pinned_in = None
         with torch.cuda.stream(stream):
             if callable(job.alignment):
-                d_aln = job.alignment(stream, self.device)
+                job.alignment(stream, self.device, v["aln"])
+                d_aln = v["aln"]
             elif isinstance(job.alignment, torch.Tensor) and job.alignment.is_cuda:
                 d_aln = job.alignment
             else:
-                h_aln = torch.from_numpy(np.ascontiguousarray(job.alignment, dtype=np.int32))
-                if not h_aln.is_pinned():
-                    h_aln = h_aln.pin_memory()
-                d_aln = h_aln.to(self.device, non_blocking=True)
+                src = np.ascontiguousarray(job.alignment, dtype=np.int32)
+                pinned_in = self._pinned(src.nbytes)
+                h = pinned_in[:src.nbytes].view(i32).view(R, C)
+                h.numpy()[:] = src
+                v["aln"].copy_(h, non_blocking=True)
+                d_aln = v["aln"]
             t_run = time.perf_counter()
             self.host_s["tokens"] += t_run - t_tok
-            nsl = max(1, min(int(np.ceil(cost / self.slice_ms)), (C + 127) // 128))
-            if nsl == 1 or not isinstance(job.branch_mask, str):
-                res = plan.run(d_aln, stream=stream, **kw)
+            if nsl == 1:
+                plan.run(d_aln, stream=stream, out=res, **kw)
             else:
                 # long job: column slices of whole 128-column tiles, each its
                 # own launch sequence, results gathered on the device
                 edges = [min(C, ((C * i // nsl) + 127) // 128 * 128) for i in range(nsl)] + [C]
-                res = None
                 for c0, c1 in zip(edges[:-1], edges[1:]):
-                    if c1 <= c0:
+                    cc = c1 - c0
+                    if cc <= 0:
                         continue
-                    part = plan.run(d_aln[:, c0:c1].contiguous(), stream=stream, **kw)
-                    if res is None:
-                        res = {k: torch.empty(v.shape[:-1] + (C,), dtype=v.dtype, device=v.device)
-                               for k, v in part.items()}
-                    for k, v in part.items():
-                        res[k][..., c0:c1].copy_(v)
+                    s_aln = v["s_aln"][:R * cc].view(R, cc)
+                    s_aln.copy_(d_aln[:, c0:c1])
+                    part = {k: v["s_" + k][:int(np.prod(shapes[k][:-1])) * cc].view(shapes[k][:-1] + (cc,))
+                            for k in want}
+                    plan.run(s_aln, stream=stream, out=part, **kw)
+                    for k in want:
+                        res[k][..., c0:c1].copy_(part[k])
             t_pin = time.perf_counter()
             self.host_s["run"] += t_pin - t_run
-            host, blocks = {}, []
-            for k, v in res.items():
-                blk = self._pinned(v.numel() * v.element_size())
+            host, blocks = {}, ([pinned_in] if pinned_in is not None else [])
+            for k, r in res.items():
+                blk = self._pinned(r.numel() * r.element_size())
                 blocks.append(blk)
-                hv = blk[:v.numel() * v.element_size()].view(v.dtype).view(v.shape)
-                hv.copy_(v, non_blocking=True)
+                hv = blk[:r.numel() * r.element_size()].view(r.dtype).view(r.shape)
+                hv.copy_(r, non_blocking=True)
                 host[k] = hv
             self.host_s["result"] += time.perf_counter() - t_pin
             ev = torch.cuda.Event()
             ev.record(stream)
         job.start = now
         self.used_bytes += nbytes
-        self.inflight.append((job, slot, ev, nbytes, (h_aln, d_aln, res, host, blocks)))
+        self.inflight.append((job, slot, ev, nbytes, (None, d_aln, res, host, blocks)))
 
     def fits(self, job: Job) -> bool:
         R, C = job.RC

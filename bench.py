@@ -438,8 +438,9 @@ def serving_bench(args):
     g.manual_seed(5)
     pools = {}
     for A_ in sorted({d['A'] for d in desc}):
-        v = torch.randint(0, 20 * A_, (max_leaves, POOL_C), dtype=torch.int32, device="cuda", generator=g)
+        v = torch.randint(0, 20 * A_, (max_leaves + 1, POOL_C), dtype=torch.int32, device="cuda", generator=g)
         pools[A_] = torch.where(v < 19 * A_, v % A_, A_ + 1).contiguous()
+        pools[A_][max_leaves].fill_(A_)
         del v
     torch.cuda.synchronize()
     jobs = []
@@ -456,14 +457,16 @@ def serving_bench(args):
         R, C = len(tree.parentIndex), d['C']
         leaf = synth.leaf_mask(tree)
 
-        leaves = torch.from_numpy(np.nonzero(leaf)[0].astype(np.int64)).cuda()
+        # pool row of every tree row: leaves take distinct random rows, internal
+        # rows the pool's constant row of A (unobserved)
+        rowmap = np.full(R, max_leaves, dtype=np.int64)
+        rowmap[leaf] = np.arange(int(leaf.sum()))
+        rowmap = torch.from_numpy(rowmap).cuda()
         off = int(np.random.default_rng(d['seed']).integers(0, POOL_C - C + 1))
 
-        def make(stream, device, out, C=C, A=A, leaves=leaves, off=off):
-            # the job's tokens, with no allocation and no host wait: internal
-            # rows unobserved (A), leaf rows a window of the pre-drawn pool
-            out.fill_(A)
-            out.index_copy_(0, leaves, pools[A][:leaves.numel(), off:off + C])
+        def make(stream, device, out, C=C, A=A, rowmap=rowmap, off=off):
+            # the job's tokens in one gather, with no allocation and no host wait
+            torch.index_select(pools[A][:, off:off + C], 0, rowmap, out=out)
         jobs.append(serve.Job(id=d['id'], alignment=make, shape=(R, C), tree=tree, model=model,
                               f81=(d['kind'] == 'f81'), want=("counts",), arrival=d['arrival']))
     srv = serve.Server(max_inflight=8, device_budget=64 << 30)

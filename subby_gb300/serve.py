@@ -5,7 +5,9 @@ Jobs (alignment, tree, model, options) arrive over time.  The loop
 * admits a waiting job as soon as a device slot is free and its device
   footprint (plan tables + tokens + outputs + workspace estimate) fits the
   memory budget — requests that arrive while others are on the GPU are
-  admitted while those run;
+  admitted while those run; among waiting jobs the one with the smallest
+  estimated device time goes first, less a credit that grows with its wait
+  (``aging``), so long jobs are delayed but not starved;
 * keeps prepared plans (tree tables, eigendecomposition-derived tables, J(t))
   resident in HBM in an LRU cache keyed by (tree, model), so a repeated
   tree/model pays no preparation;
@@ -116,7 +118,7 @@ class Server:
     """Continuous batching over CUDA streams with memory-budget admission."""
 
     def __init__(self, max_inflight: int = 8, device_budget: int = 16 << 30, plan_cache: int = 64,
-                 device=None, short_ms: float = 5.0, slice_ms: float = 8.0):
+                 device=None, short_ms: float = 5.0, slice_ms: float = 8.0, aging: float = 0.2):
         import torch
         self.torch = torch
         self.device = torch.device("cuda", torch.cuda.current_device() if device is None else device)
@@ -124,6 +126,7 @@ class Server:
         self.budget = device_budget
         self.short_ms = short_ms
         self.slice_ms = slice_ms
+        self.aging = aging          # ms of estimated cost forgiven per ms waited
         # one normal- and one high-priority stream per slot
         self.streams = [torch.cuda.Stream(device=self.device) for _ in range(max_inflight)]
         self.hi_streams = [torch.cuda.Stream(device=self.device, priority=-8) for _ in range(max_inflight)]
@@ -291,6 +294,13 @@ class Server:
         self.used_bytes += nbytes
         self.inflight.append((job, slot, ev, nbytes, (None, d_aln, res, host, blocks)))
 
+    def _cost(self, job: Job) -> float:
+        c = getattr(job, "_cost_ms", None)
+        if c is None:
+            R, C = job.RC
+            c = job._cost_ms = job_cost_ms(R, C, len(ensure_diag(job.model).pi), job.f81)
+        return c
+
     def fits(self, job: Job) -> bool:
         R, C = job.RC
         A = len(ensure_diag(job.model).pi)
@@ -339,7 +349,7 @@ class Server:
         t0 = time.perf_counter()
         now = lambda: time.perf_counter() - t0  # noqa: E731
         pending = collections.deque(sorted(jobs, key=lambda j: j.arrival))
-        waiting = collections.deque()
+        waiting = []
         while pending or waiting or self.inflight:
             t = now()
             while pending and (not realtime or pending[0].arrival <= t):
@@ -347,8 +357,15 @@ class Server:
                 if not realtime:
                     j.arrival = t
                 waiting.append(j)
-            while waiting and self.fits(waiting[0]):
-                j = waiting.popleft()
+            while waiting and self.free_slots:
+                # shortest estimated job first, aged by its wait so that long
+                # jobs are not starved; the first one that fits is admitted
+                tn = now()
+                order = sorted(waiting, key=lambda w: self._cost(w) - self.aging * 1e3 * (tn - w.arrival))
+                j = next((w for w in order if self.fits(w)), None)
+                if j is None:
+                    break
+                waiting.remove(j)
                 t1 = time.perf_counter()
                 self._launch(j, now())
                 self.host_s["launch"] += time.perf_counter() - t1

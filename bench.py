@@ -166,7 +166,7 @@ def main():
     ap.add_argument("--workload", choices=["plain_large", "precision64", "grad20", "serving"],
                     default="plain_large",
                     help="plain_large is the headline line; the others print their own line")
-    ap.add_argument("--jobs", type=int, default=2000, help="serving: number of jobs")
+    ap.add_argument("--jobs", type=int, default=10000, help="serving: number of jobs")
     ap.add_argument("--rate", type=float, default=200.0, help="serving: Poisson arrival rate (jobs/s)")
     args = ap.parse_args()
     if args.warmup < 3:
@@ -430,48 +430,58 @@ def serving_bench(args):
     import subby_gb300 as sg
     from subby_gb300 import synth, serve, models
     desc = synth.serving_jobs(n_jobs=args.jobs, rate=args.rate, seed=5)
+    # warm-up stream (other seed, not timed): loads every kernel once and
+    # grows the slot arenas and host/device pools to their working sizes
+    wdesc = synth.serving_jobs(n_jobs=max(100, 50 * args.warmup), rate=args.rate, seed=6)
     # token pools drawn once on the device, per alphabet: leaf states uniform
     # with 5% gaps (A+1); each job reads a window of its alphabet's pool
-    POOL_C = max(d['C'] for d in desc)
-    max_leaves = max(d['leaves'] for d in desc)
+    POOL_C = max(d['C'] for d in desc + wdesc)
+    max_leaves = max(d['leaves'] for d in desc + wdesc)
     g = torch.Generator(device="cuda")
     g.manual_seed(5)
     pools = {}
-    for A_ in sorted({d['A'] for d in desc}):
+    for A_ in sorted({d['A'] for d in desc + wdesc}):
         v = torch.randint(0, 20 * A_, (max_leaves + 1, POOL_C), dtype=torch.int32, device="cuda", generator=g)
         pools[A_] = torch.where(v < 19 * A_, v % A_, A_ + 1).contiguous()
         pools[A_][max_leaves].fill_(A_)
         del v
     torch.cuda.synchronize()
-    jobs = []
-    for d in desc:
-        rng = np.random.default_rng(d['seed'])
-        A = d['A']
-        if d['kind'] == 'hky85':
-            model = models.hky85_diag(2.0, rng.dirichlet(np.ones(4)))
-        elif d['kind'] == 'f81':
-            model = models.f81_model(rng.dirichlet(np.ones(A)))
-        else:
-            model, _, _ = models.random_reversible(A, rng)
-        tree = synth.random_tree(d['leaves'], 0.1, rng)
-        R, C = len(tree.parentIndex), d['C']
-        leaf = synth.leaf_mask(tree)
 
-        # pool row of every tree row: leaves take distinct random rows, internal
-        # rows the pool's constant row of A (unobserved)
-        rowmap = np.full(R, max_leaves, dtype=np.int64)
-        rowmap[leaf] = np.arange(int(leaf.sum()))
-        rowmap = torch.from_numpy(rowmap).cuda()
-        off = int(np.random.default_rng(d['seed']).integers(0, POOL_C - C + 1))
+    def build(descs):
+        out = []
+        for d in descs:
+            rng = np.random.default_rng(d['seed'])
+            A = d['A']
+            if d['kind'] == 'hky85':
+                model = models.hky85_diag(2.0, rng.dirichlet(np.ones(4)))
+            elif d['kind'] == 'f81':
+                model = models.f81_model(rng.dirichlet(np.ones(A)))
+            else:
+                model, _, _ = models.random_reversible(A, rng)
+            tree = synth.random_tree(d['leaves'], 0.1, rng)
+            R, C = len(tree.parentIndex), d['C']
+            leaf = synth.leaf_mask(tree)
+            # pool row of every tree row: leaves take distinct random rows,
+            # internal rows the pool's constant row of A (unobserved)
+            rowmap = np.full(R, max_leaves, dtype=np.int64)
+            rowmap[leaf] = np.arange(int(leaf.sum()))
+            rowmap = torch.from_numpy(rowmap).cuda()
+            off = int(np.random.default_rng(d['seed']).integers(0, POOL_C - C + 1))
 
-        def make(stream, device, out, C=C, A=A, rowmap=rowmap, off=off):
-            # the job's tokens in one gather, with no allocation and no host wait
-            torch.index_select(pools[A][:, off:off + C], 0, rowmap, out=out)
-        jobs.append(serve.Job(id=d['id'], alignment=make, shape=(R, C), tree=tree, model=model,
-                              f81=(d['kind'] == 'f81'), want=("counts",), arrival=d['arrival']))
+            def make(stream, device, out, C=C, A=A, rowmap=rowmap, off=off):
+                # the job's tokens in one gather, with no allocation and no host wait
+                torch.index_select(pools[A][:, off:off + C], 0, rowmap, out=out)
+            out.append(serve.Job(id=d['id'], alignment=make, shape=(R, C), tree=tree, model=model,
+                                 f81=(d['kind'] == 'f81'), want=("counts",), arrival=d['arrival']))
+        return out
+
+    jobs, warm = build(desc), build(wdesc)
     srv = serve.Server(max_inflight=8, device_budget=64 << 30)
     srv.prewarm(host_bytes=4 << 30, device_bytes=48 << 30)
     # the consumer takes each result as it lands and hands its buffers back
+    srv.run(warm, realtime=False, on_done=lambda j: j.release())
+    srv.completed = []
+    srv.host_s = {k: 0.0 for k in srv.host_s}
     done = srv.run(jobs, realtime=True, on_done=lambda j: j.release())
     st = serve.latency_stats(done)
     kind_of = {d['id']: f"A={d['A']} {d['kind']}" for d in desc}

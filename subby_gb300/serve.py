@@ -118,7 +118,8 @@ class Server:
     """Continuous batching over CUDA streams with memory-budget admission."""
 
     def __init__(self, max_inflight: int = 8, device_budget: int = 16 << 30, plan_cache: int = 64,
-                 device=None, short_ms: float = 5.0, slice_ms: float = 8.0, aging: float = 0.2):
+                 device=None, short_ms: float = 5.0, slice_ms: float = 8.0, aging: float = 0.2,
+                 short_slots: int = 2):
         import torch
         self.torch = torch
         self.device = torch.device("cuda", torch.cuda.current_device() if device is None else device)
@@ -127,6 +128,7 @@ class Server:
         self.short_ms = short_ms
         self.slice_ms = slice_ms
         self.aging = aging          # ms of estimated cost forgiven per ms waited
+        self.short_slots = min(short_slots, max_inflight - 1)
         # one normal- and one high-priority stream per slot
         self.streams = [torch.cuda.Stream(device=self.device) for _ in range(max_inflight)]
         self.hi_streams = [torch.cuda.Stream(device=self.device, priority=-8) for _ in range(max_inflight)]
@@ -306,6 +308,11 @@ class Server:
         A = len(ensure_diag(job.model).pi)
         need = job_device_bytes(R, C, A)
         if not self.free_slots:
+            return False
+        # long jobs may hold all but `short_slots` slots, so that short jobs
+        # always find one free
+        if self._cost(job) > self.short_ms and \
+                sum(self._cost(j) > self.short_ms for j, *_ in self.inflight) >= self.max_inflight - self.short_slots:
             return False
         key = self._key(job)
         if any(self._key(j) == key for j, *_ in self.inflight):

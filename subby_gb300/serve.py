@@ -22,8 +22,9 @@ Jobs (alignment, tree, model, options) arrive over time.  The loop
 * estimates each job's device time from its shape (``job_cost_ms``): short
   jobs go to high-priority streams, so the block scheduler starts their
   kernels ahead of queued work of long jobs, and long jobs are cut into
-  column slices of about ``slice_ms`` each (whole 128-column tiles), so a
-  short job waits for at most one slice rather than a whole long job.
+  column slices of about ``slice_ms`` each (whole waves of the persistent
+  kernels' grids), so a short job waits for at most one slice rather than a
+  whole long job.
 
 Results of a job do not depend on what else is in flight: every job runs the
 same kernel on the same inputs as it would alone (``tests/test_gpu_serving``
@@ -119,7 +120,7 @@ class Server:
 
     def __init__(self, max_inflight: int = 8, device_budget: int = 16 << 30, plan_cache: int = 64,
                  device=None, short_ms: float = 5.0, slice_ms: float = 8.0, aging: float = 0.2,
-                 short_slots: int = 2):
+                 short_slots: int = 2, wave_cols: int = 0):
         import torch
         self.torch = torch
         self.device = torch.device("cuda", torch.cuda.current_device() if device is None else device)
@@ -129,10 +130,12 @@ class Server:
         self.slice_ms = slice_ms
         self.aging = aging          # ms of estimated cost forgiven per ms waited
         self.short_slots = min(short_slots, max_inflight - 1)
+        self.wave_cols = wave_cols  # slice granularity (0: one wave of the kernels' grids)
         # one normal- and one high-priority stream per slot
         self.streams = [torch.cuda.Stream(device=self.device) for _ in range(max_inflight)]
         self.hi_streams = [torch.cuda.Stream(device=self.device, priority=-8) for _ in range(max_inflight)]
         self.arenas = [None] * max_inflight
+        self.nsm = torch.cuda.get_device_properties(self.device).multi_processor_count
         self.free_slots = list(range(max_inflight))
         self.plans = collections.OrderedDict()
         self.plan_cache = plan_cache
@@ -232,10 +235,14 @@ class Server:
         plan = self.plan_for(job.tree, job.model, self._key(job))
         kw = dict(loglike="logLike" in job.want, counts="counts" in job.want,
                   rootprob="rootProb" in job.want, f81=job.f81, branch_mask=job.branch_mask)
-        nsl = max(1, min(int(np.ceil(cost / self.slice_ms)), (C + 127) // 128))
+        # slices are whole waves of the kernels' persistent grids (a thinner
+        # slice runs as long as a full wave on fewer SMs)
+        wave = self.wave_cols or self.nsm * (128 if A == 64 else 256)
+        nsl = max(1, min(int(np.ceil(cost / self.slice_ms)), (C + wave - 1) // wave))
         if not isinstance(job.branch_mask, str):
             nsl = 1
-        cmax = C if nsl == 1 else ((C + nsl - 1) // nsl + 127) // 128 * 128
+        cmax = C if nsl == 1 else ((C + nsl - 1) // nsl + wave - 1) // wave * wave
+        nsl = (C + cmax - 1) // cmax
         f32, i32 = torch.float32, torch.int32
         shapes = {"logLike": (C,), "counts": (A, A, C), "rootProb": (A, C)}
         want = [k for k in ("logLike", "counts", "rootProb") if k in job.want]
@@ -268,7 +275,7 @@ class Server:
             else:
                 # long job: column slices of whole 128-column tiles, each its
                 # own launch sequence, results gathered on the device
-                edges = [min(C, ((C * i // nsl) + 127) // 128 * 128) for i in range(nsl)] + [C]
+                edges = [min(C, i * cmax) for i in range(nsl)] + [C]
                 for c0, c1 in zip(edges[:-1], edges[1:]):
                     cc = c1 - c0
                     if cc <= 0:

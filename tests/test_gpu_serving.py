@@ -62,7 +62,8 @@ def test_admission_respects_budget_and_slots():
 
 
 def test_sliced_long_jobs_and_priority_streams_give_identical_results():
-    """With a tiny slice budget every job is cut into 128-column slices (and
+    """With a tiny slice budget and 128-column slice granularity every job is
+    cut into 128-column slices (and
     short-job threshold 0 sends all to normal-priority streams, a large one
     to high-priority streams); the results equal the unsliced run bit for
     bit, because every column is computed independently."""
@@ -73,7 +74,8 @@ def test_sliced_long_jobs_and_priority_streams_give_identical_results():
         ref[j.id] = plan.run(j.alignment, loglike=True, counts=True, f81=j.f81)
         plan.close()
     for short_ms, slice_ms in ((0.0, 1e-6), (1e9, 1e-6)):
-        srv = serve.Server(max_inflight=4, device_budget=1 << 30, short_ms=short_ms, slice_ms=slice_ms)
+        srv = serve.Server(max_inflight=4, device_budget=1 << 30, short_ms=short_ms, slice_ms=slice_ms,
+                           wave_cols=128)
         done = srv.run(_jobs(n=8, seed=10), realtime=False)
         assert len(done) == len(jobs)
         for j in done:

@@ -491,11 +491,14 @@ def serving_bench(args):
         if sub:
             s2 = serve.latency_stats(sub)
             by_kind[k] = {"jobs": s2['jobs'], "p50_ms": s2['p50_ms'], "p99_ms": s2['p99_ms'],
+                          "queue_p99_ms": s2['queue_p99_ms'], "service_p99_ms": s2['service_p99_ms'],
                           "columns": s2['columns']}
     srv.close()
     print(json.dumps({"metric": "serving latency (Poisson arrivals, uneven R/C/A)", "value": st['p99_ms'],
                       "unit": "ms (p99)", "higher_is_better": False, "p50_ms": st['p50_ms'],
                       "p99_ms": st['p99_ms'], "max_ms": st['max_ms'], "jobs": st['jobs'],
+                      "queue_p50_ms": st['queue_p50_ms'], "queue_p99_ms": st['queue_p99_ms'],
+                      "service_p50_ms": st['service_p50_ms'], "service_p99_ms": st['service_p99_ms'],
                       "columns_per_s": st['columns_per_s'], "span_s": st['span_s'], "rate_jobs_per_s": args.rate,
                       "by_kind": by_kind,
                       "host_s": {k: round(v, 3) for k, v in srv.host_s.items()},

@@ -403,7 +403,11 @@ class Server:
 
 def latency_stats(jobs):
     lat = np.array([j.latency for j in jobs]) * 1000.0
+    wait = np.array([j.start - j.arrival for j in jobs]) * 1000.0
+    serv = np.array([j.finish - j.start for j in jobs]) * 1000.0
     cols = sum(j.RC[1] for j in jobs)
     span = max(j.finish for j in jobs) - min(j.arrival for j in jobs)
     return {"jobs": len(jobs), "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+            "queue_p50_ms": float(np.percentile(wait, 50)), "queue_p99_ms": float(np.percentile(wait, 99)),
+            "service_p50_ms": float(np.percentile(serv, 50)), "service_p99_ms": float(np.percentile(serv, 99)),
             "max_ms": float(lat.max()), "columns": int(cols), "columns_per_s": cols / span, "span_s": span}

@@ -115,8 +115,9 @@ int big_acc_group(int A);
 // mode: 0 inside pass only (LogLike / RootProb), 1 stage eigen vectors, 2 stage F81 vectors
 int launch_walk(const KParams &p, int A, int mode, bool tc, float *sa, float *sb, int c_base, int c_count,
                 int grid, cudaStream_t s);
-int launch_acc(const KParams &p, int A, bool f81, const float *sa, const float *sb, int c_base, int c_count,
-               int grid, cudaStream_t s);
+// tc: A = 64 eigen back-transform on the tensor cores
+int launch_acc(const KParams &p, int A, bool f81, bool tc, const float *sa, const float *sb, int c_base,
+               int c_count, int grid, cudaStream_t s);
 int launch_tree4(const KParams &p, bool f81, int mask_mode, int grid, int block, size_t smem,
                  cudaStream_t s);
 // A = 64 F81 accumulation on the tensor cores (k_acctc.cu); groups of 8 columns

@@ -810,11 +810,22 @@ struct AccRing {
   static_assert(S >= 3, "ring too short");
 };
 
-template <int A, bool F81>
+// Shared-memory float offset of the static [V ; V] operand tile of the
+// tensor-core back-transform (A = 64), 1 KB aligned.
+template <int A>
+__host__ __device__ constexpr int acc_vv_offset() {
+  return ((AccRing<A>::SCAL + 2 * AccGeo<A>::G + 2 * A * A + A + 2 * AccGeo<A>::G * A + AccGeo<A>::G) + 255) / 256 *
+         256;
+}
+
+// TCB: back-transform V C V^T on the tensor cores (A = 64 eigen path of the
+// tensor-core Counts); otherwise on CUDA cores.
+template <int A, bool F81, bool TCB>
 __global__ void __launch_bounds__(256, 1) k_acc(const KParams P, const float *__restrict__ stage_a,
                                                  const float *__restrict__ stage_b, int c_base, int c_count) {
   using Gm = AccGeo<A>;
   using Rg = AccRing<A>;
+  static_assert(!TCB || (A == 64 && !F81), "tensor-core back-transform is A = 64 eigen");
   constexpr int G = Gm::G;
   constexpr int S = Rg::S;
   extern __shared__ __align__(128) float sm[];
@@ -863,7 +874,41 @@ __global__ void __launch_bounds__(256, 1) k_acc(const KParams P, const float *__
     }
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
+  // tensor-core back-transform: TMEM (T = C V^T in columns 0-127, V T in
+  // 128-191), its mbarrier, and the static A operand [V ; V] (three BF16 terms)
+  __shared__ uint32_t s_tm;
+  __shared__ __align__(8) uint64_t mbT;
+  if constexpr (TCB) {
+    if ((t >> 5) == 0) {
+      asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;"
+                   ::"r"((uint32_t)__cvta_generic_to_shared(&s_tm)), "r"(256) : "memory");
+      asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    if (t == 0) {
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"((uint32_t)__cvta_generic_to_shared(&mbT))
+                   : "memory");
+      asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();   // Vs is loaded
+    unsigned char *vv = reinterpret_cast<unsigned char *>(sm + acc_vv_offset<A>());
+    for (int idx = t; idx < 128 * 64; idx += blockDim.x) {
+      const int m = idx >> 6, l = idx & 63;
+      const float v = Vs[(m & 63) * 64 + l];
+      const __nv_bfloat16 b1 = __float2bfloat16_rn(v);
+      const float r1 = v - __bfloat162float(b1);
+      const __nv_bfloat16 b2 = __float2bfloat16_rn(r1);
+      const __nv_bfloat16 b3 = __float2bfloat16_rn(r1 - __bfloat162float(b2));
+      const uint32_t o = kmaj_off(m, l);
+      *reinterpret_cast<__nv_bfloat16 *>(vv + o) = b1;
+      *reinterpret_cast<__nv_bfloat16 *>(vv + 16384 + o) = b2;
+      *reinterpret_cast<__nv_bfloat16 *>(vv + 32768 + o) = b3;
+    }
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  }
   __syncthreads();
+  if constexpr (TCB) asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  uint32_t nT = 0;  // completed phases of mbT
   uint32_t it = 0;  // ring position of the next branch to consume (all groups)
 
   for (int gi = blockIdx.x; gi < ngroups; gi += gridDim.x) {
@@ -1045,6 +1090,142 @@ __global__ void __launch_bounds__(256, 1) k_acc(const KParams P, const float *__
       __syncthreads();
       continue;
     }
+    if constexpr (TCB) {
+      // Per column pair (2p, 2p+1): B1 = [C_2p ; C_2p+1] (rows (c, k), K = l);
+      // D1 = [V ; V] B1^T holds T_c^T (lane (c, j), column k) in its
+      // diagonal blocks; A2 = those rows (K = k); D2 = A2 V^T holds
+      // (V C V^T)_c[i][j] at lane (c, j), column i.
+      const uint32_t base = (uint32_t)__cvta_generic_to_shared(sm);
+      const uint32_t B1 = base, A2 = base + 49152;
+      float *Pst = sm + (98304 / 4);                 // [i][j][2] staging of one pair
+      const uint32_t VV = base + 4u * acc_vv_offset<A>();
+      const uint32_t tm = s_tm;
+      const int warp = t >> 5, lane = t & 31, sub = warp & 3, hh = warp >> 2;
+      const int m = 32 * sub + lane, cg = m >> 6, jj = m & 63;
+      auto mma6 = [&](uint32_t d, uint32_t a, uint32_t b, uint32_t idesc) {
+        constexpr int pa[6] = {0, 0, 1, 0, 1, 2}, pb[6] = {0, 1, 0, 2, 1, 0};
+#pragma unroll
+        for (int ks = 0; ks < 4; ++ks)
+#pragma unroll
+          for (int prod = 0; prod < 6; ++prod) {
+            const uint32_t accum = (ks | prod) != 0;
+            asm volatile("{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+                         " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}"
+                         ::"r"(d), "l"(umma_desc(a + pa[prod] * 16384 + ks * 256)),
+                         "l"(umma_desc(b + pb[prod] * 16384 + ks * 256)), "r"(idesc), "r"(accum) : "memory");
+          }
+        asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
+                     ::"r"((uint32_t)__cvta_generic_to_shared(&mbT)) : "memory");
+      };
+      auto sync_tc = [&]() {
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+        __syncthreads();
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      };
+      auto wait_t = [&]() {
+        if (!mbar_wait((uint32_t)__cvta_generic_to_shared(&mbT), nT & 1)) s_err = 1;
+        ++nT;
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      };
+      auto ld32 = [&](uint32_t col, uint32_t (&r)[32]) {
+        asm volatile("tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,"
+                     "%15,%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+                     : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+                       "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+                       "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]),
+                       "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]),
+                       "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+                     : "r"(tm + ((uint32_t)(32 * sub) << 16) + col)
+                     : "memory");
+        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+      };
+      auto split3 = [](float x0, float x1, uint32_t &t1, uint32_t &t2, uint32_t &t3) {
+        const __nv_bfloat162 b1 = __floats2bfloat162_rn(x0, x1);
+        const float2 f1 = __bfloat1622float2(b1);
+        const float r0 = x0 - f1.x, r1 = x1 - f1.y;
+        const __nv_bfloat162 b2 = __floats2bfloat162_rn(r0, r1);
+        const float2 f2 = __bfloat1622float2(b2);
+        const __nv_bfloat162 b3 = __floats2bfloat162_rn(r0 - f2.x, r1 - f2.y);
+        t1 = *reinterpret_cast<const uint32_t *>(&b1);
+        t2 = *reinterpret_cast<const uint32_t *>(&b2);
+        t3 = *reinterpret_cast<const uint32_t *>(&b3);
+      };
+      const bool vec2 = (C & 1) == 0 && (c_base & 1) == 0;
+#pragma unroll
+      for (int p = 0; p < 4; ++p) {
+        // (a) B1 rows of this thread's 4 x 4 block for the two columns
+#pragma unroll
+        for (int h2 = 0; h2 < 2; ++h2) {
+          const int q = 2 * p + h2;
+#pragma unroll
+          for (int a = 0; a < 4; ++a) {
+            uint32_t u1[2], u2[2], u3[2];
+            split3(ac2[a][0][q].x, ac2[a][0][q].y, u1[0], u2[0], u3[0]);
+            split3(ac2[a][1][q].x, ac2[a][1][q].y, u1[1], u2[1], u3[1]);
+            const uint32_t o = B1 + kmaj_off(64 * h2 + k0 + a, l0);
+            asm volatile("st.shared.v2.b32 [%0], {%1, %2};" ::"r"(o), "r"(u1[0]), "r"(u1[1]) : "memory");
+            asm volatile("st.shared.v2.b32 [%0], {%1, %2};" ::"r"(o + 16384), "r"(u2[0]), "r"(u2[1]) : "memory");
+            asm volatile("st.shared.v2.b32 [%0], {%1, %2};" ::"r"(o + 32768), "r"(u3[0]), "r"(u3[1]) : "memory");
+          }
+        }
+        sync_tc();
+        if (t == 0) mma6(tm, VV, B1, kIdesc128);
+        wait_t();
+        // (e) T_c^T rows (lane (cg, jj), k in [32 hh, 32 hh + 32)) into A2
+        {
+          uint32_t r[32];
+          ld32(64u * cg + 32u * hh, r);
+#pragma unroll
+          for (int q = 0; q < 4; ++q) {
+            uint32_t w1[4], w2[4], w3[4];
+#pragma unroll
+            for (int pp = 0; pp < 4; ++pp)
+              split3(__uint_as_float(r[8 * q + 2 * pp]), __uint_as_float(r[8 * q + 2 * pp + 1]), w1[pp], w2[pp], w3[pp]);
+            const uint32_t o = A2 + kmaj_off(m, 32 * hh + 8 * q);
+            asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};" ::"r"(o), "r"(w1[0]), "r"(w1[1]), "r"(w1[2]),
+                         "r"(w1[3]) : "memory");
+            asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};" ::"r"(o + 16384), "r"(w2[0]), "r"(w2[1]),
+                         "r"(w2[2]), "r"(w2[3]) : "memory");
+            asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};" ::"r"(o + 32768), "r"(w3[0]), "r"(w3[1]),
+                         "r"(w3[2]), "r"(w3[3]) : "memory");
+          }
+        }
+        sync_tc();
+        if (t == 0) mma6(tm + 128, A2, VV, kIdesc);
+        wait_t();
+        // (i) V C V^T of (column cg, j = jj), i in [32 hh, 32 hh + 32)
+        {
+          uint32_t r[32];
+          ld32(128u + 32u * hh, r);
+#pragma unroll
+          for (int i = 0; i < 32; ++i) Pst[((32 * hh + i) * 64 + jj) * 2 + cg] = __uint_as_float(r[i]);
+        }
+        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+        __syncthreads();
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        // (k) counts rows (i, j) of the two columns
+        {
+          const int cp = c_base + g0 + 2 * p;
+          const int nc = gcols - 2 * p;
+          if (nc > 0)
+            for (int e = t; e < 64 * 64; e += 256) {
+              const int i = e >> 6, j = e & 63;
+              const float f = (i == j) ? 1.f : Ss[e];
+              const float2 v = *reinterpret_cast<const float2 *>(Pst + 2 * e);
+              float *o = P.counts + (size_t)e * C + cp;
+              if (vec2 && nc >= 2) {
+                *reinterpret_cast<float2 *>(o) = make_float2(f * v.x, f * v.y);
+              } else {
+                o[0] = f * v.x;
+                if (nc >= 2) o[1] = f * v.y;
+              }
+            }
+        }
+      }
+      __syncthreads();
+      continue;
+    }
     // back-transform: C -> T = C V^T -> VCV = V T, through shared memory [c][k][l]
     float *Cs = sm;  // G * A * A floats
     const float *V = Vs;
@@ -1149,6 +1330,13 @@ __global__ void __launch_bounds__(256, 1) k_acc(const KParams P, const float *__
     }
     __syncthreads();
   }
+  if constexpr (TCB) {
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    if ((t >> 5) == 0)
+      asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(s_tm), "r"(256) : "memory");
+  }
   if (t == 0 && s_err && P.err) atomicAdd(P.err, 1);
 }
 #undef ACC
@@ -1191,22 +1379,27 @@ int walk_launch(const KParams &p, int mode, bool tc, float *sa, float *sb, int c
   return walk_launch_tc<A, false>(p, mode, sa, sb, c_base, c_count, grid, s);
 }
 
-template <int A>
-int acc_launch(const KParams &p, bool f81, const float *sa, const float *sb, int c_base, int c_count, int grid,
-               cudaStream_t s) {
+template <int A, bool F81, bool TCB>
+int acc_launch1(const KParams &p, const float *sa, const float *sb, int c_base, int c_count, int grid,
+                cudaStream_t s) {
   using Gm = AccGeo<A>;
-  const size_t smem = (size_t)(AccRing<A>::SCAL + 2 * Gm::G + 2 * A * A + A + 2 * Gm::G * A + Gm::G) * sizeof(float);
-  cudaError_t e;
-  if (f81) {
-    e = cudaFuncSetAttribute(k_acc<A, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return (int)e;
-    k_acc<A, true><<<grid, 256, smem, s>>>(p, sa, sb, c_base, c_count);
-  } else {
-    e = cudaFuncSetAttribute(k_acc<A, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return (int)e;
-    k_acc<A, false><<<grid, 256, smem, s>>>(p, sa, sb, c_base, c_count);
-  }
+  const size_t smem = TCB ? (size_t)acc_vv_offset<A>() * sizeof(float) + 49152
+                          : (size_t)(AccRing<A>::SCAL + 2 * Gm::G + 2 * A * A + A + 2 * Gm::G * A + Gm::G) *
+                                sizeof(float);
+  cudaError_t e = cudaFuncSetAttribute(k_acc<A, F81, TCB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return (int)e;
+  k_acc<A, F81, TCB><<<grid, 256, smem, s>>>(p, sa, sb, c_base, c_count);
   return (int)cudaGetLastError();
+}
+
+template <int A>
+int acc_launch(const KParams &p, bool f81, bool tc, const float *sa, const float *sb, int c_base, int c_count,
+               int grid, cudaStream_t s) {
+  if (f81) return acc_launch1<A, true, false>(p, sa, sb, c_base, c_count, grid, s);
+  if constexpr (A == 64) {
+    if (tc) return acc_launch1<A, false, true>(p, sa, sb, c_base, c_count, grid, s);
+  }
+  return acc_launch1<A, false, false>(p, sa, sb, c_base, c_count, grid, s);
 }
 
 }  // namespace
@@ -1234,13 +1427,13 @@ int launch_walk(const KParams &p, int A, int mode, bool tc, float *sa, float *sb
   }
 }
 
-int launch_acc(const KParams &p, int A, bool f81, const float *sa, const float *sb, int c_base, int c_count,
-               int grid, cudaStream_t s) {
+int launch_acc(const KParams &p, int A, bool f81, bool tc, const float *sa, const float *sb, int c_base,
+               int c_count, int grid, cudaStream_t s) {
   switch (A) {
-    case 16: return acc_launch<16>(p, f81, sa, sb, c_base, c_count, grid, s);
-    case 20: return acc_launch<20>(p, f81, sa, sb, c_base, c_count, grid, s);
-    case 32: return acc_launch<32>(p, f81, sa, sb, c_base, c_count, grid, s);
-    case 64: return acc_launch<64>(p, f81, sa, sb, c_base, c_count, grid, s);
+    case 16: return acc_launch<16>(p, f81, false, sa, sb, c_base, c_count, grid, s);
+    case 20: return acc_launch<20>(p, f81, false, sa, sb, c_base, c_count, grid, s);
+    case 32: return acc_launch<32>(p, f81, false, sa, sb, c_base, c_count, grid, s);
+    case 64: return acc_launch<64>(p, f81, tc, sa, sb, c_base, c_count, grid, s);
     default: return -1;
   }
 }

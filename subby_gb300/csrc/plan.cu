@@ -951,7 +951,7 @@ int run_big(subby_plan *P, const int32_t *d_aln, int C, float *d_logL, float *d_
       const int G = big_acc_group(A);
       const int agrid = std::max(1, std::min((cc + G - 1) / G, P->nsm));
       lr = f81tc ? launch_acc_f81_tc(k, sa, sb, k.stage_c, c0, cc, agrid, stream)
-                 : launch_acc(k, A, (mode & kModeF81) != 0, sa, sb, c0, cc, agrid, stream);
+                 : launch_acc(k, A, (mode & kModeF81) != 0, tc, sa, sb, c0, cc, agrid, stream);
       if (lr != 0) return fail(SUBBY_ERR_CUDA, std::string("accumulate launch failed: ") + cudaGetErrorString((cudaError_t)lr));
       g_launches += 1;
     }

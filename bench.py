@@ -163,7 +163,7 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--columns", type=int, default=1 << 20)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", choices=["plain_large", "precision64", "grad20", "serving"],
+    ap.add_argument("--workload", choices=["plain_large", "precision64", "f81_64", "grad20", "serving"],
                     default="plain_large",
                     help="plain_large is the headline line; the others print their own line")
     ap.add_argument("--jobs", type=int, default=10000, help="serving: number of jobs")
@@ -188,6 +188,8 @@ def main():
         return precision64_bench(args)
     if args.workload == "grad20":
         return grad20_bench(args)
+    if args.workload == "f81_64":
+        return f81_64_bench(args)
 
     # spawn pool for the CPU baseline before any GPU work
     pool = None
@@ -393,6 +395,36 @@ def precision64_bench(args):
                                    "note": "useful walk FLOP over the whole Counts step; split-BF16 issues 6 "
                                            "MMAs per product"},
                       "variants": res}))
+    return 0
+
+
+def f81_64_bench(args):
+    """A=64 F81 model (pi ~ Dirichlet(1^64)), the precision64 tree (R=127),
+    C=65536 simulated columns: F81 fast-path Counts (closed-form walk and
+    tensor-core accumulation) and eigen-path Counts of the same model."""
+    import torch
+    import oracle
+    import subby_gb300 as sg
+    from subby_gb300 import synth, models
+    from tests._tol import colwise_err
+    C = args.columns if args.columns != (1 << 20) else 65536
+    rng = np.random.default_rng(11)
+    model = models.f81_model(rng.dirichlet(np.ones(64)))
+    tree = synth.random_tree(64, 0.1, rng)
+    aln = synth.simulated_alignment(tree, model, C, 0.05, rng)
+    plan = sg.Plan(tree, model)
+    d_aln = torch.as_tensor(aln).cuda()
+    out = {'counts': torch.empty((64, 64, C), dtype=torch.float32, device="cuda")}
+    ms_f81 = _time_fn(lambda: plan.run(d_aln, loglike=False, counts=True, f81=True, out=out), args.steps, args.warmup)
+    t = oracle.Tree(tree.parentIndex, tree.distanceToParent)
+    err = colwise_err(out['counts'][:, :, :16].cpu().numpy(),
+                      oracle.Counts(aln[:, :16], t, model._asdict(), f81_fast=True))
+    ms_eig = _time_fn(lambda: plan.run(d_aln, loglike=False, counts=True, out=out), args.steps, args.warmup)
+    print(json.dumps({"metric": "F81 fast-path Counts columns/s (A=64 F81, R=127, C=65536)", "value": C / (ms_f81 / 1e3),
+                      "unit": UNIT, "ms_per_step": ms_f81, "steps": args.steps, "warmup": args.warmup,
+                      "higher_is_better": True, "dtype": "fp32 (split-bf16 tensor-core G accumulation)",
+                      "err_vs_oracle_colwise_16cols": err,
+                      "eigen_path_same_model": {"value": C / (ms_eig / 1e3), "ms_per_step": ms_eig}}))
     return 0
 
 

@@ -960,14 +960,13 @@ int run_big(subby_plan *P, const int32_t *d_aln, int C, float *d_logL, float *d_
 }
 
 // Columns per chunk of the host-pointer pipeline: whole waves of the
-// one-CTA-per-SM kernels (nsm x 256 columns), about sixteen chunks for large
-// C (the pipeline fill — first copy-in, last kernel and copy-out — shrinks
-// with the chunk), a single chunk below two waves (nothing to overlap).
+// one-CTA-per-SM kernels (nsm x 256 columns), about eight chunks for large C,
+// a single chunk below two waves (nothing to overlap).
 int host_chunk_columns(const subby_plan *P, int C) {
   const long long wave = (long long)std::max(P->nsm, 1) * 256;
   if (C < 2 * wave) return std::max(C, 1);
   const long long waves = (C + wave - 1) / wave;
-  const long long per = std::max(1LL, (waves + 15) / 16);
+  const long long per = std::max(1LL, (waves + 7) / 8);
   return (int)std::min<long long>(C, per * wave);
 }
 

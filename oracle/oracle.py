@@ -284,6 +284,59 @@ def f81_counts(U, D, logNormU, logNormD, logLike, distances, pi, parentIndex,
     return out
 
 
+def accumulate_C_per_branch(D_tilde, U_tilde, J, logNormU, logNormD, logLike, parentIndex,
+                            branch_mask=None):
+    """Per-branch eigenbasis counts (R, A, A, C), branch 0 zero; oracle.py:1047-1084."""
+    R, C, A = U_tilde.shape
+    out = np.zeros((R, A, A, C))
+    for n in range(1, R):
+        s = np.exp(logNormD[n] + logNormU[n] - logLike)
+        if branch_mask is not None:
+            s = np.where(np.asarray(branch_mask)[n], s, 0.0)
+        out[n] = np.einsum('ck,kl,cl->klc', D_tilde[n] * s[:, None], J[n], U_tilde[n])
+    return out
+
+
+def back_transform_per_branch(Ceig, model):
+    """V C_n V^T per branch: dwell on the diagonal, S * VCV off it; oracle.py:1140-1183."""
+    V = np.asarray(model['eigenvectors'], dtype=np.float64)
+    mu = np.asarray(model['eigenvalues'], dtype=np.float64)
+    S = (V * mu[None, :]) @ V.T
+    VCV = np.einsum('ik,nklc,jl->nijc', V, Ceig, V)
+    A = V.shape[0]
+    eye = np.eye(A, dtype=bool)[None, :, :, None]
+    return np.where(eye, VCV, S[None, :, :, None] * VCV)
+
+
+def f81_counts_per_branch(U, D, logNormU, logNormD, logLike, distances, pi, parentIndex,
+                          branch_mask=None):
+    """Closed-form F81/JC counts per branch (R, A, A, C); oracle.py:1259-1331."""
+    R, C, A = U.shape
+    pi = np.asarray(pi, dtype=np.float64)
+    mu = 1.0 / (1.0 - np.sum(pi ** 2))
+    out = np.zeros((R, A, A, C))
+    offdiag = ~np.eye(A, dtype=bool)
+    for n in range(1, R):
+        t = distances[n]
+        e = np.exp(-mu * t)
+        p = 1.0 - e
+        alpha = t * e
+        beta = p / mu - t * e
+        gamma = t * (1.0 + e) - 2.0 * p / mu
+        s = np.exp(logNormD[n] + logNormU[n] - logLike)
+        if branch_mask is not None:
+            s = np.where(np.asarray(branch_mask)[n], s, 0.0)
+        Ds = D[n] * s[:, None]
+        piU = U[n] @ pi
+        Dsum = Ds.sum(-1)
+        I = (alpha * np.einsum('ci,cj->ijc', Ds, U[n])
+             + beta * (np.einsum('ci,c->ic', Ds, piU)[:, None, :]
+                       + np.einsum('i,c,cj->ijc', pi, Dsum, U[n]))
+             + gamma * np.einsum('i,c->ic', pi, Dsum * piU)[:, None, :])
+        out[n] = np.where(offdiag[:, :, None], mu * pi[None, :, None] * I, I)
+    return out
+
+
 def compute_branch_mask(alignment, parentIndex, A):
     """Steiner-tree branch mask of ungapped leaves; oracle.py:1372-1435.
 
@@ -337,6 +390,25 @@ def Counts(alignment, tree, model, f81_fast=False, branch_mask="auto"):
     Ut, Dt = eigenbasis_project(U, D, model)
     Ceig = accumulate_C(Dt, Ut, J, lnU, lnD, lnL, tree.parentIndex, branch_mask=branch_mask)
     return back_transform(Ceig, model)
+
+
+def BranchCounts(alignment, tree, model, f81_fast=False, branch_mask=None):
+    """(R, A, A, C) per-branch dwell/substitution counts, branch 0 zero;
+    oracle.py:1517-1568.  The default mask is None, as in subby.jax.BranchCounts
+    (subby/jax/__init__.py:450-540), which does not mask."""
+    A = len(model['pi'])
+    if isinstance(branch_mask, str) and branch_mask == "auto":
+        branch_mask = compute_branch_mask(alignment, tree.parentIndex, A)
+    M = compute_sub_matrices(model, tree.distanceToParent)
+    U, lnU, lnL = upward_pass(alignment, tree, M, model['pi'])
+    D, lnD = downward_pass(U, lnU, tree, M, model['pi'], alignment)
+    if f81_fast:
+        return f81_counts_per_branch(U, D, lnU, lnD, lnL, tree.distanceToParent, model['pi'],
+                                     tree.parentIndex, branch_mask=branch_mask)
+    J = compute_J(model['eigenvalues'], tree.distanceToParent)
+    Ut, Dt = eigenbasis_project(U, D, model)
+    return back_transform_per_branch(
+        accumulate_C_per_branch(Dt, Ut, J, lnU, lnD, lnL, tree.parentIndex, branch_mask=branch_mask), model)
 
 
 def RootProb(alignment, tree, model):

@@ -16,8 +16,8 @@ and runs it on
 
 and writes one ``.npz`` per case holding the inputs, the reference oracle's
 outputs (logLike, unmasked and Steiner-masked Counts, F81 fast-path Counts
-where the model is F81/JC, RootProb, branch mask) and, for the small A=4
-cases, its intermediates.  The fixtures travel with the repository; the
+where the model is F81/JC, per-branch counts for A <= 8, RootProb, branch
+mask) and, for the small A=4 cases, its intermediates.  The fixtures travel with the repository; the
 reference itself is never read by the GPU tests.
 """
 from __future__ import annotations
@@ -60,6 +60,13 @@ def run_case(oracle, RTree, name, alignment, parent, dist, model, f81_ok,
         if masked:
             out['counts_f81_masked'] = oracle.Counts(alignment, tree, m, f81_fast=True,
                                                      branch_mask="auto")
+    if A <= 8:
+        # per-branch outputs (the reference's loops are O(R C A^4): small A only)
+        out['branch_counts'] = oracle.BranchCounts(alignment, tree, m, branch_mask=None)
+        if masked:
+            out['branch_counts_masked'] = oracle.BranchCounts(alignment, tree, m, branch_mask="auto")
+        if f81_ok:
+            out['branch_counts_f81'] = oracle.BranchCounts(alignment, tree, m, f81_fast=True, branch_mask=None)
     out['root_prob'] = oracle.RootProb(alignment, tree, m)
     out['branch_mask'] = oracle.compute_branch_mask(alignment, parent, A)
     if intermediates:

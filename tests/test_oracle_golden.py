@@ -45,6 +45,15 @@ def test_outputs_match_reference_oracle(name):
     np.testing.assert_allclose(oracle.RootProb(aln, tree, model), g['root_prob'], rtol=1e-12, atol=1e-12)
     np.testing.assert_array_equal(
         oracle.compute_branch_mask(aln, g['parentIndex'], int(g['A'])), g['branch_mask'])
+    if 'branch_counts' in g:
+        np.testing.assert_allclose(oracle.BranchCounts(aln, tree, model), g['branch_counts'],
+                                   rtol=1e-9, atol=1e-11)
+    if 'branch_counts_masked' in g:
+        np.testing.assert_allclose(oracle.BranchCounts(aln, tree, model, branch_mask="auto"),
+                                   g['branch_counts_masked'], rtol=1e-9, atol=1e-11)
+    if 'branch_counts_f81' in g:
+        np.testing.assert_allclose(oracle.BranchCounts(aln, tree, model, f81_fast=True),
+                                   g['branch_counts_f81'], rtol=1e-9, atol=1e-11)
 
 
 @pytest.mark.parametrize("name", [n for n in CASES if 'U' in _golden.load(n)])

@@ -92,6 +92,18 @@ int subby_plan_create(const int32_t *parent_index, const double *distances,
 int subby_plan_destroy(subby_plan *plan);
 /* Bytes of device memory the plan currently holds (tables + workspace). */
 size_t subby_plan_device_bytes(const subby_plan *plan);
+/*
+ * Per-branch counts: branchCounts (R, A, A, C) — for each branch n (the
+ * branch above node n; n = 0, the root, is zeros) the dwell times (diagonal)
+ * and substitution counts (off-diagonal) per column.  counts_kind, mask_mode
+ * and mask as for subby_plan_run (subby.jax.BranchCounts does not mask: pass
+ * SUBBY_MASK_NONE for its semantics).  Implemented for A = 4; other
+ * alphabets return SUBBY_ERR_UNSUPPORTED.  Replaces subby.jax BranchCounts
+ * (subby/jax/__init__.py:450-540) and the oracle's BranchCounts
+ * (subby/oracle/oracle.py:1517-1568).
+ */
+int subby_plan_branch_counts(subby_plan *plan, const int32_t *alignment, int C, float *branchCounts,
+                             int counts_kind, int mask_mode, const uint8_t *mask, int flags, void *stream);
 /* Release the plan's workspace (staging, scratch, host-call buffers) in
  * stream order after its last enqueued kernel; the tables stay.  The next
  * run allocates again (from the library pool).  For servers that keep many

@@ -6,10 +6,11 @@ root posteriors.  Drop-in for the single-model entry points of ``subby.jax``.
 from .types import Tree, DiagModel, RateModel
 from .models import (hky85_diag, jukes_cantor_model, f81_model, diagonalize_rate_matrix,
                      reversible_rate_matrix, random_reversible)
-from .api import LogLike, Counts, RootProb, LogLikeCustomGrad, Plan, get_plan, clear_plan_cache
+from .api import (LogLike, Counts, BranchCounts, RootProb, LogLikeCustomGrad, Plan, get_plan,
+                  clear_plan_cache)
 from . import _lib
 
-__all__ = ["Tree", "DiagModel", "RateModel", "hky85_diag", "jukes_cantor_model", "f81_model",
+__all__ = ["BranchCounts", "Tree", "DiagModel", "RateModel", "hky85_diag", "jukes_cantor_model", "f81_model",
            "diagonalize_rate_matrix", "reversible_rate_matrix", "random_reversible", "LogLike",
            "Counts", "RootProb", "LogLikeCustomGrad", "Plan", "get_plan", "clear_plan_cache"]
 

@@ -171,6 +171,52 @@ class Plan:
                 "subby_plan_run")
         return res
 
+    def branch_counts(self, alignment, f81=False, branch_mask=None, out=None, stream=None):
+        """Per-branch counts (R, A, A, C): dwell times (diagonal) and
+        substitution counts (off-diagonal) of every branch (branch 0, the
+        root, is zeros).  ``branch_mask`` defaults to None (unmasked), as in
+        subby.jax.BranchCounts; "auto" and an (R, C) array are accepted."""
+        lib = _lib.load()
+        kind = _lib.COUNTS_F81 if f81 else _lib.COUNTS_EIGEN
+        if isinstance(branch_mask, str):
+            if branch_mask != "auto":
+                raise ValueError('branch_mask must be "auto", None or an (R, C) array')
+            mask_mode, mask = _lib.MASK_AUTO, None
+        elif branch_mask is None:
+            mask_mode, mask = _lib.MASK_NONE, None
+        else:
+            mask_mode, mask = _lib.MASK_GIVEN, branch_mask
+        A, R = self.A, self.R
+        if _is_torch(alignment) and alignment.is_cuda:
+            import torch
+            aln = alignment.to(torch.int32).contiguous()
+            if aln.dim() != 2 or aln.shape[0] != R:
+                raise ValueError(f"alignment must have shape (R={R}, C)")
+            C = int(aln.shape[1])
+            res = out if out is not None else torch.empty((R, A, A, C), dtype=torch.float32, device=aln.device)
+            dmask = None
+            if mask_mode == _lib.MASK_GIVEN:
+                dmask = torch.as_tensor(np.asarray(mask) if not _is_torch(mask) else mask)
+                dmask = dmask.to(device=aln.device, dtype=torch.uint8).contiguous()
+            st = (stream if stream is not None else torch.cuda.current_stream(aln.device)).cuda_stream
+            with self._lock, _device_ctx(aln.device):
+                _lib.check(lib.subby_plan_branch_counts(
+                    self._handle, ct.c_void_p(aln.data_ptr()), C, ct.c_void_p(res.data_ptr()), kind, mask_mode,
+                    ct.c_void_p(dmask.data_ptr()) if dmask is not None else None, _lib.DEVICE_PTRS,
+                    ct.c_void_p(st)), "subby_plan_branch_counts")
+            return res
+        aln = _np(alignment, np.int32)
+        if aln.ndim != 2 or aln.shape[0] != R:
+            raise ValueError(f"alignment must have shape (R={R}, C)")
+        C = int(aln.shape[1])
+        res = out if out is not None else np.empty((R, A, A, C), dtype=np.float32)
+        hmask = _np(mask, np.uint8) if mask_mode == _lib.MASK_GIVEN else None
+        with self._lock, _device_ctx(self.device):
+            _lib.check(lib.subby_plan_branch_counts(
+                self._handle, _ptr(aln), C, _ptr(res), kind, mask_mode,
+                _ptr(hmask) if hmask is not None else None, 0, None), "subby_plan_branch_counts")
+        return res
+
     def grad(self, alignment, g=None, want_loglike=True):
         """(logLike (C,), d(sum g logL)/dt (R,), d(sum g logL)/dS~ (A, A) FP64)."""
         lib = _lib.load()
@@ -290,6 +336,16 @@ def Counts(alignment, tree: Tree, model, maxChunkSize: int = 128, f81_fast_flag:
     del maxChunkSize
     return get_plan(tree, model, _device_of(alignment)).run(
         alignment, loglike=False, counts=True, f81=f81_fast_flag, branch_mask=branch_mask)['counts']
+
+
+def BranchCounts(alignment, tree: Tree, model, maxChunkSize: int = 128, f81_fast_flag: bool = False,
+                 branch_mask=None):
+    """(R, A, A, C) per-branch dwell times and substitution counts, branch 0
+    zeros; subby/jax/__init__.py:450 (unmasked there; ``branch_mask`` as in
+    the oracle's BranchCounts, subby/oracle/oracle.py:1517)."""
+    del maxChunkSize
+    return get_plan(tree, model, _device_of(alignment)).branch_counts(
+        alignment, f81=f81_fast_flag, branch_mask=branch_mask)
 
 
 def RootProb(alignment, tree: Tree, model, maxChunkSize: int = 128):

@@ -22,6 +22,7 @@ enum : int {
   kModeF81 = 8,          // F81 closed form instead of the eigenbasis path
   kModeBT64 = 16,        // FP64 back-transform
   kModeGrad = 32,        // gradient accumulation instead of counts output
+  kModeBranch = 64,      // per-branch counts (R, A, A, C) instead of their sum
 };
 
 enum : int { kMaskNone = 0, kMaskAuto = 1, kMaskGiven = 2 };

@@ -113,7 +113,9 @@ struct N4 {
 //   stab[2] J    R x 16 (eigen) or F81 R x 4
 //   stab[3] K    R x 5 x 20 (eigen: K_n[code][k][l] = J_n[k][l] Ut[code][l], rows padded)
 //   stab[4] LV   5 x 4 (observation rows), followed by piL[5] (pi . L(code))
-template <bool F81, int MASK>
+// BR: per-branch counts (R, 4, 4, C) written branch by branch instead of
+// the sum over branches.
+template <bool F81, int MASK, bool BR>
 __global__ void __launch_bounds__(256, 1) k_tree4(const KParams P) {
   extern __shared__ __align__(16) float sm[];
   for (int t = 0; t < P.ntab; ++t) {
@@ -308,10 +310,81 @@ __global__ void __launch_bounds__(256, 1) k_tree4(const KParams P) {
     for (int k = 0; k < 4; ++k) acc[k] = hacc;
 
     // branch above node n; for leaves `code` >= 0 selects the table rows
+    // per-branch counts of branch n (BR): 16 values from the rows I_i
+    auto put_branch = [&](int n, const F4 (&I)[4]) {
+      float *o = P.counts + (size_t)n * 16 * C + col;
+      const float r[4][4] = {{I[0].a.x, I[0].a.y, I[0].b.x, I[0].b.y}, {I[1].a.x, I[1].a.y, I[1].b.x, I[1].b.y},
+                             {I[2].a.x, I[2].a.y, I[2].b.x, I[2].b.y}, {I[3].a.x, I[3].a.y, I[3].b.x, I[3].b.y}};
+      if (valid)
+#pragma unroll
+        for (int i2 = 0; i2 < 4; ++i2)
+#pragma unroll
+          for (int j = 0; j < 4; ++j) o[(size_t)(i2 * 4 + j) * C] = r[i2][j];
+    };
     auto branch = [&](int n, const F4 &D, const F4 &U, int code, int eDU, int active) {
       float s = invP * __int_as_float((max(-127, min(127, eDU - eRoot)) + 127) << 23);
       if (MASK != kMaskNone) s = active ? s : 0.f;
       const F4 Ds = scale4(D, s);
+      if constexpr (BR) {
+        F4 I[4];
+        if constexpr (F81) {
+          // I_ij = (alpha Ds_i + beta pi_i sum(Ds)) U_j + (beta Ds_i + gamma pi_i sum(Ds)) pi.U,
+          // dwell I_ii, substitutions mu pi_j I_ij (subby/oracle/oracle.py:1259-1331)
+          const float4 abg = *reinterpret_cast<const float4 *>(TB + n * 4);
+          const float piU = (code >= 0) ? piL[code] : dot4(piv, U);
+          const float dsum = sum4(Ds);
+          const float dk[4] = {Ds.a.x, Ds.a.y, Ds.b.x, Ds.b.y}, pk[4] = {piv.a.x, piv.a.y, piv.b.x, piv.b.y};
+#pragma unroll
+          for (int i2 = 0; i2 < 4; ++i2) {
+            const float cu = fmaf(abg.x, dk[i2], abg.y * pk[i2] * dsum);
+            const float c1 = fmaf(abg.y, dk[i2], abg.z * pk[i2] * dsum) * piU;
+            F4 row = fma4(cu, U, F4{make_float2(c1, c1), make_float2(c1, c1)});
+            // substitutions: mu pi_j I_ij off the diagonal
+            F4 f = scale4(piv, mu81);
+            float *fe = i2 < 2 ? (i2 == 0 ? &f.a.x : &f.a.y) : (i2 == 2 ? &f.b.x : &f.b.y);
+            *fe = 1.f;
+            I[i2] = mul4(row, f);
+          }
+        } else {
+          // eigenbasis C_kl = dt_k (J o U~)_l (leaves: K rows), then V C V^T and S
+          F4 dt = scale4(ld4s(Vd), Ds.a.x);
+          dt = fma4(Ds.a.y, ld4s(Vd + 4), dt);
+          dt = fma4(Ds.b.x, ld4s(Vd + 8), dt);
+          dt = fma4(Ds.b.y, ld4s(Vd + 12), dt);
+          const float dk[4] = {dt.a.x, dt.a.y, dt.b.x, dt.b.y};
+          F4 Cb[4];
+          if (code >= 0) {
+            const float *K = KT + (n * 5 + code) * 20;
+#pragma unroll
+            for (int k = 0; k < 4; ++k) Cb[k] = scale4(ld4s(K + 4 * k), dk[k]);
+          } else {
+            const F4 ut = matvec4(Vu, U);
+            const float *Jn = TB + n * 16;
+#pragma unroll
+            for (int k = 0; k < 4; ++k) Cb[k] = scale4(mul4(ld4s(Jn + 4 * k), ut), dk[k]);
+          }
+          // T_k = C_k V^T (row k: T[k][j] = sum_l C[k][l] V[j][l]); VCV_i = sum_k V[i][k] T_k
+          F4 T[4];
+#pragma unroll
+          for (int k = 0; k < 4; ++k)
+            T[k] = F4{make_float2(dot4(Cb[k], ld4s(V32)), dot4(Cb[k], ld4s(V32 + 4))),
+                      make_float2(dot4(Cb[k], ld4s(V32 + 8)), dot4(Cb[k], ld4s(V32 + 12)))};
+#pragma unroll
+          for (int i2 = 0; i2 < 4; ++i2) {
+            const F4 vi = ld4s(V32 + 4 * i2);
+            F4 row = scale4(T[0], vi.a.x);
+            row = fma4(vi.a.y, T[1], row);
+            row = fma4(vi.b.x, T[2], row);
+            row = fma4(vi.b.y, T[3], row);
+            F4 f = ld4s(S32 + 4 * i2);
+            float *fe = i2 < 2 ? (i2 == 0 ? &f.a.x : &f.a.y) : (i2 == 2 ? &f.b.x : &f.b.y);
+            *fe = 1.f;
+            I[i2] = mul4(row, f);
+          }
+        }
+        put_branch(n, I);
+        return;
+      }
       if constexpr (F81) {
         const float4 abg = *reinterpret_cast<const float4 *>(TB + n * 4);
         const float piU = (code >= 0) ? piL[code] : dot4(piv, U);
@@ -423,7 +496,7 @@ __global__ void __launch_bounds__(256, 1) k_tree4(const KParams P) {
       for (int q = 0; q < 7; ++q) tk[q] = tn[q];
     }
     // ------------------------------------------------------------ epilogue
-    if (!valid) continue;
+    if (BR || !valid) continue;
     float *out = P.counts + col;
     if constexpr (F81) {
       float pi_[4] = {piv.a.x, piv.a.y, piv.b.x, piv.b.y};
@@ -495,26 +568,32 @@ __global__ void __launch_bounds__(256, 1) k_tree4(const KParams P) {
                  : "memory");
 }
 
-template <bool F, int M>
+template <bool F, int M, bool B>
 int t4launch(const KParams &p, int grid, int block, size_t smem, cudaStream_t s) {
-  cudaError_t e = cudaFuncSetAttribute(k_tree4<F, M>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaError_t e = cudaFuncSetAttribute(k_tree4<F, M, B>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return (int)e;
-  k_tree4<F, M><<<grid, block, smem, s>>>(p);
+  k_tree4<F, M, B><<<grid, block, smem, s>>>(p);
   return (int)cudaGetLastError();
+}
+
+template <bool B>
+int t4launch_m(const KParams &p, bool f81, int mask_mode, int grid, int block, size_t smem, cudaStream_t s) {
+  if (f81) {
+    if (mask_mode == kMaskAuto) return t4launch<true, kMaskAuto, B>(p, grid, block, smem, s);
+    if (mask_mode == kMaskGiven) return t4launch<true, kMaskGiven, B>(p, grid, block, smem, s);
+    return t4launch<true, kMaskNone, B>(p, grid, block, smem, s);
+  }
+  if (mask_mode == kMaskAuto) return t4launch<false, kMaskAuto, B>(p, grid, block, smem, s);
+  if (mask_mode == kMaskGiven) return t4launch<false, kMaskGiven, B>(p, grid, block, smem, s);
+  return t4launch<false, kMaskNone, B>(p, grid, block, smem, s);
 }
 
 }  // namespace
 
 int launch_tree4(const KParams &p, bool f81, int mask_mode, int grid, int block, size_t smem,
                  cudaStream_t s) {
-  if (f81) {
-    if (mask_mode == kMaskAuto) return t4launch<true, kMaskAuto>(p, grid, block, smem, s);
-    if (mask_mode == kMaskGiven) return t4launch<true, kMaskGiven>(p, grid, block, smem, s);
-    return t4launch<true, kMaskNone>(p, grid, block, smem, s);
-  }
-  if (mask_mode == kMaskAuto) return t4launch<false, kMaskAuto>(p, grid, block, smem, s);
-  if (mask_mode == kMaskGiven) return t4launch<false, kMaskGiven>(p, grid, block, smem, s);
-  return t4launch<false, kMaskNone>(p, grid, block, smem, s);
+  return (p.mode & kModeBranch) ? t4launch_m<true>(p, f81, mask_mode, grid, block, smem, s)
+                                : t4launch_m<false>(p, f81, mask_mode, grid, block, smem, s);
 }
 
 }  // namespace subby

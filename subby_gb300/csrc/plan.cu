@@ -984,6 +984,13 @@ int ensure_pipeline(subby_plan *P, int nev) {
 int run_common(subby_plan *P, const int32_t *d_aln, int C, float *d_logL, float *d_counts,
                float *d_root, int mode, int mask_mode, const uint8_t *d_mask, const float *d_g,
                double *d_gt, double *d_gC, int *grid_out, cudaStream_t stream) {
+  if (mode & kModeBranch) {
+    // per-branch counts: the A = 4 tree-program kernel
+    Launch L4;
+    if (P->A != 4 || plan_tree4(P, mode, C, L4) != 0)
+      return fail(SUBBY_ERR_UNSUPPORTED, "per-branch counts are implemented for A = 4 (tree program within "
+                                         "the on-chip budget)");
+  }
   if (big_supported(P->A) && !(mode & kModeGrad) && g_kernel_sel != 1)
     return run_big(P, d_aln, C, d_logL, d_counts, d_root, mode, mask_mode, d_mask, stream);
   Launch L;
@@ -1163,6 +1170,60 @@ int subby_plan_run(subby_plan *P, const int32_t *aln, int C, float *logL, float 
       return fail(SUBBY_ERR_TIMEOUT, "a bounded device wait gave up (tensor-core walk)");
     }
   }
+  if (dev != P->device) cudaSetDevice(dev);
+  return SUBBY_OK;
+}
+
+int subby_plan_branch_counts(subby_plan *P, const int32_t *aln, int C, float *branchCounts, int counts_kind,
+                             int mask_mode, const uint8_t *mask, int flags, void *stream_) {
+  g_last_error.clear();
+  g_launches = 0;
+  if (!P || !aln || !branchCounts) return fail(SUBBY_ERR_ARG, "null argument");
+  if (C < 0) return fail(SUBBY_ERR_ARG, "negative column count");
+  if (mask_mode < 0 || mask_mode > 2) return fail(SUBBY_ERR_ARG, "bad mask_mode");
+  if (mask_mode == SUBBY_MASK_GIVEN && !mask) return fail(SUBBY_ERR_ARG, "mask required");
+  if (counts_kind != SUBBY_COUNTS_EIGEN && counts_kind != SUBBY_COUNTS_F81)
+    return fail(SUBBY_ERR_ARG, "bad counts_kind");
+  if (C == 0) return SUBBY_OK;
+  std::lock_guard<std::mutex> g(P->lock);
+  cudaStream_t stream = (cudaStream_t)stream_;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev != P->device) CU(cudaSetDevice(P->device));
+  const int A = P->A, R = P->R;
+  CU(cudaStreamWaitEvent(stream, P->ready, 0));
+  const int mode = kModeCounts | kModeBranch | (counts_kind == SUBBY_COUNTS_F81 ? kModeF81 : 0);
+  const size_t b_out = (size_t)R * A * A * C * sizeof(float);
+  int rc;
+  if (flags & SUBBY_DEVICE_PTRS) {
+    // branch 0 (the root) has no branch: zeros
+    CU(cudaMemsetAsync(branchCounts, 0, (size_t)A * A * C * sizeof(float), stream));
+    if (R > 1)
+      rc = run_common(P, aln, C, nullptr, branchCounts, nullptr, mode, mask_mode, mask, nullptr, nullptr, nullptr,
+                      nullptr, stream);
+    else
+      rc = 0;
+    if (dev != P->device) cudaSetDevice(dev);
+    return rc;
+  }
+  const size_t b_aln = (size_t)R * C * sizeof(int32_t);
+  const size_t b_mask = (mask_mode == SUBBY_MASK_GIVEN) ? (size_t)R * C : 0;
+  auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
+  if ((rc = P->grow(P->io, al(b_aln) + al(b_mask) + al(b_out), stream))) return rc;
+  char *base = (char *)P->io.p;
+  int32_t *d_aln = (int32_t *)base;
+  uint8_t *d_mask = b_mask ? (uint8_t *)(base + al(b_aln)) : nullptr;
+  float *d_out = (float *)(base + al(b_aln) + al(b_mask));
+  CU(cudaMemcpyAsync(d_aln, aln, b_aln, cudaMemcpyHostToDevice, stream));
+  if (b_mask) CU(cudaMemcpyAsync(d_mask, mask, b_mask, cudaMemcpyHostToDevice, stream));
+  CU(cudaMemsetAsync(d_out, 0, (size_t)A * A * C * sizeof(float), stream));
+  if (R > 1 && (rc = run_common(P, d_aln, C, nullptr, d_out, nullptr, mode, mask_mode, d_mask, nullptr, nullptr,
+                                nullptr, nullptr, stream))) {
+    cudaStreamSynchronize(stream);
+    return rc;
+  }
+  CU(cudaMemcpyAsync(branchCounts, d_out, b_out, cudaMemcpyDeviceToHost, stream));
+  CU(cudaStreamSynchronize(stream));
   if (dev != P->device) cudaSetDevice(dev);
   return SUBBY_OK;
 }

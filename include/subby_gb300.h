@@ -97,8 +97,8 @@ size_t subby_plan_device_bytes(const subby_plan *plan);
  * branch above node n; n = 0, the root, is zeros) the dwell times (diagonal)
  * and substitution counts (off-diagonal) per column.  counts_kind, mask_mode
  * and mask as for subby_plan_run (subby.jax.BranchCounts does not mask: pass
- * SUBBY_MASK_NONE for its semantics).  Implemented for A = 4; other
- * alphabets return SUBBY_ERR_UNSUPPORTED.  Replaces subby.jax BranchCounts
+ * SUBBY_MASK_NONE for its semantics).  Implemented for A = 4, 16, 20, 32
+ * and 64; other alphabets return SUBBY_ERR_UNSUPPORTED.  Replaces subby.jax BranchCounts
  * (subby/jax/__init__.py:450-540) and the oracle's BranchCounts
  * (subby/oracle/oracle.py:1517-1568).
  */

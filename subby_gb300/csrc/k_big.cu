@@ -827,11 +827,14 @@ __host__ __device__ constexpr int acc_vv_offset() {
 
 // TCB: back-transform V C V^T on the tensor cores (A = 64 eigen path of the
 // tensor-core Counts); otherwise on CUDA cores.
-template <int A, bool F81, bool TCB>
+// PB: per-branch counts — each work item is one (branch, column group) and
+// writes that branch's counts (R, A, A, C layout) instead of summing.
+template <int A, bool F81, bool TCB, bool PB = false>
 __global__ void __launch_bounds__(256, 1) k_acc(const KParams P, const float *__restrict__ stage_a,
                                                  const float *__restrict__ stage_b, int c_base, int c_count) {
   using Gm = AccGeo<A>;
   using Rg = AccRing<A>;
+  static_assert(!(PB && TCB), "per-branch counts use the CUDA-core back-transform");
   static_assert(!TCB || (A == 64 && !F81), "tensor-core back-transform is A = 64 eigen");
   constexpr int G = Gm::G;
   constexpr int S = Rg::S;
@@ -851,6 +854,8 @@ __global__ void __launch_bounds__(256, 1) k_acc(const KParams P, const float *__
   const int C = P.C;
   const int nbr = P.R - 1;
   const int ngroups = (c_count + G - 1) / G;
+  const int nitems = PB ? ngroups * nbr : ngroups;
+  float *cbase = P.counts;   // PB: the current branch's slab
   // V, S (eigen path) and pi, copied once per CTA behind the F81 scalars
   float *Vs = sm + Rg::SCAL + 2 * G, *Ss = Vs + A * A, *pis = Ss + A * A;
   if (!F81)
@@ -863,7 +868,7 @@ __global__ void __launch_bounds__(256, 1) k_acc(const KParams P, const float *__
   // stores when the rows are 16-byte aligned and all 8 columns exist
   const bool vec_out = (C & 3) == 0 && (c_base & 3) == 0;
   auto store8 = [&](size_t r, const float (&v)[8], int col0, int ncols) {
-    float *o = P.counts + r * C + col0;
+    float *o = cbase + r * C + col0;
     if (vec_out && ncols >= 8) {
       *reinterpret_cast<float4 *>(o) = make_float4(v[0], v[1], v[2], v[3]);
       *reinterpret_cast<float4 *>(o + 4) = make_float4(v[4], v[5], v[6], v[7]);
@@ -918,7 +923,10 @@ __global__ void __launch_bounds__(256, 1) k_acc(const KParams P, const float *__
   uint32_t nT = 0;  // completed phases of mbT
   uint32_t it = 0;  // ring position of the next branch to consume (all groups)
 
-  for (int gi = blockIdx.x; gi < ngroups; gi += gridDim.x) {
+  for (int wi = blockIdx.x; wi < nitems; wi += gridDim.x) {
+    const int gi = PB ? wi % ngroups : wi;
+    const int n_lo = PB ? wi / ngroups : 0, n_hi = PB ? n_lo + 1 : nbr;   // branches of this item
+    if constexpr (PB) cbase = P.counts + (size_t)(n_lo + 1) * A * A * C;
     const int g0 = gi * G;                       // first column (chunk-relative)
     const int gcols = min(G, c_count - g0);
     // accumulators: ac2[a][p][q] = (C[k0+a][l0+2p], C[k0+a][l0+2p+1]) of column q
@@ -972,12 +980,12 @@ __global__ void __launch_bounds__(256, 1) k_acc(const KParams P, const float *__
                    : "memory");
     };
     if (t == 0)
-      for (int n = 0; n < S - 1 && n < nbr; ++n) load(n, it + n);
+      for (int n = n_lo; n < n_lo + S - 1 && n < n_hi; ++n) load(n, it + (n - n_lo));
     float *scal = sm + Rg::SCAL;  // F81: piU, Dsum per column
-    for (int n = 0; n < nbr; ++n, ++it) {
+    for (int n = n_lo; n < n_hi; ++n, ++it) {
       // every thread is done with the stage of branch n - 1: refill it
       __syncthreads();
-      if (t == 0 && n + S - 1 < nbr) load(n + S - 1, it + S - 1);
+      if (t == 0 && n + S - 1 < n_hi) load(n + S - 1, it + S - 1);
       const int st = (int)(it % S);
       const float *cur = sm + st * Rg::STAGE;
       if (!mbar_wait((uint32_t)__cvta_generic_to_shared(&mbar[st]), (it / S) & 1)) s_err = 1;
@@ -1386,22 +1394,26 @@ int walk_launch(const KParams &p, int mode, bool tc, float *sa, float *sb, int c
   return walk_launch_tc<A, false>(p, mode, sa, sb, c_base, c_count, grid, s);
 }
 
-template <int A, bool F81, bool TCB>
+template <int A, bool F81, bool TCB, bool PB = false>
 int acc_launch1(const KParams &p, const float *sa, const float *sb, int c_base, int c_count, int grid,
                 cudaStream_t s) {
   using Gm = AccGeo<A>;
   const size_t smem = TCB ? (size_t)acc_vv_offset<A>() * sizeof(float) + 49152
                           : (size_t)(AccRing<A>::SCAL + 2 * Gm::G + 2 * A * A + A + 2 * Gm::G * A + Gm::G) *
                                 sizeof(float);
-  cudaError_t e = cudaFuncSetAttribute(k_acc<A, F81, TCB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaError_t e =
+      cudaFuncSetAttribute(k_acc<A, F81, TCB, PB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return (int)e;
-  k_acc<A, F81, TCB><<<grid, 256, smem, s>>>(p, sa, sb, c_base, c_count);
+  k_acc<A, F81, TCB, PB><<<grid, 256, smem, s>>>(p, sa, sb, c_base, c_count);
   return (int)cudaGetLastError();
 }
 
 template <int A>
 int acc_launch(const KParams &p, bool f81, bool tc, const float *sa, const float *sb, int c_base, int c_count,
                int grid, cudaStream_t s) {
+  if (p.mode & kModeBranch)
+    return f81 ? acc_launch1<A, true, false, true>(p, sa, sb, c_base, c_count, grid, s)
+               : acc_launch1<A, false, false, true>(p, sa, sb, c_base, c_count, grid, s);
   if (f81) return acc_launch1<A, true, false>(p, sa, sb, c_base, c_count, grid, s);
   if constexpr (A == 64) {
     if (tc) return acc_launch1<A, false, true>(p, sa, sb, c_base, c_count, grid, s);

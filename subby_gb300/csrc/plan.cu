@@ -918,7 +918,7 @@ int run_big(subby_plan *P, const int32_t *d_aln, int C, float *d_logL, float *d_
   const size_t slot_ints = (size_t)walk_grid * k.nslots * tile;
   const size_t stage_floats = counts ? (size_t)(R - 1) * chunk * A : 0;
   // A = 64 F81 counts on the tensor cores: per-branch scalars staged too
-  const bool f81tc = counts && (mode & kModeF81) && tc;
+  const bool f81tc = counts && (mode & kModeF81) && tc && !(mode & kModeBranch);
   const size_t stage_c_floats = f81tc ? (size_t)(R - 1) * chunk * 2 : 0;
   auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
   int rc;
@@ -949,7 +949,8 @@ int run_big(subby_plan *P, const int32_t *d_aln, int C, float *d_logL, float *d_
     g_launches += 1;
     if (counts) {
       const int G = big_acc_group(A);
-      const int agrid = std::max(1, std::min((cc + G - 1) / G, P->nsm));
+      const long long items = (long long)(cc + G - 1) / G * ((mode & kModeBranch) ? (R - 1) : 1);
+      const int agrid = (int)std::max<long long>(1, std::min<long long>(items, P->nsm));
       lr = f81tc ? launch_acc_f81_tc(k, sa, sb, k.stage_c, c0, cc, agrid, stream)
                  : launch_acc(k, A, (mode & kModeF81) != 0, tc, sa, sb, c0, cc, agrid, stream);
       if (lr != 0) return fail(SUBBY_ERR_CUDA, std::string("accumulate launch failed: ") + cudaGetErrorString((cudaError_t)lr));
@@ -985,11 +986,13 @@ int run_common(subby_plan *P, const int32_t *d_aln, int C, float *d_logL, float 
                float *d_root, int mode, int mask_mode, const uint8_t *d_mask, const float *d_g,
                double *d_gt, double *d_gC, int *grid_out, cudaStream_t stream) {
   if (mode & kModeBranch) {
-    // per-branch counts: the A = 4 tree-program kernel
+    // per-branch counts: the A = 4 tree-program kernel, or the large-alphabet
+    // walk with the per-branch accumulation
     Launch L4;
-    if (P->A != 4 || plan_tree4(P, mode, C, L4) != 0)
+    const bool ok4 = P->A == 4 && plan_tree4(P, mode, C, L4) == 0;
+    if (!ok4 && !(big_supported(P->A) && g_kernel_sel != 1))
       return fail(SUBBY_ERR_UNSUPPORTED, "per-branch counts are implemented for A = 4 (tree program within "
-                                         "the on-chip budget)");
+                                         "the on-chip budget) and A = 16, 20, 32, 64");
   }
   if (big_supported(P->A) && !(mode & kModeGrad) && g_kernel_sel != 1)
     return run_big(P, d_aln, C, d_logL, d_counts, d_root, mode, mask_mode, d_mask, stream);

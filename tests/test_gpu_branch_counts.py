@@ -91,9 +91,26 @@ def test_given_mask_device_pointers_and_api():
     plan.close()
 
 
+@pytest.mark.parametrize("A,leaves,C", [(16, 9, 45), (20, 7, 33), (32, 5, 17), (64, 6, 21)])
+def test_large_alphabets_vs_oracle(A, leaves, C):
+    """Walk staging + the per-branch accumulation kernel (A >= 16), eigen
+    and F81 counts, unmasked and masked; tensor-core walk at A = 64."""
+    rng = np.random.default_rng(30 + A)
+    m = models.near_degenerate_reversible(A, rng)[0]
+    tree = synth.random_tree(leaves, 0.1, rng)
+    aln = synth.simulated_alignment(tree, m, C, 0.1, rng)
+    ot = oracle.Tree(tree.parentIndex, tree.distanceToParent)
+    plan = sg.Plan(tree, m)
+    for f81, bm in ((False, None), (False, "auto"), (True, None)):
+        got = plan.branch_counts(aln, f81=f81, branch_mask=bm)
+        _assert_bc(got, oracle.BranchCounts(aln, ot, m._asdict(), f81_fast=f81, branch_mask=bm),
+                   f"A={A} f81={f81} mask={bm}")
+    plan.close()
+
+
 def test_unsupported_alphabet_raises():
     rng = np.random.default_rng(2)
-    m = models.random_reversible(16, rng)[0]
+    m = models.random_reversible(6, rng)[0]
     tree = synth.random_tree(6, 0.1, rng)
     aln = synth.simulated_alignment(tree, m, 8, 0.1, rng)
     plan = sg.Plan(tree, m)

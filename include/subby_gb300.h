@@ -104,6 +104,11 @@ size_t subby_plan_device_bytes(const subby_plan *plan);
  */
 int subby_plan_branch_counts(subby_plan *plan, const int32_t *alignment, int C, float *branchCounts,
                              int counts_kind, int mask_mode, const uint8_t *mask, int flags, void *stream);
+/* Wait for the plan's enqueued work and report SUBBY_ERR_TIMEOUT if a
+ * bounded device wait (tensor-core kernels) gave up since the last check
+ * (device-pointer runs return before their kernels finish, so they report
+ * it here); clears the record.  No counterpart in the reference. */
+int subby_plan_status(subby_plan *plan);
 /* Release the plan's workspace (staging, scratch, host-call buffers) in
  * stream order after its last enqueued kernel; the tables stay.  The next
  * run allocates again (from the library pool).  For servers that keep many

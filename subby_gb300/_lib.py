@@ -20,7 +20,8 @@ COUNTS_EIGEN, COUNTS_F81 = 0, 1
 # Exported symbols, as declared in include/subby_gb300.h.
 EXPORTS = (
     "subby_version", "subby_strerror", "subby_last_error", "subby_plan_create",
-    "subby_plan_destroy", "subby_plan_device_bytes", "subby_plan_trim", "subby_plan_branch_counts", "subby_plan_run", "subby_plan_grad",
+    "subby_plan_destroy", "subby_plan_device_bytes", "subby_plan_trim", "subby_plan_branch_counts",
+    "subby_plan_status", "subby_plan_run", "subby_plan_grad",
     "subby_loglike", "subby_counts", "subby_rootprob", "subby_last_launch_count",
     "subby_debug_set_kernel", "subby_counts_noalloc",
 )
@@ -62,6 +63,8 @@ def _declare(lib):
     lib.subby_plan_device_bytes.argtypes = [_p]
     lib.subby_plan_trim.restype = ct.c_int
     lib.subby_plan_trim.argtypes = [_p]
+    lib.subby_plan_status.restype = ct.c_int
+    lib.subby_plan_status.argtypes = [_p]
     lib.subby_plan_branch_counts.restype = ct.c_int
     lib.subby_plan_branch_counts.argtypes = [_p, _p, ct.c_int, _p, ct.c_int, ct.c_int, _p, ct.c_int, _p]
     lib.subby_plan_run.restype = ct.c_int

@@ -238,6 +238,12 @@ class Plan:
     def device_bytes(self) -> int:
         return int(_lib.load().subby_plan_device_bytes(self._handle))
 
+    def status(self):
+        """Raise SubbyError if a bounded device wait of this plan's kernels
+        gave up since the last check (waits for the plan's enqueued work)."""
+        with self._lock:
+            _lib.check(_lib.load().subby_plan_status(self._handle), "subby_plan_status")
+
     def trim(self):
         """Release the workspace (kept tables); the next run allocates again."""
         with self._lock:

@@ -635,6 +635,29 @@ int subby_plan_destroy(subby_plan *P) {
   return SUBBY_OK;
 }
 
+int subby_plan_status(subby_plan *P) {
+  if (!P) return fail(SUBBY_ERR_ARG, "null plan");
+  std::lock_guard<std::mutex> g(P->lock);
+  if (!P->d_err) return SUBBY_OK;
+  int cur = 0;
+  cudaGetDevice(&cur);
+  if (cur != P->device) cudaSetDevice(P->device);
+  int dev_err = 0;
+  cudaError_t e = cudaSuccess;
+  if (P->used) e = cudaStreamWaitEvent(P->s_prep, P->last_use, 0);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&dev_err, P->d_err, sizeof(int), cudaMemcpyDeviceToHost, P->s_prep);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(P->s_prep);
+  if (e == cudaSuccess && dev_err) {
+    cudaMemsetAsync(P->d_err, 0, sizeof(int), P->s_prep);
+    e = cudaStreamSynchronize(P->s_prep);
+  }
+  if (cur != P->device) cudaSetDevice(cur);
+  if (e != cudaSuccess) return cuda_fail(e, "plan status");
+  if (dev_err) return fail(SUBBY_ERR_TIMEOUT, "a bounded device wait gave up in " + std::to_string(dev_err) +
+                                                 " CTA(s) since the last status check");
+  return SUBBY_OK;
+}
+
 int subby_plan_trim(subby_plan *P) {
   if (!P) return fail(SUBBY_ERR_ARG, "null plan");
   std::lock_guard<std::mutex> g(P->lock);

@@ -61,6 +61,7 @@ class Job:
     start: float = -1.0
     finish: float = -1.0
     result: dict = field(default_factory=dict)
+    error: str = ""                # set when the device reported a failed wait
 
     @property
     def latency(self):
@@ -338,9 +339,14 @@ class Server:
                 job.result = {k: v.numpy() for k, v in bufs[3].items()}
                 job._pinned = bufs[4]
                 job._give_back = self._give_back
-                # the plan stays cached; its workspace goes back to the pool
+                # the plan stays cached; its workspace goes back to the pool.
+                # A bounded device wait that gave up marks the job failed.
                 plan = self.plans.get(self._key(job))
                 if plan is not None:
+                    try:
+                        plan.status()
+                    except Exception as exc:  # noqa: BLE001
+                        job.error = str(exc)
                     plan.trim()
                 self.free_slots.append(slot)
                 self.used_bytes -= nbytes

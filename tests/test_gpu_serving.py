@@ -35,6 +35,7 @@ def test_results_identical_alone_and_in_the_mix():
     assert len(done) == len(jobs)
     assert len({j.id for j in done}) == len(jobs)
     for j in done:
+        assert not j.error, f"job {j.id}: {j.error}"
         plan = sg.Plan(j.tree, j.model)
         alone = plan.run(j.alignment, loglike=True, counts=True, f81=j.f81)
         plan.close()

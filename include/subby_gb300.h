@@ -193,7 +193,9 @@ int subby_counts_noalloc(const int32_t *alignment, const int32_t *parent_index,
  * thread-per-column kernel (A <= 8) / warp-per-column kernel (larger A), 2
  * tree program with shared-memory slots (A <= 8) / FP32 CUDA-core tree walk
  * (larger A), 3 tree program with global-memory slots, 4 generic tree
- * program with tensor-memory slots.  No reference counterpart. */
+ * program with tensor-memory slots, 5 (A = 64) tensor-core walk with the
+ * CUDA-core back-transform, 6 (A = 64) CUDA-core walk with the tensor-core
+ * back-transform.  No reference counterpart. */
 int subby_debug_set_kernel(int which);
 
 /* Number of kernel launches the most recent subby_plan_run /

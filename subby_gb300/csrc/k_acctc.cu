@@ -226,7 +226,8 @@ __global__ void __launch_bounds__(256, 1) k_acc_f81_tc(const KParams P, const fl
         uint32_t v[32];
         const uint32_t ta = tmem + ((uint32_t)(32 * sub) << 16) + 128u * p + 64u * cg + (uint32_t)j0;
         asm volatile("tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,"
-                     "%15,%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+                     "%15,%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];\n"
+                 "tcgen05.wait::ld.sync.aligned;"
                      : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]),
                        "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]),
                        "=r"(v[14]), "=r"(v[15]), "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]), "=r"(v[20]),
@@ -234,7 +235,6 @@ __global__ void __launch_bounds__(256, 1) k_acc_f81_tc(const KParams P, const fl
                        "=r"(v[28]), "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
                      : "r"(ta)
                      : "memory");
-        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
         float *dst = Gs + ((size_t)(2 * p + cg) * kA + i) * kA + j0;
 #pragma unroll
         for (int q = 0; q < 8; ++q)

@@ -189,7 +189,8 @@ struct Walk {
     uint32_t r[32];
     const uint32_t ta = tcs.tmem + ((uint32_t)(32 * (warp & 3)) << 16) + col;
     asm volatile("tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
-                 "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+                 "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];\n"
+                 "tcgen05.wait::ld.sync.aligned;"
                  : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
                    "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]),
                    "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]),
@@ -197,7 +198,6 @@ struct Walk {
                    "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
                  : "r"(ta)
                  : "memory");
-    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
     for (int i = 0; i < 32; ++i) y.v[i] = __uint_as_float(r[i]);
   }
@@ -1145,7 +1145,8 @@ __global__ void __launch_bounds__(256, 1) k_acc(const KParams P, const float *__
       };
       auto ld32 = [&](uint32_t col, uint32_t (&r)[32]) {
         asm volatile("tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,"
-                     "%15,%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+                     "%15,%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];\n"
+                 "tcgen05.wait::ld.sync.aligned;"
                      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
                        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
                        "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]),
@@ -1153,7 +1154,6 @@ __global__ void __launch_bounds__(256, 1) k_acc(const KParams P, const float *__
                        "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
                      : "r"(tm + ((uint32_t)(32 * sub) << 16) + col)
                      : "memory");
-        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
       };
       auto split3 = [](float x0, float x1, uint32_t &t1, uint32_t &t2, uint32_t &t3) {
         const __nv_bfloat162 b1 = __floats2bfloat162_rn(x0, x1);

@@ -311,7 +311,7 @@ const char *subby_strerror(int s) {
 const char *subby_last_error(void) { return g_last_error.c_str(); }
 
 int subby_debug_set_kernel(int which) {
-  if (which < 0 || which > 4) return fail(SUBBY_ERR_ARG, "kernel selector must be 0..4");
+  if (which < 0 || which > 6) return fail(SUBBY_ERR_ARG, "kernel selector must be 0..6");
   g_kernel_sel = which;
   return SUBBY_OK;
 }
@@ -921,7 +921,10 @@ int run_big(subby_plan *P, const int32_t *d_aln, int C, float *d_logL, float *d_
   k.nslots = std::max(P->prog_slots, 1);
   k.tab16 = P->d_tab16;
   k.err = P->d_err;
-  const bool tc = (A == 64) && P->d_tab16 && g_kernel_sel == 0;
+  // 5: tensor-core walk with the CUDA-core back-transform; 6: CUDA-core walk
+  // with the tensor-core back-transform (test hooks)
+  const bool tc = (A == 64) && P->d_tab16 && (g_kernel_sel == 0 || g_kernel_sel == 5);
+  const bool tcb = (A == 64) && P->d_tab16 && (g_kernel_sel == 0 || g_kernel_sel == 6);
   const int tile = big_tile();
   const int H = (A + 31) / 32;
   const bool counts = (mode & kModeCounts) != 0 && R > 1;
@@ -975,7 +978,7 @@ int run_big(subby_plan *P, const int32_t *d_aln, int C, float *d_logL, float *d_
       const long long items = (long long)(cc + G - 1) / G * ((mode & kModeBranch) ? (R - 1) : 1);
       const int agrid = (int)std::max<long long>(1, std::min<long long>(items, P->nsm));
       lr = f81tc ? launch_acc_f81_tc(k, sa, sb, k.stage_c, c0, cc, agrid, stream)
-                 : launch_acc(k, A, (mode & kModeF81) != 0, tc, sa, sb, c0, cc, agrid, stream);
+                 : launch_acc(k, A, (mode & kModeF81) != 0, tcb, sa, sb, c0, cc, agrid, stream);
       if (lr != 0) return fail(SUBBY_ERR_CUDA, std::string("accumulate launch failed: ") + cudaGetErrorString((cudaError_t)lr));
       g_launches += 1;
     }

@@ -702,20 +702,14 @@ __global__ void __launch_bounds__(128 * Geo<A>::H, 1) k_walk(const KParams P, fl
         eO = eD + wk.rescale(O);
       }
 #pragma unroll
-      // both children's outside vectors first: O and the siblings' vectors
-      // die here, which keeps the per-side work within the register budget
-      BV<A> Dcs[2];
-#pragma unroll
-      for (int q = 0; q < S; ++q) {
-        Dcs[0].v[q] = O.v[q] * nr.cc.v[q];
-        Dcs[1].v[q] = O.v[q] * nl.cc.v[q];
-      }
 #pragma unroll
       for (int side = 0; side < 2; ++side) {
         const BN<A> &me = side ? nr : nl;
         const BN<A> &sib = side ? nl : nr;
         const int4 sc = side ? s2 : s1;
-        const BV<A> &Dc = Dcs[side];
+        BV<A> Dc;
+#pragma unroll
+        for (int q = 0; q < S; ++q) Dc.v[q] = O.v[q] * sib.cc.v[q];
         const int eDc = eO + sib.e;
         const int stc = me.init | (stp & me.hh);
         const int actc = act_of(sc.x, stc, stp);

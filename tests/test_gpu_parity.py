@@ -269,3 +269,21 @@ def test_fp32_vs_fp64_back_transform_both_within_tolerance():
     for bt in (True, False):
         r = plan.run(w['alignment'], loglike=False, counts=True, branch_mask=None, bt64=bt)
         assert_cols(r['counts'], ref, COUNTS_RTOL, f"counts bt64={bt}")
+
+
+def test_tensor_core_walk_repeatable_small_tree():
+    """A=64 reversible model, 6-leaf tree, 314 columns (three 128-column
+    tiles, the last one ragged): 30 runs of the tensor-core path give
+    bit-identical counts (a walk variant once produced intermittently wrong
+    tiles on this shape)."""
+    rng = np.random.default_rng(77)
+    m = models.random_reversible(64, rng)[0]
+    tree = sg.Tree(np.array([-1, 0, 1, 2, 2, 1, 5, 5, 7, 7, 0], dtype=np.int32),
+                   rng.exponential(0.1, 11))
+    aln = synth.simulated_alignment(tree, m, 314, 0.05, rng)
+    plan = sg.Plan(tree, m)
+    ref = plan.run(aln, loglike=True, counts=True)['counts']
+    assert np.isfinite(ref).all()
+    for _ in range(30):
+        np.testing.assert_array_equal(plan.run(aln, loglike=True, counts=True)['counts'], ref)
+    plan.close()

@@ -104,6 +104,19 @@ size_t subby_plan_device_bytes(const subby_plan *plan);
  */
 int subby_plan_branch_counts(subby_plan *plan, const int32_t *alignment, int C, float *branchCounts,
                              int counts_kind, int mask_mode, const uint8_t *mask, int flags, void *stream);
+/*
+ * Posteriors of the inside-outside tables.  node = -1: nodePost (R, A, C) is
+ * the posterior state distribution of every node (row 0, the root, equals
+ * RootProb) and branchPost (R, A, A, C) the joint posterior of (parent state
+ * i, child state j) on every branch (branch 0 zeros).  node = n >= 0: the
+ * same for node n only, nodePost (A, C) and branchPost (A, A, C) (n > 0 for
+ * branchPost).  Either output may be NULL.  Implemented for A = 4, 8, 16,
+ * 20, 32 and 64.  Replaces subby.jax InsideOutside.node_posterior /
+ * branch_posterior (subby/jax/__init__.py:868-1040) and the oracle's
+ * (subby/oracle/oracle.py:1755-1905).
+ */
+int subby_plan_posteriors(subby_plan *plan, const int32_t *alignment, int C, int node, float *nodePost,
+                          float *branchPost, int flags, void *stream);
 /* Wait for the plan's enqueued work and report SUBBY_ERR_TIMEOUT if a
  * bounded device wait (tensor-core kernels) gave up since the last check
  * (device-pointer runs return before their kernels finish, so they report

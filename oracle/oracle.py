@@ -419,6 +419,58 @@ def RootProb(alignment, tree, model):
     return (np.asarray(model['pi'])[None, :] * U[0] * scale[:, None]).T
 
 
+def _inside_outside(alignment, tree, model):
+    """U, D, scales and M with the root's outside vector set to pi / max(pi),
+    as InsideOutside.__init__ does (oracle.py:1631-1661)."""
+    M = compute_sub_matrices(model, tree.distanceToParent)
+    U, lnU, lnL = upward_pass(alignment, tree, M, model['pi'])
+    D, lnD = downward_pass(U, lnU, tree, M, model['pi'], alignment)
+    pi = np.asarray(model['pi'], dtype=np.float64)
+    mx = max(float(np.max(pi)), RESCALE_FLOOR)
+    D[0] = pi[None, :] / mx
+    lnD[0] = np.log(mx)
+    return M, U, lnU, lnL, D, lnD
+
+
+def _normalise(x, axes):
+    """Divide by the sum over `axes` where that sum is positive (oracle.py:1793-1795)."""
+    tot = np.sum(x, axis=axes, keepdims=True)
+    return np.where(tot > 0, x / np.where(tot > 0, tot, 1.0), x)
+
+
+def NodePosterior(alignment, tree, model, node=None):
+    """Posterior state distribution of node(s); InsideOutside.node_posterior,
+    oracle.py:1755-1831 (subby/jax/__init__.py:868-946).
+
+    Root: pi_a U_0a; node n > 0: (sum_a D_na M_n[a, j]) U_nj; times
+    exp(logNormU + logNormD - logLike), normalised over the states.
+    Returns (A, C) for one node, (R, A, C) for node=None."""
+    M, U, lnU, lnL, D, lnD = _inside_outside(alignment, tree, model)
+    scale = np.exp(lnU + lnD - lnL[None, :])                       # (R, C)
+    Dt = np.einsum('rca,raj->rcj', D, M)
+    Dt[0] = D[0]
+    post = _normalise(Dt * U * scale[:, :, None], -1)              # (R, C, A)
+    post = post.transpose(0, 2, 1)
+    return post if node is None else post[node]
+
+
+def BranchPosterior(alignment, tree, model, node=None):
+    """Joint posterior of (parent state i, child state j) on branch(es);
+    InsideOutside.branch_posterior, oracle.py:1833-1905
+    (subby/jax/__init__.py:948-1040): D_ni M_n[i, j] U_nj exp(logNormD +
+    logNormU - logLike), normalised over (i, j).  Returns (A, A, C) for one
+    node (> 0), (R, A, A, C) with branch 0 zero for node=None."""
+    M, U, lnU, lnL, D, lnD = _inside_outside(alignment, tree, model)
+    scale = np.exp(lnU + lnD - lnL[None, :])
+    joint = D[:, :, :, None] * M[:, None, :, :] * U[:, :, None, :] * scale[:, :, None, None]  # (R, C, A, A)
+    joint = _normalise(joint, (-2, -1))
+    joint = joint.transpose(0, 2, 3, 1)
+    if node is not None:
+        return joint[node]
+    joint[0] = 0.0
+    return joint
+
+
 def pipeline(alignment, tree, model, branch_mask=None, f81_fast=False):
     """Every intermediate of one Counts call, for fixture comparison."""
     M = compute_sub_matrices(model, tree.distanceToParent)

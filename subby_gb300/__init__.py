@@ -6,13 +6,13 @@ root posteriors.  Drop-in for the single-model entry points of ``subby.jax``.
 from .types import Tree, DiagModel, RateModel
 from .models import (hky85_diag, jukes_cantor_model, f81_model, diagonalize_rate_matrix,
                      reversible_rate_matrix, random_reversible)
-from .api import (LogLike, Counts, BranchCounts, RootProb, LogLikeCustomGrad, Plan, get_plan,
+from .api import (LogLike, Counts, BranchCounts, RootProb, LogLikeCustomGrad, InsideOutside, Plan, get_plan,
                   clear_plan_cache)
 from . import _lib
 
 __all__ = ["BranchCounts", "Tree", "DiagModel", "RateModel", "hky85_diag", "jukes_cantor_model", "f81_model",
            "diagonalize_rate_matrix", "reversible_rate_matrix", "random_reversible", "LogLike",
-           "Counts", "RootProb", "LogLikeCustomGrad", "Plan", "get_plan", "clear_plan_cache"]
+           "Counts", "RootProb", "LogLikeCustomGrad", "InsideOutside", "Plan", "get_plan", "clear_plan_cache"]
 
 __version__ = "0.1.0"
 

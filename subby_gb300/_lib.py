@@ -21,7 +21,7 @@ COUNTS_EIGEN, COUNTS_F81 = 0, 1
 EXPORTS = (
     "subby_version", "subby_strerror", "subby_last_error", "subby_plan_create",
     "subby_plan_destroy", "subby_plan_device_bytes", "subby_plan_trim", "subby_plan_branch_counts",
-    "subby_plan_status", "subby_plan_run", "subby_plan_grad",
+    "subby_plan_posteriors", "subby_plan_status", "subby_plan_run", "subby_plan_grad",
     "subby_loglike", "subby_counts", "subby_rootprob", "subby_last_launch_count",
     "subby_debug_set_kernel", "subby_counts_noalloc",
 )
@@ -67,6 +67,8 @@ def _declare(lib):
     lib.subby_plan_status.argtypes = [_p]
     lib.subby_plan_branch_counts.restype = ct.c_int
     lib.subby_plan_branch_counts.argtypes = [_p, _p, ct.c_int, _p, ct.c_int, ct.c_int, _p, ct.c_int, _p]
+    lib.subby_plan_posteriors.restype = ct.c_int
+    lib.subby_plan_posteriors.argtypes = [_p, _p, ct.c_int, ct.c_int, _p, _p, ct.c_int, _p]
     lib.subby_plan_run.restype = ct.c_int
     lib.subby_plan_run.argtypes = [_p, _p, ct.c_int, _p, _p, _p, ct.c_int, ct.c_int, _p, ct.c_int, _p]
     lib.subby_plan_grad.restype = ct.c_int

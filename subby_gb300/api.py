@@ -217,6 +217,56 @@ class Plan:
                 _ptr(hmask) if hmask is not None else None, 0, None), "subby_plan_branch_counts")
         return res
 
+    def posteriors(self, alignment, node=None, want_node=True, want_branch=False, stream=None):
+        """Inside-outside posteriors: ``{'node': ..., 'branch': ...}`` with
+        the node posteriors (R, A, C) (row 0: the root, = RootProb) and the
+        branch joint posteriors (R, A, A, C) [n, i, j, c] = P(parent of n = i,
+        n = j | column c) (branch 0 zeros); for ``node=n`` only that node's
+        (A, C) / (A, A, C).  Numpy in, numpy out; a CUDA tensor in, tensors on
+        its device out (enqueued on ``stream`` or the current stream)."""
+        if not (want_node or want_branch):
+            raise ValueError("request the node and/or the branch posteriors")
+        lib = _lib.load()
+        A, R = self.A, self.R
+        nd = -1 if node is None else int(node)
+        if nd < -1 or nd >= R:
+            raise IndexError(f"node {node} out of range for R={R}")
+        if want_branch and nd == 0:
+            raise ValueError("node 0 (the root) has no branch")
+        lead = (R,) if nd < 0 else ()
+        res = {}
+        if _is_torch(alignment) and alignment.is_cuda:
+            import torch
+            aln = alignment.to(torch.int32).contiguous()
+            if aln.dim() != 2 or aln.shape[0] != R:
+                raise ValueError(f"alignment must have shape (R={R}, C)")
+            C = int(aln.shape[1])
+            kw = dict(dtype=torch.float32, device=aln.device)
+            if want_node:
+                res['node'] = torch.empty(lead + (A, C), **kw)
+            if want_branch:
+                res['branch'] = torch.empty(lead + (A, A, C), **kw)
+            dp = lambda k: ct.c_void_p(res[k].data_ptr()) if k in res else None  # noqa: E731
+            st = (stream if stream is not None else torch.cuda.current_stream(aln.device)).cuda_stream
+            with self._lock, _device_ctx(aln.device):
+                _lib.check(lib.subby_plan_posteriors(
+                    self._handle, ct.c_void_p(aln.data_ptr()), C, nd, dp('node'), dp('branch'), _lib.DEVICE_PTRS,
+                    ct.c_void_p(st)), "subby_plan_posteriors")
+            return res
+        aln = _np(alignment, np.int32)
+        if aln.ndim != 2 or aln.shape[0] != R:
+            raise ValueError(f"alignment must have shape (R={R}, C)")
+        C = int(aln.shape[1])
+        if want_node:
+            res['node'] = np.empty(lead + (A, C), dtype=np.float32)
+        if want_branch:
+            res['branch'] = np.empty(lead + (A, A, C), dtype=np.float32)
+        hp = lambda k: _ptr(res[k]) if k in res else None  # noqa: E731
+        with self._lock, _device_ctx(self.device):
+            _lib.check(lib.subby_plan_posteriors(self._handle, _ptr(aln), C, nd, hp('node'), hp('branch'), 0, None),
+                       "subby_plan_posteriors")
+        return res
+
     def grad(self, alignment, g=None, want_loglike=True):
         """(logLike (C,), d(sum g logL)/dt (R,), d(sum g logL)/dS~ (A, A) FP64)."""
         lib = _lib.load()
@@ -374,3 +424,51 @@ def LogLikeCustomGrad(alignment, tree: Tree, model, maxChunkSize: int = 128, met
         raise ValueError("method must be 'eigen' or 'pade'")
     from .autograd import loglike_with_grad
     return loglike_with_grad(alignment, tree, model)
+
+
+class InsideOutside:
+    """Inside-outside queries on one alignment; subby/jax/__init__.py:681-1040.
+
+    The reference runs both passes once and keeps U and D for the queries;
+    here the (tree, model) plan stays resident and each query runs its fused
+    kernels (walk + accumulation or posterior kernel) over the alignment, so
+    nothing of size R x C x A is held between queries.  Model lists and grids
+    raise ``NotImplementedError`` (the reference raises for grids too).
+    """
+
+    def __init__(self, alignment, tree: Tree, model, maxChunkSize: int = 128):
+        del maxChunkSize
+        if isinstance(model, (list, tuple)) and not hasattr(model, '_fields'):
+            raise NotImplementedError("InsideOutside does not support model lists or grids here")
+        self._alignment = alignment
+        self._tree = tree
+        self._plan = get_plan(tree, model, _device_of(alignment))
+        self._logLike = None
+
+    @property
+    def log_likelihood(self):
+        """Per-column log-likelihoods (C,)."""
+        if self._logLike is None:
+            self._logLike = self._plan.run(self._alignment, loglike=True)['logLike']
+        return self._logLike
+
+    def counts(self, f81_fast_flag: bool = False, branch_mask="auto"):
+        """(A, A, C) dwell times and substitution counts (as ``Counts``)."""
+        return self._plan.run(self._alignment, loglike=False, counts=True, f81=f81_fast_flag,
+                              branch_mask=branch_mask)['counts']
+
+    def branch_counts(self, f81_fast_flag: bool = False):
+        """(R, A, A, C) per-branch counts, unmasked (as ``BranchCounts``)."""
+        return self._plan.branch_counts(self._alignment, f81=f81_fast_flag)
+
+    def node_posterior(self, node=None):
+        """Posterior state distribution: (A, C) for ``node``, (R, A, C) for
+        every node when ``node`` is None."""
+        return self._plan.posteriors(self._alignment, node=node)['node']
+
+    def branch_posterior(self, node=None):
+        """Joint posterior of (parent state, child state): (A, A, C) for
+        ``node`` > 0, (R, A, A, C) with branch 0 zeros when ``node`` is None."""
+        if node is not None and int(node) == 0:
+            raise ValueError("node 0 (the root) has no branch")
+        return self._plan.posteriors(self._alignment, node=node, want_node=False, want_branch=True)['branch']

@@ -116,6 +116,16 @@ int big_acc_group(int A);
 // mode: 0 inside pass only (LogLike / RootProb), 1 stage eigen vectors, 2 stage F81 vectors
 int launch_walk(const KParams &p, int A, int mode, bool tc, float *sa, float *sb, int c_base, int c_count,
                 int grid, cudaStream_t s);
+// MODE 2 staging (D_n s_n, U_n in the original basis) for A = 4, 8 and the
+// large alphabets
+int launch_walk_raw(const KParams &p, int A, bool tc, float *sa, float *sb, int c_base, int c_count, int grid,
+                    cudaStream_t s);
+// node / branch posteriors of branches [n_lo, n_hi) from the raw staging
+// (k_post.cu); output row = n - row_off; either output may be null
+bool post_supported(int A);
+int post_tile();
+int launch_post(const KParams &p, int A, const float *sa, const float *sb, int c_base, int c_count, int n_lo,
+                int n_hi, int row_off, float *node_out, float *br_out, int grid, cudaStream_t s);
 // tc: A = 64 eigen back-transform on the tensor cores
 int launch_acc(const KParams &p, int A, bool f81, bool tc, const float *sa, const float *sb, int c_base,
                int c_count, int grid, cudaStream_t s);

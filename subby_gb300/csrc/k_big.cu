@@ -1440,6 +1440,22 @@ int launch_walk(const KParams &p, int A, int mode, bool tc, float *sa, float *sb
   }
 }
 
+// raw per-branch staging (MODE 2) for the posteriors, also at A = 4 and 8
+template <int A>
+int walk_stage_raw(const KParams &p, float *sa, float *sb, int c_base, int c_count, int grid, cudaStream_t s) {
+  return p.f81_model ? walk_launch1<A, 2, false, true>(p, sa, sb, c_base, c_count, grid, s)
+                     : walk_launch1<A, 2, false, false>(p, sa, sb, c_base, c_count, grid, s);
+}
+
+int launch_walk_raw(const KParams &p, int A, bool tc, float *sa, float *sb, int c_base, int c_count, int grid,
+                    cudaStream_t s) {
+  switch (A) {
+    case 4: return walk_stage_raw<4>(p, sa, sb, c_base, c_count, grid, s);
+    case 8: return walk_stage_raw<8>(p, sa, sb, c_base, c_count, grid, s);
+    default: return launch_walk(p, A, 2, tc, sa, sb, c_base, c_count, grid, s);
+  }
+}
+
 int launch_acc(const KParams &p, int A, bool f81, bool tc, const float *sa, const float *sb, int c_base,
                int c_count, int grid, cudaStream_t s) {
   switch (A) {

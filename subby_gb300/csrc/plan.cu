@@ -895,14 +895,14 @@ int mark_use(subby_plan *P, cudaStream_t stream) {
   return 0;
 }
 
-int run_big(subby_plan *P, const int32_t *d_aln, int C, float *d_logL, float *d_counts, float *d_root,
-            int mode, int mask_mode, const uint8_t *d_mask, cudaStream_t stream) {
-  const int A = P->A, R = P->R;
+// Parameters of the walk (k_walk) and the kernels that consume its staging.
+KParams walk_params(const subby_plan *P, const int32_t *d_aln, int C, int mode, int mask_mode,
+                    const uint8_t *d_mask, float *d_logL, float *d_counts, float *d_root) {
   KParams k{};
   k.aln = d_aln;
   k.C = C;
-  k.R = R;
-  k.A = A;
+  k.R = P->R;
+  k.A = P->A;
   k.nInt = P->nInt;
   k.mode = mode;
   k.mask_mode = mask_mode;
@@ -921,6 +921,13 @@ int run_big(subby_plan *P, const int32_t *d_aln, int C, float *d_logL, float *d_
   k.nslots = std::max(P->prog_slots, 1);
   k.tab16 = P->d_tab16;
   k.err = P->d_err;
+  return k;
+}
+
+int run_big(subby_plan *P, const int32_t *d_aln, int C, float *d_logL, float *d_counts, float *d_root,
+            int mode, int mask_mode, const uint8_t *d_mask, cudaStream_t stream) {
+  const int A = P->A, R = P->R;
+  KParams k = walk_params(P, d_aln, C, mode, mask_mode, d_mask, d_logL, d_counts, d_root);
   // 5: tensor-core walk with the CUDA-core back-transform; 6: CUDA-core walk
   // with the tensor-core back-transform (test hooks)
   const bool tc = (A == 64) && P->d_tab16 && (g_kernel_sel == 0 || g_kernel_sel == 5);
@@ -982,6 +989,70 @@ int run_big(subby_plan *P, const int32_t *d_aln, int C, float *d_logL, float *d_
       if (lr != 0) return fail(SUBBY_ERR_CUDA, std::string("accumulate launch failed: ") + cudaGetErrorString((cudaError_t)lr));
       g_launches += 1;
     }
+  }
+  return mark_use(P, stream);
+}
+
+int run_common(subby_plan *P, const int32_t *d_aln, int C, float *d_logL, float *d_counts, float *d_root, int mode,
+               int mask_mode, const uint8_t *d_mask, const float *d_g, double *d_gt, double *d_gC, int *grid_out,
+               cudaStream_t stream);
+
+// Node / branch posteriors: the walk stages D_n s_n and U_n of every branch
+// (MODE 2, raw basis), then k_post forms the posteriors of branches
+// [n_lo, n_hi).  node < 0: every node (row 0 of the node posteriors is the
+// walk's RootProb, branch 0 of the branch posteriors zero); node > 0: that
+// node only, in row 0.  Columns in chunks bounded by the staging budget.
+int run_post(subby_plan *P, const int32_t *d_aln, int C, int node, float *d_node, float *d_br,
+             cudaStream_t stream) {
+  const int A = P->A, R = P->R;
+  const bool all = node < 0;
+  if (all && d_br) CU(cudaMemsetAsync(d_br, 0, (size_t)A * A * C * sizeof(float), stream));
+  if (R == 1 || node == 0) {
+    // the root alone: its posterior is RootProb
+    if (!d_node) return mark_use(P, stream);
+    return run_common(P, d_aln, C, nullptr, nullptr, d_node, kModeRootProb, SUBBY_MASK_NONE, nullptr, nullptr,
+                      nullptr, nullptr, nullptr, stream);
+  }
+  const int mode = (all && d_node) ? kModeRootProb : 0;
+  KParams k = walk_params(P, d_aln, C, mode, SUBBY_MASK_NONE, nullptr, nullptr, nullptr, all ? d_node : nullptr);
+  const bool tc = (A == 64) && P->d_tab16 && (g_kernel_sel == 0 || g_kernel_sel == 5);
+  const int tile = big_tile();
+  const int H = (A + 31) / 32;
+  const size_t per_col = (size_t)2 * (R - 1) * A * sizeof(float);
+  size_t cmax = std::max<size_t>(tile, kStageBudget / per_col);
+  cmax = cmax / tile * tile;
+  const size_t nch = ((size_t)C + cmax - 1) / cmax;
+  const size_t even = ((size_t)C + nch - 1) / nch;
+  const int chunk = (int)std::min<size_t>((size_t)C, (even + tile - 1) / tile * tile);
+  const int per_sm = A <= 8 ? 8 : (H == 2 ? 1 : 2);
+  const int walk_grid = std::max(1, std::min((chunk + tile - 1) / tile, P->nsm * per_sm));
+  const size_t slot_floats = (size_t)walk_grid * k.nslots * tile * A;
+  const size_t slot_ints = (size_t)walk_grid * k.nslots * tile;
+  const size_t stage_floats = (size_t)(R - 1) * chunk * A;
+  auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
+  int rc;
+  if ((rc = P->grow(P->work, al(slot_floats * 4) + al(slot_ints * 4) + 2 * al(stage_floats * 4) + 256, stream)))
+    return rc;
+  char *base = (char *)P->work.p;
+  k.scrV = (float *)base;
+  base += al(slot_floats * 4);
+  k.scrW = (int *)base;
+  base += al(slot_ints * 4);
+  float *sa = (float *)base;
+  base += al(stage_floats * 4);
+  float *sb = (float *)base;
+  const int n_lo = all ? 1 : node, n_hi = all ? R : node + 1;
+  const int row_off = all ? 0 : node;
+  for (int c0 = 0; c0 < C; c0 += chunk) {
+    const int cc = std::min(chunk, C - c0);
+    int lr = launch_walk_raw(k, A, tc, sa, sb, c0, cc, walk_grid, stream);
+    if (lr != 0) return fail(SUBBY_ERR_CUDA, std::string("walk launch failed: ") + cudaGetErrorString((cudaError_t)lr));
+    g_launches += 1;
+    const long long items = (long long)(cc + post_tile() - 1) / post_tile() * (n_hi - n_lo);
+    const int pgrid = (int)std::max<long long>(1, std::min<long long>(items, (long long)P->nsm * 4));
+    lr = launch_post(k, A, sa, sb, c0, cc, n_lo, n_hi, row_off, d_node, d_br, pgrid, stream);
+    if (lr != 0) return fail(SUBBY_ERR_CUDA, std::string("posterior launch failed: ") + cudaGetErrorString((cudaError_t)lr));
+    g_launches += 1;
   }
   return mark_use(P, stream);
 }
@@ -1252,6 +1323,53 @@ int subby_plan_branch_counts(subby_plan *P, const int32_t *aln, int C, float *br
     return rc;
   }
   CU(cudaMemcpyAsync(branchCounts, d_out, b_out, cudaMemcpyDeviceToHost, stream));
+  CU(cudaStreamSynchronize(stream));
+  if (dev != P->device) cudaSetDevice(dev);
+  return SUBBY_OK;
+}
+
+int subby_plan_posteriors(subby_plan *P, const int32_t *aln, int C, int node, float *nodePost, float *branchPost,
+                          int flags, void *stream_) {
+  g_last_error.clear();
+  g_launches = 0;
+  if (!P || !aln) return fail(SUBBY_ERR_ARG, "null plan or alignment");
+  if (!nodePost && !branchPost) return fail(SUBBY_ERR_ARG, "no output requested");
+  if (C < 0) return fail(SUBBY_ERR_ARG, "negative column count");
+  if (node < -1 || node >= P->R) return fail(SUBBY_ERR_ARG, "node index out of range");
+  if (node == 0 && branchPost) return fail(SUBBY_ERR_ARG, "node 0 (the root) has no branch");
+  if (!post_supported(P->A))
+    return fail(SUBBY_ERR_UNSUPPORTED, "posteriors are implemented for A = 4, 8, 16, 20, 32, 64");
+  if (C == 0) return SUBBY_OK;
+  std::lock_guard<std::mutex> g(P->lock);
+  cudaStream_t stream = (cudaStream_t)stream_;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev != P->device) CU(cudaSetDevice(P->device));
+  const int A = P->A, R = P->R;
+  CU(cudaStreamWaitEvent(stream, P->ready, 0));
+  const size_t rows = node < 0 ? (size_t)R : 1;
+  int rc;
+  if (flags & SUBBY_DEVICE_PTRS) {
+    rc = run_post(P, aln, C, node, nodePost, branchPost, stream);
+    if (dev != P->device) cudaSetDevice(dev);
+    return rc;
+  }
+  const size_t b_aln = (size_t)R * C * sizeof(int32_t);
+  const size_t b_node = nodePost ? rows * A * C * sizeof(float) : 0;
+  const size_t b_br = branchPost ? rows * A * A * C * sizeof(float) : 0;
+  auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
+  if ((rc = P->grow(P->io, al(b_aln) + al(b_node) + al(b_br), stream))) return rc;
+  char *base = (char *)P->io.p;
+  int32_t *d_aln = (int32_t *)base;
+  float *d_node = b_node ? (float *)(base + al(b_aln)) : nullptr;
+  float *d_br = b_br ? (float *)(base + al(b_aln) + al(b_node)) : nullptr;
+  CU(cudaMemcpyAsync(d_aln, aln, b_aln, cudaMemcpyHostToDevice, stream));
+  if ((rc = run_post(P, d_aln, C, node, d_node, d_br, stream))) {
+    cudaStreamSynchronize(stream);
+    return rc;
+  }
+  if (b_node) CU(cudaMemcpyAsync(nodePost, d_node, b_node, cudaMemcpyDeviceToHost, stream));
+  if (b_br) CU(cudaMemcpyAsync(branchPost, d_br, b_br, cudaMemcpyDeviceToHost, stream));
   CU(cudaStreamSynchronize(stream));
   if (dev != P->device) cudaSetDevice(dev);
   return SUBBY_OK;

@@ -5,12 +5,15 @@
 * Counts and root posteriors: per-column norm-wise relative error
   max_ij |d_ijc| / max(max_ij |ref_ijc|, 1e-3) <= 1e-4 (entries can be ~0,
   so per-entry relative error is ill-defined).
+* Node and branch posteriors: the same norm-wise measure per (node, column)
+  over the states (node) or state pairs (branch), <= 1e-4.
 """
 import numpy as np
 
 LOGLIKE_RTOL = 1e-5
 COUNTS_RTOL = 1e-4
 ROOTPROB_RTOL = 1e-4
+POSTERIOR_RTOL = 1e-4
 
 
 def loglike_err(got, ref):

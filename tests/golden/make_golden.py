@@ -16,8 +16,8 @@ and runs it on
 
 and writes one ``.npz`` per case holding the inputs, the reference oracle's
 outputs (logLike, unmasked and Steiner-masked Counts, F81 fast-path Counts
-where the model is F81/JC, per-branch counts for A <= 8, RootProb, branch
-mask) and, for the small A=4 cases, its intermediates.  The fixtures travel with the repository; the
+where the model is F81/JC, per-branch counts for A <= 8, RootProb, node and
+branch posteriors of InsideOutside, branch mask) and, for the small A=4 cases, its intermediates.  The fixtures travel with the repository; the
 reference itself is never read by the GPU tests.
 """
 from __future__ import annotations
@@ -68,6 +68,10 @@ def run_case(oracle, RTree, name, alignment, parent, dist, model, f81_ok,
         if f81_ok:
             out['branch_counts_f81'] = oracle.BranchCounts(alignment, tree, m, f81_fast=True, branch_mask=None)
     out['root_prob'] = oracle.RootProb(alignment, tree, m)
+    # posteriors of InsideOutside (loops O(R C A^2))
+    io = oracle.InsideOutside(alignment, tree, m)
+    out['node_posterior'] = io.node_posterior()
+    out['branch_posterior'] = io.branch_posterior()
     out['branch_mask'] = oracle.compute_branch_mask(alignment, parent, A)
     if intermediates:
         M = oracle.compute_sub_matrices(m, dist)
@@ -79,7 +83,7 @@ def run_case(oracle, RTree, name, alignment, parent, dist, model, f81_ok,
         out.update(sub_matrices=M, U=U, logNormU=lnU, D=D, logNormD=lnD, J=J,
                    U_tilde=Ut, D_tilde=Dt, C_eigen=Ce)
     path = os.path.join(HERE, f"{name}.npz")
-    np.savez(path, **out)
+    np.savez_compressed(path, **out)
     print(f"  {name}: R={len(parent)} C={alignment.shape[1]} A={A} -> {os.path.basename(path)}")
 
 

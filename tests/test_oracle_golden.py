@@ -54,6 +54,10 @@ def test_outputs_match_reference_oracle(name):
     if 'branch_counts_f81' in g:
         np.testing.assert_allclose(oracle.BranchCounts(aln, tree, model, f81_fast=True),
                                    g['branch_counts_f81'], rtol=1e-9, atol=1e-11)
+    np.testing.assert_allclose(oracle.NodePosterior(aln, tree, model), g['node_posterior'],
+                               rtol=1e-10, atol=1e-12)
+    np.testing.assert_allclose(oracle.BranchPosterior(aln, tree, model), g['branch_posterior'],
+                               rtol=1e-10, atol=1e-12)
 
 
 @pytest.mark.parametrize("name", [n for n in CASES if 'U' in _golden.load(n)])

@@ -116,10 +116,10 @@ int big_acc_group(int A);
 // mode: 0 inside pass only (LogLike / RootProb), 1 stage eigen vectors, 2 stage F81 vectors
 int launch_walk(const KParams &p, int A, int mode, bool tc, float *sa, float *sb, int c_base, int c_count,
                 int grid, cudaStream_t s);
-// MODE 2 staging (D_n s_n, U_n in the original basis) for A = 4, 8 and the
-// large alphabets
-int launch_walk_raw(const KParams &p, int A, bool tc, float *sa, float *sb, int c_base, int c_count, int grid,
-                    cudaStream_t s);
+// the walk for the posteriors at A = 4, 8 and the large alphabets: mode 0
+// (inside only) or 2 (D_n s_n, U_n staged in the original basis)
+int launch_walk_raw(const KParams &p, int A, int mode, bool tc, float *sa, float *sb, int c_base, int c_count,
+                    int grid, cudaStream_t s);
 // node / branch posteriors of branches [n_lo, n_hi) from the raw staging
 // (k_post.cu); output row = n - row_off; either output may be null
 bool post_supported(int A);

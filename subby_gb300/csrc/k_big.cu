@@ -1440,19 +1440,23 @@ int launch_walk(const KParams &p, int A, int mode, bool tc, float *sa, float *sb
   }
 }
 
-// raw per-branch staging (MODE 2) for the posteriors, also at A = 4 and 8
+// the walk of the posteriors, also at A = 4 and 8: mode 0 (inside only, the
+// root's posterior) or 2 (raw per-branch staging)
 template <int A>
-int walk_stage_raw(const KParams &p, float *sa, float *sb, int c_base, int c_count, int grid, cudaStream_t s) {
+int walk_post(const KParams &p, int mode, float *sa, float *sb, int c_base, int c_count, int grid, cudaStream_t s) {
+  if (mode == 0)
+    return p.f81_model ? walk_launch1<A, 0, false, true>(p, sa, sb, c_base, c_count, grid, s)
+                       : walk_launch1<A, 0, false, false>(p, sa, sb, c_base, c_count, grid, s);
   return p.f81_model ? walk_launch1<A, 2, false, true>(p, sa, sb, c_base, c_count, grid, s)
                      : walk_launch1<A, 2, false, false>(p, sa, sb, c_base, c_count, grid, s);
 }
 
-int launch_walk_raw(const KParams &p, int A, bool tc, float *sa, float *sb, int c_base, int c_count, int grid,
-                    cudaStream_t s) {
+int launch_walk_raw(const KParams &p, int A, int mode, bool tc, float *sa, float *sb, int c_base, int c_count,
+                    int grid, cudaStream_t s) {
   switch (A) {
-    case 4: return walk_stage_raw<4>(p, sa, sb, c_base, c_count, grid, s);
-    case 8: return walk_stage_raw<8>(p, sa, sb, c_base, c_count, grid, s);
-    default: return launch_walk(p, A, 2, tc, sa, sb, c_base, c_count, grid, s);
+    case 4: return walk_post<4>(p, mode, sa, sb, c_base, c_count, grid, s);
+    case 8: return walk_post<8>(p, mode, sa, sb, c_base, c_count, grid, s);
+    default: return launch_walk(p, A, mode, tc, sa, sb, c_base, c_count, grid, s);
   }
 }
 

@@ -993,10 +993,6 @@ int run_big(subby_plan *P, const int32_t *d_aln, int C, float *d_logL, float *d_
   return mark_use(P, stream);
 }
 
-int run_common(subby_plan *P, const int32_t *d_aln, int C, float *d_logL, float *d_counts, float *d_root, int mode,
-               int mask_mode, const uint8_t *d_mask, const float *d_g, double *d_gt, double *d_gC, int *grid_out,
-               cudaStream_t stream);
-
 // Node / branch posteriors: the walk stages D_n s_n and U_n of every branch
 // (MODE 2, raw basis), then k_post forms the posteriors of branches
 // [n_lo, n_hi).  node < 0: every node (row 0 of the node posteriors is the
@@ -1007,28 +1003,29 @@ int run_post(subby_plan *P, const int32_t *d_aln, int C, int node, float *d_node
   const int A = P->A, R = P->R;
   const bool all = node < 0;
   if (all && d_br) CU(cudaMemsetAsync(d_br, 0, (size_t)A * A * C * sizeof(float), stream));
-  if (R == 1 || node == 0) {
-    // the root alone: its posterior is RootProb
-    if (!d_node) return mark_use(P, stream);
-    return run_common(P, d_aln, C, nullptr, nullptr, d_node, kModeRootProb, SUBBY_MASK_NONE, nullptr, nullptr,
-                      nullptr, nullptr, nullptr, stream);
-  }
-  const int mode = (all && d_node) ? kModeRootProb : 0;
-  KParams k = walk_params(P, d_aln, C, mode, SUBBY_MASK_NONE, nullptr, nullptr, nullptr, all ? d_node : nullptr);
+  // the root alone (node 0, or a one-node tree): the inside walk's RootProb,
+  // the same arithmetic as row 0 of the all-node result
+  const bool stage = R > 1 && node != 0;
+  if (!stage && !d_node) return mark_use(P, stream);
+  const int mode = (node <= 0 && d_node) ? kModeRootProb : 0;
+  KParams k = walk_params(P, d_aln, C, mode, SUBBY_MASK_NONE, nullptr, nullptr, nullptr, node <= 0 ? d_node : nullptr);
   const bool tc = (A == 64) && P->d_tab16 && (g_kernel_sel == 0 || g_kernel_sel == 5);
   const int tile = big_tile();
   const int H = (A + 31) / 32;
-  const size_t per_col = (size_t)2 * (R - 1) * A * sizeof(float);
-  size_t cmax = std::max<size_t>(tile, kStageBudget / per_col);
-  cmax = cmax / tile * tile;
-  const size_t nch = ((size_t)C + cmax - 1) / cmax;
-  const size_t even = ((size_t)C + nch - 1) / nch;
-  const int chunk = (int)std::min<size_t>((size_t)C, (even + tile - 1) / tile * tile);
+  int chunk = C;
+  if (stage) {
+    const size_t per_col = (size_t)2 * (R - 1) * A * sizeof(float);
+    size_t cmax = std::max<size_t>(tile, kStageBudget / per_col);
+    cmax = cmax / tile * tile;
+    const size_t nch = ((size_t)C + cmax - 1) / cmax;
+    const size_t even = ((size_t)C + nch - 1) / nch;
+    chunk = (int)std::min<size_t>((size_t)C, (even + tile - 1) / tile * tile);
+  }
   const int per_sm = A <= 8 ? 8 : (H == 2 ? 1 : 2);
   const int walk_grid = std::max(1, std::min((chunk + tile - 1) / tile, P->nsm * per_sm));
   const size_t slot_floats = (size_t)walk_grid * k.nslots * tile * A;
   const size_t slot_ints = (size_t)walk_grid * k.nslots * tile;
-  const size_t stage_floats = (size_t)(R - 1) * chunk * A;
+  const size_t stage_floats = stage ? (size_t)(R - 1) * chunk * A : 0;
   auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
   int rc;
   if ((rc = P->grow(P->work, al(slot_floats * 4) + al(slot_ints * 4) + 2 * al(stage_floats * 4) + 256, stream)))
@@ -1045,9 +1042,10 @@ int run_post(subby_plan *P, const int32_t *d_aln, int C, int node, float *d_node
   const int row_off = all ? 0 : node;
   for (int c0 = 0; c0 < C; c0 += chunk) {
     const int cc = std::min(chunk, C - c0);
-    int lr = launch_walk_raw(k, A, tc, sa, sb, c0, cc, walk_grid, stream);
+    int lr = launch_walk_raw(k, A, stage ? 2 : 0, tc, sa, sb, c0, cc, walk_grid, stream);
     if (lr != 0) return fail(SUBBY_ERR_CUDA, std::string("walk launch failed: ") + cudaGetErrorString((cudaError_t)lr));
     g_launches += 1;
+    if (!stage) continue;
     const long long items = (long long)(cc + post_tile() - 1) / post_tile() * (n_hi - n_lo);
     const int pgrid = (int)std::max<long long>(1, std::min<long long>(items, (long long)P->nsm * 4));
     lr = launch_post(k, A, sa, sb, c0, cc, n_lo, n_hi, row_off, d_node, d_br, pgrid, stream);

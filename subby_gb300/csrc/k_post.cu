@@ -77,8 +77,10 @@ __global__ void __launch_bounds__(kPostTile) k_post(const KParams P, const float
 #pragma unroll
       for (int q = 0; q < JB / 4; ++q) {
         const float4 u = __ldg(reinterpret_cast<const float4 *>(pb + jb) + q);
-        const float y0 = acc[4 * q] * u.x, y1 = acc[4 * q + 1] * u.y, y2 = acc[4 * q + 2] * u.z,
-                    y3 = acc[4 * q + 3] * u.w;
+        // rounded products (no contraction into the sum), so that every
+        // variant of the kernel forms the same Z
+        const float y0 = __fmul_rn(acc[4 * q], u.x), y1 = __fmul_rn(acc[4 * q + 1], u.y),
+                    y2 = __fmul_rn(acc[4 * q + 2], u.z), y3 = __fmul_rn(acc[4 * q + 3], u.w);
         Z += (y0 + y1) + (y2 + y3);
         if constexpr (NODE) {
           ys[(jb + 4 * q) * kPostTile + t] = y0;

@@ -100,6 +100,10 @@ struct KParams {
   int f81_model;
   // F81 staging (k_walk MODE 2): per branch and column (pi . U, sum s D), or null
   float2 *stage_c;
+  // node posteriors (k_walk MODE 3): (R, A, C) for npost_node < 0, else the
+  // (A, C) of node npost_node
+  float *npost;
+  int npost_node;
 };
 
 // launchers (k_small.cu / k_warp.cu)
@@ -116,16 +120,17 @@ int big_acc_group(int A);
 // mode: 0 inside pass only (LogLike / RootProb), 1 stage eigen vectors, 2 stage F81 vectors
 int launch_walk(const KParams &p, int A, int mode, bool tc, float *sa, float *sb, int c_base, int c_count,
                 int grid, cudaStream_t s);
-// the walk for the posteriors at A = 4, 8 and the large alphabets: mode 0
-// (inside only) or 2 (D_n s_n, U_n staged in the original basis)
-int launch_walk_raw(const KParams &p, int A, int mode, bool tc, float *sa, float *sb, int c_base, int c_count,
-                    int grid, cudaStream_t s);
-// node / branch posteriors of branches [n_lo, n_hi) from the raw staging
-// (k_post.cu); output row = n - row_off; either output may be null
+// the walk of the posteriors (k_walkpost.cu) at A = 4, 8 and the large
+// alphabets: mode 0 (inside only: the root's posterior) or 3 (node
+// posteriors, and D_n s_n, U_n staged in the original basis when sa is given)
+int launch_walk_post(const KParams &p, int A, int mode, bool tc, float *sa, float *sb, int c_base, int c_count,
+                     int grid, cudaStream_t s);
+// branch posteriors of branches [n_lo, n_hi) from the raw staging
+// (k_post.cu); output row = n - row_off
 bool post_supported(int A);
 int post_tile();
 int launch_post(const KParams &p, int A, const float *sa, const float *sb, int c_base, int c_count, int n_lo,
-                int n_hi, int row_off, float *node_out, float *br_out, int grid, cudaStream_t s);
+                int n_hi, int row_off, float *br_out, int grid, cudaStream_t s);
 // tc: A = 64 eigen back-transform on the tensor cores
 int launch_acc(const KParams &p, int A, bool f81, bool tc, const float *sa, const float *sb, int c_base,
                int c_count, int grid, cudaStream_t s);

@@ -993,22 +993,24 @@ int run_big(subby_plan *P, const int32_t *d_aln, int C, float *d_logL, float *d_
   return mark_use(P, stream);
 }
 
-// Node / branch posteriors: the walk stages D_n s_n and U_n of every branch
-// (MODE 2, raw basis), then k_post forms the posteriors of branches
-// [n_lo, n_hi).  node < 0: every node (row 0 of the node posteriors is the
-// walk's RootProb, branch 0 of the branch posteriors zero); node > 0: that
-// node only, in row 0.  Columns in chunks bounded by the staging budget.
+// Node / branch posteriors.  The walk (mode 3) writes the node posteriors of
+// every non-root node from the D_n, U_n it holds and, for the branch
+// posteriors, stages D_n s_n and U_n (raw basis) for k_post; the root's row
+// is the walk's RootProb (mode 0 alone for node 0 or a one-node tree).
+// node < 0: every node (branch 0 of the branch posteriors zero); node > 0:
+// that node only, in row 0.  Columns in chunks bounded by the staging budget.
 int run_post(subby_plan *P, const int32_t *d_aln, int C, int node, float *d_node, float *d_br,
              cudaStream_t stream) {
   const int A = P->A, R = P->R;
   const bool all = node < 0;
   if (all && d_br) CU(cudaMemsetAsync(d_br, 0, (size_t)A * A * C * sizeof(float), stream));
-  // the root alone (node 0, or a one-node tree): the inside walk's RootProb,
-  // the same arithmetic as row 0 of the all-node result
-  const bool stage = R > 1 && node != 0;
-  if (!stage && !d_node) return mark_use(P, stream);
+  const bool outside = R > 1 && node != 0;
+  if (!outside && !d_node) return mark_use(P, stream);
+  const bool stage = outside && d_br;
   const int mode = (node <= 0 && d_node) ? kModeRootProb : 0;
   KParams k = walk_params(P, d_aln, C, mode, SUBBY_MASK_NONE, nullptr, nullptr, nullptr, node <= 0 ? d_node : nullptr);
+  k.npost = d_node;
+  k.npost_node = node;
   const bool tc = (A == 64) && P->d_tab16 && (g_kernel_sel == 0 || g_kernel_sel == 5);
   const int tile = big_tile();
   const int H = (A + 31) / 32;
@@ -1035,20 +1037,20 @@ int run_post(subby_plan *P, const int32_t *d_aln, int C, int node, float *d_node
   base += al(slot_floats * 4);
   k.scrW = (int *)base;
   base += al(slot_ints * 4);
-  float *sa = (float *)base;
+  float *sa = stage ? (float *)base : nullptr;
   base += al(stage_floats * 4);
-  float *sb = (float *)base;
+  float *sb = stage ? (float *)base : nullptr;
   const int n_lo = all ? 1 : node, n_hi = all ? R : node + 1;
   const int row_off = all ? 0 : node;
   for (int c0 = 0; c0 < C; c0 += chunk) {
     const int cc = std::min(chunk, C - c0);
-    int lr = launch_walk_raw(k, A, stage ? 2 : 0, tc, sa, sb, c0, cc, walk_grid, stream);
+    int lr = launch_walk_post(k, A, outside ? 3 : 0, tc, sa, sb, c0, cc, walk_grid, stream);
     if (lr != 0) return fail(SUBBY_ERR_CUDA, std::string("walk launch failed: ") + cudaGetErrorString((cudaError_t)lr));
     g_launches += 1;
     if (!stage) continue;
     const long long items = (long long)(cc + post_tile() - 1) / post_tile() * (n_hi - n_lo);
-    const int pgrid = (int)std::max<long long>(1, std::min<long long>(items, (long long)P->nsm * 4));
-    lr = launch_post(k, A, sa, sb, c0, cc, n_lo, n_hi, row_off, d_node, d_br, pgrid, stream);
+    const int pgrid = (int)std::max<long long>(1, std::min<long long>(items, (long long)P->nsm * 8));
+    lr = launch_post(k, A, sa, sb, c0, cc, n_lo, n_hi, row_off, d_br, pgrid, stream);
     if (lr != 0) return fail(SUBBY_ERR_CUDA, std::string("posterior launch failed: ") + cudaGetErrorString((cudaError_t)lr));
     g_launches += 1;
   }

@@ -104,6 +104,9 @@ struct KParams {
   // (A, C) of node npost_node
   float *npost;
   int npost_node;
+  // branch joint posteriors (k_tree4, A = 4): (R, 4, 4, C) or the (4, 4, C)
+  // of node npost_node
+  float *bpost;
 };
 
 // launchers (k_small.cu / k_warp.cu)
@@ -136,6 +139,8 @@ int launch_acc(const KParams &p, int A, bool f81, bool tc, const float *sa, cons
                int c_count, int grid, cudaStream_t s);
 int launch_tree4(const KParams &p, bool f81, int mask_mode, int grid, int block, size_t smem,
                  cudaStream_t s);
+// A = 4 posteriors (npost / bpost) from the tree-program kernel
+int launch_tree4_post(const KParams &p, int grid, int block, size_t smem, cudaStream_t s);
 // A = 64 F81 accumulation on the tensor cores (k_acctc.cu); groups of 8 columns
 int launch_acc_f81_tc(const KParams &p, const float *sa, const float *sb, const float2 *sc, int c_base,
                       int c_count, int grid, cudaStream_t s);

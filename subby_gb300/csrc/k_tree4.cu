@@ -113,9 +113,13 @@ struct N4 {
 //   stab[2] J    R x 16 (eigen) or F81 R x 4
 //   stab[3] K    R x 5 x 20 (eigen: K_n[code][k][l] = J_n[k][l] Ut[code][l], rows padded)
 //   stab[4] LV   5 x 4 (observation rows), followed by piL[5] (pi . L(code))
-// BR: per-branch counts (R, 4, 4, C) written branch by branch instead of
-// the sum over branches.
-template <bool F81, int MASK, bool BR>
+// OUT: kOutSum, the counts summed over branches; kOutBranch, per-branch
+// counts (R, 4, 4, C) written branch by branch; kOutPost, node posteriors
+// (npost) and / or branch joint posteriors (bpost) of every non-root node
+// (InsideOutside.node_posterior / branch_posterior, subby/oracle/oracle.py:
+// 1755-1905), the root's row from RootProb.
+constexpr int kOutSum = 0, kOutBranch = 1, kOutPost = 2;
+template <bool F81, int MASK, int OUT>
 __global__ void __launch_bounds__(256, 1) k_tree4(const KParams P) {
   extern __shared__ __align__(16) float sm[];
   for (int t = 0; t < P.ntab; ++t) {
@@ -296,7 +300,8 @@ __global__ void __launch_bounds__(256, 1) k_tree4(const KParams P) {
       P.rootp[(size_t)2 * C + col] = q.b.x;
       P.rootp[(size_t)3 * C + col] = q.b.y;
     }
-    if (!(P.mode & kModeCounts)) continue;
+    if (!(P.mode & kModeCounts) && OUT != kOutPost) continue;
+    if (OUT == kOutPost && (P.nsteps == 0 || P.npost_node == 0)) continue;
     if (P.nsteps == 0) {
       if (valid)
         for (int i = 0; i < 16; ++i) P.counts[(size_t)i * C + col] = 0.f;
@@ -310,7 +315,7 @@ __global__ void __launch_bounds__(256, 1) k_tree4(const KParams P) {
     for (int k = 0; k < 4; ++k) acc[k] = hacc;
 
     // branch above node n; for leaves `code` >= 0 selects the table rows
-    // per-branch counts of branch n (BR): 16 values from the rows I_i
+    // per-branch counts of branch n (kOutBranch): 16 values from the rows I_i
     auto put_branch = [&](int n, const F4 (&I)[4]) {
       float *o = P.counts + (size_t)n * 16 * C + col;
       const float r[4][4] = {{I[0].a.x, I[0].a.y, I[0].b.x, I[0].b.y}, {I[1].a.x, I[1].a.y, I[1].b.x, I[1].b.y},
@@ -324,8 +329,42 @@ __global__ void __launch_bounds__(256, 1) k_tree4(const KParams P) {
     auto branch = [&](int n, const F4 &D, const F4 &U, int code, int eDU, int active) {
       float s = invP * __int_as_float((max(-127, min(127, eDU - eRoot)) + 127) << 23);
       if (MASK != kMaskNone) s = active ? s : 0.f;
+      if constexpr (OUT == kOutPost) {
+        // y = D^T M_n; node posterior y o U / Z, branch joint D_i M_n[i][j] U_j / Z
+        (void)s;
+        if (P.npost_node >= 0 && n != P.npost_node) return;
+        const float *Mn = MT + n * 20;
+        const F4 p = mul4(vecmat4(Mn, D), U);
+        const float z = sum4(p);
+        const float inv = z > 0.f ? 1.0f / z : 1.0f;
+        if (!valid) return;
+        const size_t row = P.npost_node < 0 ? (size_t)n : 0;
+        if (P.npost) {
+          float *o = P.npost + row * 4 * C + col;
+          o[0] = p.a.x * inv;
+          o[(size_t)C] = p.a.y * inv;
+          o[(size_t)2 * C] = p.b.x * inv;
+          o[(size_t)3 * C] = p.b.y * inv;
+        }
+        if (P.bpost) {
+          float *o = P.bpost + row * 16 * C + col;
+          const F4 ui = scale4(U, inv);
+          const float dk[4] = {D.a.x, D.a.y, D.b.x, D.b.y};
+#pragma unroll
+          for (int i2 = 0; i2 < 4; ++i2) {
+            // row i of M_n is column i of the MT rows: M_n[i][j] = MT[n][j][i]
+            const F4 mi = F4{make_float2(Mn[i2], Mn[4 + i2]), make_float2(Mn[8 + i2], Mn[12 + i2])};
+            const F4 r = scale4(mul4(mi, ui), dk[i2]);
+            o[(size_t)(4 * i2) * C] = r.a.x;
+            o[(size_t)(4 * i2 + 1) * C] = r.a.y;
+            o[(size_t)(4 * i2 + 2) * C] = r.b.x;
+            o[(size_t)(4 * i2 + 3) * C] = r.b.y;
+          }
+        }
+        return;
+      }
       const F4 Ds = scale4(D, s);
-      if constexpr (BR) {
+      if constexpr (OUT == kOutBranch) {
         F4 I[4];
         if constexpr (F81) {
           // I_ij = (alpha Ds_i + beta pi_i sum(Ds)) U_j + (beta Ds_i + gamma pi_i sum(Ds)) pi.U,
@@ -496,7 +535,7 @@ __global__ void __launch_bounds__(256, 1) k_tree4(const KParams P) {
       for (int q = 0; q < 7; ++q) tk[q] = tn[q];
     }
     // ------------------------------------------------------------ epilogue
-    if (BR || !valid) continue;
+    if (OUT != kOutSum || !valid) continue;
     float *out = P.counts + col;
     if constexpr (F81) {
       float pi_[4] = {piv.a.x, piv.a.y, piv.b.x, piv.b.y};
@@ -568,32 +607,36 @@ __global__ void __launch_bounds__(256, 1) k_tree4(const KParams P) {
                  : "memory");
 }
 
-template <bool F, int M, bool B>
+template <bool F, int M, int O>
 int t4launch(const KParams &p, int grid, int block, size_t smem, cudaStream_t s) {
-  cudaError_t e = cudaFuncSetAttribute(k_tree4<F, M, B>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaError_t e = cudaFuncSetAttribute(k_tree4<F, M, O>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return (int)e;
-  k_tree4<F, M, B><<<grid, block, smem, s>>>(p);
+  k_tree4<F, M, O><<<grid, block, smem, s>>>(p);
   return (int)cudaGetLastError();
 }
 
-template <bool B>
+template <int O>
 int t4launch_m(const KParams &p, bool f81, int mask_mode, int grid, int block, size_t smem, cudaStream_t s) {
   if (f81) {
-    if (mask_mode == kMaskAuto) return t4launch<true, kMaskAuto, B>(p, grid, block, smem, s);
-    if (mask_mode == kMaskGiven) return t4launch<true, kMaskGiven, B>(p, grid, block, smem, s);
-    return t4launch<true, kMaskNone, B>(p, grid, block, smem, s);
+    if (mask_mode == kMaskAuto) return t4launch<true, kMaskAuto, O>(p, grid, block, smem, s);
+    if (mask_mode == kMaskGiven) return t4launch<true, kMaskGiven, O>(p, grid, block, smem, s);
+    return t4launch<true, kMaskNone, O>(p, grid, block, smem, s);
   }
-  if (mask_mode == kMaskAuto) return t4launch<false, kMaskAuto, B>(p, grid, block, smem, s);
-  if (mask_mode == kMaskGiven) return t4launch<false, kMaskGiven, B>(p, grid, block, smem, s);
-  return t4launch<false, kMaskNone, B>(p, grid, block, smem, s);
+  if (mask_mode == kMaskAuto) return t4launch<false, kMaskAuto, O>(p, grid, block, smem, s);
+  if (mask_mode == kMaskGiven) return t4launch<false, kMaskGiven, O>(p, grid, block, smem, s);
+  return t4launch<false, kMaskNone, O>(p, grid, block, smem, s);
 }
 
 }  // namespace
 
 int launch_tree4(const KParams &p, bool f81, int mask_mode, int grid, int block, size_t smem,
                  cudaStream_t s) {
-  return (p.mode & kModeBranch) ? t4launch_m<true>(p, f81, mask_mode, grid, block, smem, s)
-                                : t4launch_m<false>(p, f81, mask_mode, grid, block, smem, s);
+  return (p.mode & kModeBranch) ? t4launch_m<kOutBranch>(p, f81, mask_mode, grid, block, smem, s)
+                                : t4launch_m<kOutSum>(p, f81, mask_mode, grid, block, smem, s);
+}
+
+int launch_tree4_post(const KParams &p, int grid, int block, size_t smem, cudaStream_t s) {
+  return t4launch<false, kMaskNone, kOutPost>(p, grid, block, smem, s);
 }
 
 }  // namespace subby

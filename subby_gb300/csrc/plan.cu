@@ -1006,6 +1006,34 @@ int run_post(subby_plan *P, const int32_t *d_aln, int C, int node, float *d_node
   if (all && d_br) CU(cudaMemsetAsync(d_br, 0, (size_t)A * A * C * sizeof(float), stream));
   const bool outside = R > 1 && node != 0;
   if (!outside && !d_node) return mark_use(P, stream);
+  Launch L4;
+  if (A == 4 && R > 1 && plan_tree4(P, 0, C, L4) == 0) {
+    // the A = 4 tree-program kernel writes both posteriors directly
+    KParams &k = L4.kp;
+    k.aln = d_aln;
+    k.C = C;
+    k.R = R;
+    k.A = A;
+    k.nInt = P->nInt;
+    k.mode = (node <= 0 && d_node) ? kModeRootProb : 0;
+    k.mask_mode = kMaskNone;
+    k.tab = P->d_tab;
+    k.tab64 = P->d_tab64;
+    k.off = P->off;
+    k.steps = P->d_steps;
+    k.slots = P->d_slots;
+    k.root_is_leaf = P->root_is_leaf;
+    k.f81_mu = P->f81_mu;
+    k.nworkers = L4.nworkers;
+    k.rootp = node <= 0 ? d_node : nullptr;
+    k.npost = d_node;
+    k.npost_node = node;
+    k.bpost = d_br;
+    const int lr = launch_tree4_post(k, L4.grid, L4.block, L4.smem, stream);
+    if (lr != 0) return fail(SUBBY_ERR_CUDA, std::string("kernel launch failed: ") + cudaGetErrorString((cudaError_t)lr));
+    g_launches += 1;
+    return mark_use(P, stream);
+  }
   const bool stage = outside && d_br;
   const int mode = (node <= 0 && d_node) ? kModeRootProb : 0;
   KParams k = walk_params(P, d_aln, C, mode, SUBBY_MASK_NONE, nullptr, nullptr, nullptr, node <= 0 ? d_node : nullptr);

@@ -92,6 +92,34 @@ def test_plain_workloads_vs_oracle_and_identities():
         plan.close()
 
 
+def test_a4_walk_route_matches_tree_kernel_route():
+    """A = 4 posteriors come from the tree-program kernel; with it switched
+    off (kernel selector 1) the walk + branch-posterior kernel serve them.
+    Both match the oracle, eigen and F81 models, all nodes and one node."""
+    for w in (synth.plain_small(seed=9, C=333), synth.plain_large(seed=10, C=200, f81=True)):
+        aln, tree, m = w['alignment'], w['tree'], w['model']
+        ot = oracle.Tree(tree.parentIndex, tree.distanceToParent)
+        ref_n = oracle.NodePosterior(aln, ot, m._asdict())
+        ref_b = oracle.BranchPosterior(aln, ot, m._asdict())
+        plan = sg.Plan(tree, m)
+        got = {}
+        try:
+            for sel in (0, 1):
+                _lib.load().subby_debug_set_kernel(sel)
+                got[sel] = plan.posteriors(aln, want_node=True, want_branch=True)
+                one = plan.posteriors(aln, node=3, want_node=True, want_branch=True)
+                np.testing.assert_array_equal(one['node'], got[sel]['node'][3])
+                np.testing.assert_array_equal(one['branch'], got[sel]['branch'][3])
+                root = plan.posteriors(aln, node=0)['node']
+                np.testing.assert_array_equal(root, got[sel]['node'][0])
+        finally:
+            _lib.load().subby_debug_set_kernel(0)
+        for sel in (0, 1):
+            _check(got[sel]['node'], ref_n, f"selector {sel} node")
+            _check(got[sel]['branch'], ref_b, f"selector {sel} branch")
+        plan.close()
+
+
 @pytest.mark.parametrize("A,leaves,C", [(8, 9, 70), (16, 9, 45), (20, 7, 33), (32, 5, 17), (64, 6, 140)])
 def test_large_alphabets_vs_oracle(A, leaves, C):
     """The walk's raw staging at A = 8 .. 64 (tensor-core walk at A = 64), a

@@ -586,7 +586,9 @@ __global__ void __launch_bounds__(128 * Geo<A>::H, 1) k_walk(const KParams P, fl
 
     // ---------------------------------------------------------------- outside
     // stage the two vectors of the branch above node n for column cc0
-    auto emit = [&](int n, const BV<A> &D, const BV<A> &U, int leafcode, int eDU, int active) {
+    // DM: D^T M_n when the caller has it (mode 3 node posteriors)
+    auto emit = [&](int n, const BV<A> &D, const BV<A> &U, int leafcode, int eDU, int active,
+                    const BV<A> *DM = nullptr) {
       float s = invP * __int_as_float((max(-127, min(127, eDU - eRoot)) + 127) << 23);
       s = active ? s : 0.f;
       float *pa = stage_a + ((size_t)(n - 1) * c_count + (valid ? cc0 : c_count - 1)) * A + 32 * h;
@@ -604,7 +606,8 @@ __global__ void __launch_bounds__(128 * Geo<A>::H, 1) k_walk(const KParams P, fl
           // (oracle.py:1755-1831); the scale s cancels
           if (P.npost && (P.npost_node < 0 || n == P.npost_node)) {
             BV<A> y;
-            mprod(y, D, n, true);
+            if (DM) y = *DM;
+            else mprod(y, D, n, true);
             float z = 0.f;
 #pragma unroll
             for (int q = 0; q < S; ++q) {
@@ -719,6 +722,9 @@ __global__ void __launch_bounds__(128 * Geo<A>::H, 1) k_walk(const KParams P, fl
           } else {
             emit_tc(s0.x, D, &U, -1, eD + eUp, actp, O, P.tab16 + (size_t)s0.x * 24576 + 12288);
           }
+        } else if constexpr (MODE == 3) {
+          mprod(O, D, s0.x, true);
+          emit(s0.x, D, U, -1, eD + eUp, actp, &O);
         } else {
           emit(s0.x, D, U, -1, eD + eUp, actp);
           mprod(O, D, s0.x, true);
@@ -768,11 +774,14 @@ __global__ void __launch_bounds__(128 * Geo<A>::H, 1) k_walk(const KParams P, fl
             if constexpr (kFuse) {
               if constexpr (f81m) emit_tc(sc.x, Dc, &du, -1, eDc + me.e, actc, Onone, nullptr);
               else emit_tc(sc.x, Dc, &du, -1, eDc + me.e, actc, Oc, P.tab16 + (size_t)sc.x * 24576 + 12288);
+            } else if constexpr (MODE == 3) {
+              mprod(Oc, Dc, sc.x, true);
+              emit(sc.x, Dc, du, -1, eDc + me.e, actc, &Oc);
             } else {
               emit(sc.x, Dc, du, -1, eDc + me.e, actc);
             }
           }
-          if constexpr (!kFuse || f81m) mprod(Oc, Dc, sc.x, true);
+          if constexpr ((!kFuse || f81m) && MODE != 3) mprod(Oc, Dc, sc.x, true);
           wk.obs(Oc, dcode);
           const int eOc = eDc + wk.rescale(Oc);
 #pragma unroll

@@ -139,6 +139,107 @@ def diagonalize_rate_matrix(subRate, rootProb):
     return {'eigenvalues': ev, 'eigenvectors': V, 'pi': pi}
 
 
+def diagonalize_irreversible(subRate, rootProb):
+    """Complex eigensystem R = V diag(mu) V^-1 via numpy eig; oracle.py:265-288."""
+    subRate = np.asarray(subRate, dtype=np.float64)
+    mu, V = np.linalg.eig(subRate)
+    return {'eigenvalues': mu, 'eigenvectors': V, 'eigenvectors_inv': np.linalg.inv(V),
+            'pi': np.asarray(rootProb, dtype=np.float64), 'reversible': False}
+
+
+def irrev_model_from_rate_matrix(subRate, pi):
+    """oracle.py:291-301."""
+    return diagonalize_irreversible(subRate, pi)
+
+
+def is_irrev(model):
+    """A model dict is irreversible when it says reversible=False
+    (oracle.py:1442-1444) or carries V^-1."""
+    return (not model.get('reversible', True)) or ('eigenvectors_inv' in model)
+
+
+def compute_sub_matrices_irrev(model, distances):
+    """M_ij(t) = Re sum_k V_ik e^{mu_k t} Vinv_kj; oracle.py:474-501."""
+    V = np.asarray(model['eigenvectors'], dtype=np.complex128)
+    Vi = np.asarray(model['eigenvectors_inv'], dtype=np.complex128)
+    mu = np.asarray(model['eigenvalues'], dtype=np.complex128)
+    t = np.asarray(distances, dtype=np.float64)
+    E = np.exp(mu[None, :] * t[:, None])                    # (R, A)
+    return np.einsum('ik,rk,kj->rij', V, E, Vi).real
+
+
+def compute_J_complex(eigenvalues, distances):
+    """Complex J^{kl}(t), 1e-8 degeneracy test on |mu_k - mu_l|; oracle.py:508-534."""
+    mu = np.asarray(eigenvalues, dtype=np.complex128)
+    t = np.asarray(distances, dtype=np.float64)
+    E = np.exp(mu[None, :] * t[:, None])
+    diff = mu[:, None] - mu[None, :]
+    deg = np.abs(diff) < DEGENERATE_THRESHOLD
+    safe = np.where(deg, 1.0, diff)
+    J = (E[:, :, None] - E[:, None, :]) / safe[None]
+    Jdeg = t[:, None, None] * E[:, :, None] * np.ones_like(diff)[None]
+    return np.where(deg[None], Jdeg, J)
+
+
+def eigenbasis_project_irrev(U, D, model):
+    """U~_k = sum_b U_b V_bk, D~_k = sum_a D_a Vinv_ka; oracle.py:537-570."""
+    V = np.asarray(model['eigenvectors'], dtype=np.complex128)
+    Vi = np.asarray(model['eigenvectors_inv'], dtype=np.complex128)
+    return U @ V, D @ Vi.T
+
+
+def accumulate_C_complex(D_tilde, U_tilde, J, logNormU, logNormD, logLike, parentIndex,
+                         branch_mask=None):
+    """Complex C_kl,c = sum_{n>0} D~_k J_kl U~_l exp(lnD+lnU-lnL); oracle.py:573-603."""
+    R, C, A = U_tilde.shape
+    out = np.zeros((A, A, C), dtype=np.complex128)
+    for n in range(1, R):
+        s = np.exp(logNormD[n] + logNormU[n] - logLike)
+        if branch_mask is not None:
+            s = np.where(np.asarray(branch_mask)[n], s, 0.0)
+        out += np.einsum('ck,kl,cl->klc', D_tilde[n] * s[:, None], J[n], U_tilde[n])
+    return out
+
+
+def accumulate_C_complex_per_branch(D_tilde, U_tilde, J, logNormU, logNormD, logLike, parentIndex,
+                                    branch_mask=None):
+    """Per-branch complex C (R, A, A, C), branch 0 zero; oracle.py:606-639."""
+    R, C, A = U_tilde.shape
+    out = np.zeros((R, A, A, C), dtype=np.complex128)
+    for n in range(1, R):
+        s = np.exp(logNormD[n] + logNormU[n] - logLike)
+        if branch_mask is not None:
+            s = np.where(np.asarray(branch_mask)[n], s, 0.0)
+        out[n] = np.einsum('ck,kl,cl->klc', D_tilde[n] * s[:, None], J[n], U_tilde[n])
+    return out
+
+
+def _rate_irrev(model):
+    V = np.asarray(model['eigenvectors'], dtype=np.complex128)
+    Vi = np.asarray(model['eigenvectors_inv'], dtype=np.complex128)
+    mu = np.asarray(model['eigenvalues'], dtype=np.complex128)
+    return V, Vi, (V * mu[None, :]) @ Vi
+
+
+def back_transform_irrev(Ceig, model):
+    """Re of V C Vinv on the diagonal, of R_ij (V C Vinv)_ij off it, with
+    R = V diag(mu) Vinv; oracle.py:642-693."""
+    V, Vi, Rm = _rate_irrev(model)
+    VCV = np.einsum('ik,klc,lj->ijc', V, Ceig, Vi)
+    A = V.shape[0]
+    eye = np.eye(A, dtype=bool)[:, :, None]
+    return np.where(eye, VCV, Rm[:, :, None] * VCV).real
+
+
+def back_transform_irrev_per_branch(Ceig, model):
+    """oracle.py:696-740."""
+    V, Vi, Rm = _rate_irrev(model)
+    VCV = np.einsum('ik,nklc,lj->nijc', V, Ceig, Vi)
+    A = V.shape[0]
+    eye = np.eye(A, dtype=bool)[None, :, :, None]
+    return np.where(eye, VCV, Rm[None, :, :, None] * VCV).real
+
+
 # ---------------------------------------------------------------------------
 # Substitution matrices, inside and outside — oracle.py:747-924
 # ---------------------------------------------------------------------------
@@ -371,7 +472,7 @@ def compute_branch_mask(alignment, parentIndex, A):
 
 def LogLike(alignment, tree, model):
     """Per-column log-likelihood (C,); oracle.py:1454-1467."""
-    M = compute_sub_matrices(model, tree.distanceToParent)
+    M = _sub_matrices(model, tree.distanceToParent)
     return upward_pass(alignment, tree, M, model['pi'])[2]
 
 
@@ -380,12 +481,19 @@ def Counts(alignment, tree, model, f81_fast=False, branch_mask="auto"):
     A = len(model['pi'])
     if isinstance(branch_mask, str) and branch_mask == "auto":
         branch_mask = compute_branch_mask(alignment, tree.parentIndex, A)
-    M = compute_sub_matrices(model, tree.distanceToParent)
+    if is_irrev(model) and f81_fast:
+        raise ValueError("the F81 fast path is reversible-only")
+    M = _sub_matrices(model, tree.distanceToParent)
     U, lnU, lnL = upward_pass(alignment, tree, M, model['pi'])
     D, lnD = downward_pass(U, lnU, tree, M, model['pi'], alignment)
     if f81_fast:
         return f81_counts(U, D, lnU, lnD, lnL, tree.distanceToParent, model['pi'],
                           tree.parentIndex, branch_mask=branch_mask)
+    if is_irrev(model):
+        J = compute_J_complex(model['eigenvalues'], tree.distanceToParent)
+        Ut, Dt = eigenbasis_project_irrev(U, D, model)
+        return back_transform_irrev(
+            accumulate_C_complex(Dt, Ut, J, lnU, lnD, lnL, tree.parentIndex, branch_mask=branch_mask), model)
     J = compute_J(model['eigenvalues'], tree.distanceToParent)
     Ut, Dt = eigenbasis_project(U, D, model)
     Ceig = accumulate_C(Dt, Ut, J, lnU, lnD, lnL, tree.parentIndex, branch_mask=branch_mask)
@@ -399,12 +507,20 @@ def BranchCounts(alignment, tree, model, f81_fast=False, branch_mask=None):
     A = len(model['pi'])
     if isinstance(branch_mask, str) and branch_mask == "auto":
         branch_mask = compute_branch_mask(alignment, tree.parentIndex, A)
-    M = compute_sub_matrices(model, tree.distanceToParent)
+    if is_irrev(model) and f81_fast:
+        raise ValueError("the F81 fast path is reversible-only")
+    M = _sub_matrices(model, tree.distanceToParent)
     U, lnU, lnL = upward_pass(alignment, tree, M, model['pi'])
     D, lnD = downward_pass(U, lnU, tree, M, model['pi'], alignment)
     if f81_fast:
         return f81_counts_per_branch(U, D, lnU, lnD, lnL, tree.distanceToParent, model['pi'],
                                      tree.parentIndex, branch_mask=branch_mask)
+    if is_irrev(model):
+        J = compute_J_complex(model['eigenvalues'], tree.distanceToParent)
+        Ut, Dt = eigenbasis_project_irrev(U, D, model)
+        return back_transform_irrev_per_branch(
+            accumulate_C_complex_per_branch(Dt, Ut, J, lnU, lnD, lnL, tree.parentIndex,
+                                            branch_mask=branch_mask), model)
     J = compute_J(model['eigenvalues'], tree.distanceToParent)
     Ut, Dt = eigenbasis_project(U, D, model)
     return back_transform_per_branch(
@@ -413,16 +529,23 @@ def BranchCounts(alignment, tree, model, f81_fast=False, branch_mask=None):
 
 def RootProb(alignment, tree, model):
     """(A, C) root posterior pi_a U_root,a e^{lnU_root - lnL}; oracle.py:1571-1595."""
-    M = compute_sub_matrices(model, tree.distanceToParent)
+    M = _sub_matrices(model, tree.distanceToParent)
     U, lnU, lnL = upward_pass(alignment, tree, M, model['pi'])
     scale = np.exp(lnU[0] - lnL)
     return (np.asarray(model['pi'])[None, :] * U[0] * scale[:, None]).T
 
 
+def _sub_matrices(model, distances):
+    """oracle.py:1447-1451: the irreversible M(t) for irreversible models."""
+    if is_irrev(model):
+        return compute_sub_matrices_irrev(model, distances)
+    return compute_sub_matrices(model, distances)
+
+
 def _inside_outside(alignment, tree, model):
     """U, D, scales and M with the root's outside vector set to pi / max(pi),
     as InsideOutside.__init__ does (oracle.py:1631-1661)."""
-    M = compute_sub_matrices(model, tree.distanceToParent)
+    M = _sub_matrices(model, tree.distanceToParent)
     U, lnU, lnL = upward_pass(alignment, tree, M, model['pi'])
     D, lnD = downward_pass(U, lnU, tree, M, model['pi'], alignment)
     pi = np.asarray(model['pi'], dtype=np.float64)

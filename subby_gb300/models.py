@@ -11,12 +11,17 @@ The eigendecomposition stays in FP64 on the host, as in the reference
 
 ``reversible_rate_matrix`` / ``random_reversible`` build the synthetic
 general-reversible models used for the A=16/20/64 workloads.
+
+Irreversible models: ``irrev_model_from_rate_matrix`` /
+``diagonalize_irreversible`` (subby/jax/diagonalize.py:49-138; oracle
+subby/oracle/oracle.py:265-301: numpy ``eig`` and ``inv`` in complex128) and
+``random_irreversible`` (synthetic, with complex eigenvalue pairs).
 """
 from __future__ import annotations
 
 import numpy as np
 
-from .types import DiagModel, RateModel
+from .types import DiagModel, IrrevDiagModel, RateModel
 
 
 def hky85_diag(kappa: float, pi) -> DiagModel:
@@ -61,18 +66,68 @@ def diagonalize_rate_matrix(subRate, rootProb) -> DiagModel:
     return DiagModel(evals, evecs, pi)
 
 
-def ensure_diag(model) -> DiagModel:
-    """RateModel -> DiagModel (subby/jax/__init__.py:44-50); DiagModel as is."""
+def diagonalize_irreversible(subRate, rootProb) -> IrrevDiagModel:
+    """R = V diag(mu) V^-1 in complex128 (numpy eig, inv)."""
+    subRate = np.asarray(subRate, dtype=np.float64)
+    mu, V = np.linalg.eig(subRate)
+    return IrrevDiagModel(mu.astype(np.complex128), V.astype(np.complex128),
+                          np.linalg.inv(V).astype(np.complex128), np.asarray(rootProb, dtype=np.float64))
+
+
+def irrev_model_from_rate_matrix(subRate, pi) -> IrrevDiagModel:
+    return diagonalize_irreversible(subRate, pi)
+
+
+def stationary_distribution(subRate) -> np.ndarray:
+    """pi with pi^T R = 0, sum 1 (FP64)."""
+    subRate = np.asarray(subRate, dtype=np.float64)
+    A = subRate.shape[0]
+    M = np.vstack([subRate.T, np.ones(A)])
+    b = np.zeros(A + 1)
+    b[-1] = 1.0
+    return np.linalg.lstsq(M, b, rcond=None)[0]
+
+
+def random_irreversible(A: int, rng: np.random.Generator, cycle: float = 2.0) -> IrrevDiagModel:
+    """Random irreversible rate matrix with a strong cyclic component
+    (state a -> a+1 mod A), which gives complex eigenvalue pairs; pi is its
+    stationary distribution; normalised to one expected substitution per
+    unit time."""
+    Q = rng.uniform(0.05, 1.0, size=(A, A))
+    for a in range(A):
+        Q[a, (a + 1) % A] += cycle
+    np.fill_diagonal(Q, 0.0)
+    np.fill_diagonal(Q, -Q.sum(axis=1))
+    pi = stationary_distribution(Q)
+    Q /= -np.sum(pi * np.diag(Q))
+    return irrev_model_from_rate_matrix(Q, pi)
+
+
+def is_irrev(model) -> bool:
+    return isinstance(model, IrrevDiagModel) or hasattr(model, 'eigenvectors_inv') or (
+        isinstance(model, dict) and ('eigenvectors_inv' in model or model.get('reversible', True) is False))
+
+
+def ensure_diag(model):
+    """RateModel -> DiagModel (subby/jax/__init__.py:44-50); DiagModel and
+    IrrevDiagModel as they are (dicts with 'eigenvectors_inv' become
+    IrrevDiagModel)."""
     if isinstance(model, RateModel):
         return diagonalize_rate_matrix(model.subRate, model.rootProb)
+    if isinstance(model, (DiagModel, IrrevDiagModel)):
+        return model
     if isinstance(model, dict):
+        if 'eigenvectors_inv' in model:
+            return IrrevDiagModel(np.asarray(model['eigenvalues'], np.complex128),
+                                  np.asarray(model['eigenvectors'], np.complex128),
+                                  np.asarray(model['eigenvectors_inv'], np.complex128), np.asarray(model['pi']))
         return DiagModel(np.asarray(model['eigenvalues']), np.asarray(model['eigenvectors']),
                          np.asarray(model['pi']))
-    if isinstance(model, DiagModel):
-        return model
     if hasattr(model, 'eigenvalues') and hasattr(model, 'eigenvectors') and hasattr(model, 'pi'):
         if hasattr(model, 'eigenvectors_inv'):
-            raise NotImplementedError("irreversible (complex) models are not supported")
+            return IrrevDiagModel(np.asarray(model.eigenvalues, np.complex128),
+                                  np.asarray(model.eigenvectors, np.complex128),
+                                  np.asarray(model.eigenvectors_inv, np.complex128), np.asarray(model.pi))
         return DiagModel(np.asarray(model.eigenvalues), np.asarray(model.eigenvectors),
                          np.asarray(model.pi))
     raise TypeError(f"unsupported model type {type(model).__name__}")

@@ -9,6 +9,9 @@ They mirror subby's own NamedTuples so that code written against
 * ``DiagModel`` — subby/jax/types.py:8-11: ``eigenvalues`` (A,),
   ``eigenvectors`` (A, A) with ``v[a, k]`` = component a of eigenvector k of
   the symmetrised rate matrix, ``pi`` (A,).
+* ``IrrevDiagModel`` — subby/jax/types.py:14-18: complex ``eigenvalues``
+  (A,), right eigenvectors ``eigenvectors`` V (A, A), ``eigenvectors_inv``
+  V^-1 (A, A), real ``pi`` (A,) (root distribution).
 * ``RateModel`` — subby/jax/types.py:21-23: ``subRate`` (A, A), ``rootProb``
   (A,); diagonalised on the host on entry (subby/jax/__init__.py:44-50).
 """
@@ -27,6 +30,13 @@ class Tree(NamedTuple):
 class DiagModel(NamedTuple):
     eigenvalues: np.ndarray
     eigenvectors: np.ndarray
+    pi: np.ndarray
+
+
+class IrrevDiagModel(NamedTuple):
+    eigenvalues: np.ndarray
+    eigenvectors: np.ndarray
+    eigenvectors_inv: np.ndarray
     pi: np.ndarray
 
 

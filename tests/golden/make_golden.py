@@ -12,7 +12,8 @@ and runs it on
   7node_jc64), and
 * seeded synthetic cases of this repository (plain_small column subsets,
   legacy -1 gaps, F81 with non-uniform pi, zero-length branches, random
-  reversible A=16 / A=20 models with near-degenerate eigenvalue pairs),
+  reversible A=16 / A=20 models with near-degenerate eigenvalue pairs,
+  irreversible A=4 / 8 / 16 models with complex eigenvalue pairs),
 
 and writes one ``.npz`` per case holding the inputs, the reference oracle's
 outputs (logLike, unmasked and Steiner-masked Counts, F81 fast-path Counts
@@ -45,12 +46,21 @@ def run_case(oracle, RTree, name, alignment, parent, dist, model, f81_ok,
     alignment = np.asarray(alignment, dtype=np.int32)
     parent = np.asarray(parent, dtype=np.int32)
     dist = np.asarray(dist, dtype=np.float64)
-    m = {k: np.asarray(model[k], dtype=np.float64) for k in ('eigenvalues', 'eigenvectors', 'pi')}
+    if 'eigenvectors_inv' in model:
+        # irreversible: complex eigensystem (subby/oracle/oracle.py:265-301)
+        m = {k: np.asarray(model[k], dtype=np.complex128) for k in ('eigenvalues', 'eigenvectors',
+                                                                   'eigenvectors_inv')}
+        m['pi'] = np.asarray(model['pi'], dtype=np.float64)
+        m['reversible'] = False
+    else:
+        m = {k: np.asarray(model[k], dtype=np.float64) for k in ('eigenvalues', 'eigenvectors', 'pi')}
     tree = RTree(parentIndex=parent, distanceToParent=dist)
     A = len(m['pi'])
     out = dict(alignment=alignment, parentIndex=parent, distanceToParent=dist,
                eigenvalues=m['eigenvalues'], eigenvectors=m['eigenvectors'], pi=m['pi'],
                A=np.int64(A))
+    if 'eigenvectors_inv' in m:
+        out['eigenvectors_inv'] = m['eigenvectors_inv']
     out['logLike'] = oracle.LogLike(alignment, tree, m)
     out['counts'] = oracle.Counts(alignment, tree, m, branch_mask=None)
     if masked:
@@ -147,6 +157,18 @@ def main():
         tr = synth.random_tree(L, 0.1, rng)
         aln = synth.simulated_alignment(tr, m, C, 0.1, rng)
         run_case(oracle, RTree, f"reversible_{A}", aln, tr.parentIndex, tr.distanceToParent,
+                 m._asdict(), False)
+
+    # irreversible models with complex eigenvalue pairs (cyclic rate
+    # component), A = 4, 8 and 16; gaps and unobserved cells included
+    for A, L, C, seed in [(4, 8, 24, 17), (8, 6, 10, 18), (16, 5, 4, 19)]:
+        rng = np.random.default_rng(seed)
+        m = models.random_irreversible(A, rng)
+        tr = synth.random_tree(L, 0.2, rng)
+        R = len(tr.parentIndex)
+        aln = rng.integers(0, A + 2, size=(R, C)).astype(np.int32)
+        aln[:, 0] = A + 1
+        run_case(oracle, RTree, f"irrev_{A}", aln, tr.parentIndex, tr.distanceToParent,
                  m._asdict(), False)
 
 

@@ -40,7 +40,7 @@ def _assert_bc(got, ref, what):
 
 
 def _model(g):
-    return sg.DiagModel(g['eigenvalues'], g['eigenvectors'], g['pi'])
+    return sg.models.ensure_diag(_golden.model_dict(g))
 
 
 @pytest.mark.parametrize("name", [n for n in _golden.names() if 'branch_counts' in _golden.load(n)])

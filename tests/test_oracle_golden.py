@@ -23,7 +23,7 @@ def _tree(g):
 
 
 def _model(g):
-    return {'eigenvalues': g['eigenvalues'], 'eigenvectors': g['eigenvectors'], 'pi': g['pi']}
+    return _golden.model_dict(g)
 
 
 @pytest.mark.parametrize("name", CASES)

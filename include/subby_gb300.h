@@ -89,6 +89,21 @@ const char *subby_last_error(void);
 int subby_plan_create(const int32_t *parent_index, const double *distances,
                       const double *eigenvalues, const double *eigenvectors,
                       const double *pi, int R, int A, subby_plan **out);
+/*
+ * The same for an irreversible model (subby.jax IrrevDiagModel,
+ * subby/jax/types.py:14-18): eigenvalues (A complex), eigenvectors V and
+ * eigenvectors_inv V^-1 (A x A complex, row-major), each complex value as
+ * two doubles (re, im) — the memory layout of numpy complex128.  M(t) =
+ * Re V diag(e^{mu t}) V^-1 and the complex J(t) are formed in FP64 on the
+ * host (subby/oracle/oracle.py:474-534).  LogLike, RootProb, posteriors,
+ * Counts and per-branch counts (complex accumulation and back-transform,
+ * oracle.py:537-740) then run on this plan; the F81 fast path and the
+ * gradient return errors (the reference's F81 path is reversible-only).
+ * Counts are implemented for A = 4, 8, 16, 20, 32, 64.
+ */
+int subby_plan_create_irrev(const int32_t *parent_index, const double *distances, const double *eigenvalues,
+                            const double *eigenvectors, const double *eigenvectors_inv, const double *pi, int R,
+                            int A, subby_plan **out);
 int subby_plan_destroy(subby_plan *plan);
 /* Bytes of device memory the plan currently holds (tables + workspace). */
 size_t subby_plan_device_bytes(const subby_plan *plan);

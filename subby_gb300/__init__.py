@@ -3,14 +3,16 @@ hot path: Felsenstein inside pass, outside pass, eigenbasis J(t) count
 accumulation (general and F81/JC fast path), per-column LogLike, Counts and
 root posteriors.  Drop-in for the single-model entry points of ``subby.jax``.
 """
-from .types import Tree, DiagModel, RateModel
+from .types import Tree, DiagModel, IrrevDiagModel, RateModel
 from .models import (hky85_diag, jukes_cantor_model, f81_model, diagonalize_rate_matrix,
-                     reversible_rate_matrix, random_reversible)
+                     reversible_rate_matrix, random_reversible, irrev_model_from_rate_matrix,
+                     diagonalize_irreversible)
 from .api import (LogLike, Counts, BranchCounts, RootProb, LogLikeCustomGrad, InsideOutside, Plan, get_plan,
                   clear_plan_cache)
 from . import _lib
 
-__all__ = ["BranchCounts", "Tree", "DiagModel", "RateModel", "hky85_diag", "jukes_cantor_model", "f81_model",
+__all__ = ["BranchCounts", "Tree", "DiagModel", "IrrevDiagModel", "RateModel", "irrev_model_from_rate_matrix",
+           "diagonalize_irreversible", "hky85_diag", "jukes_cantor_model", "f81_model",
            "diagonalize_rate_matrix", "reversible_rate_matrix", "random_reversible", "LogLike",
            "Counts", "RootProb", "LogLikeCustomGrad", "InsideOutside", "Plan", "get_plan", "clear_plan_cache"]
 

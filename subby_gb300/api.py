@@ -9,9 +9,11 @@ Inputs may be numpy arrays (results come back as numpy float32, copies in
 and out are part of the call) or CUDA ``torch`` tensors (results stay on the
 device as torch tensors, work is enqueued on the current torch stream).
 
-Not supported (raise ``NotImplementedError``): per-column model lists and
-model grids (subby/jax/__init__.py:53-205), irreversible complex models
-(``IrrevDiagModel``), and ``*H`` batch dimensions.
+Irreversible models (``IrrevDiagModel``, complex eigensystem) are accepted
+by every entry point except the F81 fast path (reversible-only in the
+reference too) and the gradient.  Not supported (raise
+``NotImplementedError``): per-column model lists and model grids
+(subby/jax/__init__.py:53-205) and ``*H`` batch dimensions.
 """
 from __future__ import annotations
 
@@ -24,7 +26,7 @@ import numpy as np
 
 from . import _lib
 from .models import ensure_diag
-from .types import Tree
+from .types import IrrevDiagModel, Tree
 
 _PLAN_CACHE_SIZE = 32
 
@@ -60,11 +62,17 @@ class Plan:
         m = ensure_diag(model)
         self.parentIndex = _np(tree.parentIndex, np.int32)
         self.distances = _np(tree.distanceToParent, np.float64)
-        self.eigenvalues = _np(m.eigenvalues, np.float64)
-        self.eigenvectors = _np(m.eigenvectors, np.float64)
+        self.irreversible = isinstance(m, IrrevDiagModel)
+        if self.irreversible:
+            self.eigenvalues = _np(m.eigenvalues, np.complex128)
+            self.eigenvectors = _np(m.eigenvectors, np.complex128)
+            self.eigenvectors_inv = _np(m.eigenvectors_inv, np.complex128)
+        else:
+            if np.iscomplexobj(m.eigenvalues) or np.iscomplexobj(m.eigenvectors):
+                raise ValueError("complex eigensystems need an IrrevDiagModel (with eigenvectors_inv)")
+            self.eigenvalues = _np(m.eigenvalues, np.float64)
+            self.eigenvectors = _np(m.eigenvectors, np.float64)
         self.pi = _np(m.pi, np.float64)
-        if np.iscomplexobj(m.eigenvalues) or np.iscomplexobj(m.eigenvectors):
-            raise NotImplementedError("irreversible (complex) models are not supported")
         self.R = int(self.parentIndex.shape[0])
         self.A = int(self.pi.shape[0])
         if self.distances.shape != (self.R,):
@@ -75,10 +83,18 @@ class Plan:
         self._handle = ct.c_void_p()
         self._lock = threading.Lock()
         with _device_ctx(device):
-            _lib.check(lib.subby_plan_create(
-                _ptr(self.parentIndex), _ptr(self.distances), _ptr(self.eigenvalues),
-                _ptr(self.eigenvectors), _ptr(self.pi), self.R, self.A, ct.byref(self._handle)),
-                "subby_plan_create")
+            if self.irreversible:
+                if self.eigenvectors_inv.shape != (self.A, self.A):
+                    raise ValueError("eigenvectors_inv must have shape (A, A)")
+                _lib.check(lib.subby_plan_create_irrev(
+                    _ptr(self.parentIndex), _ptr(self.distances), _ptr(self.eigenvalues),
+                    _ptr(self.eigenvectors), _ptr(self.eigenvectors_inv), _ptr(self.pi), self.R, self.A,
+                    ct.byref(self._handle)), "subby_plan_create_irrev")
+            else:
+                _lib.check(lib.subby_plan_create(
+                    _ptr(self.parentIndex), _ptr(self.distances), _ptr(self.eigenvalues),
+                    _ptr(self.eigenvectors), _ptr(self.pi), self.R, self.A, ct.byref(self._handle)),
+                    "subby_plan_create")
 
     # ------------------------------------------------------------------ run
     def run(self, alignment, loglike=True, counts=False, rootprob=False, f81=False,
@@ -337,8 +353,11 @@ _cache_lock = threading.Lock()
 
 def _key(tree, model, device):
     h = hashlib.sha1()
-    for a in (tree.parentIndex, tree.distanceToParent, model.eigenvalues, model.eigenvectors, model.pi):
-        arr = np.ascontiguousarray(_np(a, np.float64))
+    parts = [tree.parentIndex, tree.distanceToParent, model.eigenvalues, model.eigenvectors, model.pi]
+    if isinstance(model, IrrevDiagModel):
+        parts.append(model.eigenvectors_inv)
+    for a in parts:
+        arr = np.ascontiguousarray(_np(a, np.complex128 if np.iscomplexobj(a) else np.float64))
         h.update(arr.tobytes())
         h.update(str(arr.shape).encode())
     h.update(str(device).encode())

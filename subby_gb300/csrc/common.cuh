@@ -107,6 +107,8 @@ struct KParams {
   // branch joint posteriors (k_tree4, A = 4): (R, 4, 4, C) or the (4, 4, C)
   // of node npost_node
   float *bpost;
+  // irreversible models: complex J (R x A x A), V, Vinv, rate matrix (A x A)
+  const float2 *cx;
 };
 
 // launchers (k_small.cu / k_warp.cu)
@@ -139,6 +141,12 @@ int launch_acc(const KParams &p, int A, bool f81, bool tc, const float *sa, cons
                int c_count, int grid, cudaStream_t s);
 int launch_tree4(const KParams &p, bool f81, int mask_mode, int grid, int block, size_t smem,
                  cudaStream_t s);
+// irreversible counts (k_acccx.cu): complex accumulation + back-transform
+// over the walk's raw staging; pb: per-branch counts
+bool cx_supported(int A);
+int cx_columns_per_cta(int A);
+int launch_acc_cx(const KParams &p, int A, bool pb, const float *sa, const float *sb, int c_base, int c_count,
+                  int grid, cudaStream_t s);
 // A = 4 posteriors (npost / bpost) from the tree-program kernel
 int launch_tree4_post(const KParams &p, int grid, int block, size_t smem, cudaStream_t s);
 // A = 64 F81 accumulation on the tensor cores (k_acctc.cu); groups of 8 columns

@@ -5,6 +5,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <complex>
 #include <cstdlib>
 #include <cstdio>
 #include <cstring>
@@ -240,6 +241,10 @@ struct subby_plan {
   std::vector<double> V, mu, pi;
   float f81_mu = 0.f;
   int f81_model = 0;   // M(t) has the F81 / JC closed form (checked on the host)
+  // irreversible model: M(t) from the complex eigensystem (host FP64), and
+  // the complex tables of the counts (J (R x A x A), V, V^-1, rate matrix)
+  bool irrev = false;
+  float2 *d_cx = nullptr;
   TableOffsets off{};
   float *d_tab = nullptr;
   double *d_tab64 = nullptr;
@@ -317,8 +322,17 @@ int subby_debug_set_kernel(int which) {
 }
 int subby_last_launch_count(void) { return g_launches; }
 
-int subby_plan_create(const int32_t *parent, const double *dist, const double *evals,
-                      const double *evecs, const double *pi, int R, int A, subby_plan **out) {
+}  // extern "C"
+
+namespace {
+
+// Irreversible input: complex eigenvalues, V and V^-1 (interleaved re, im).
+struct IrrevInput {
+  const double *mu, *V, *Vi;
+};
+
+int plan_create(const int32_t *parent, const double *dist, const double *evals, const double *evecs,
+                const double *pi, int R, int A, subby_plan **out, const IrrevInput *ir) {
   g_last_error.clear();
   if (!out || !parent || !dist || !evals || !evecs || !pi) return fail(SUBBY_ERR_ARG, "null argument");
   *out = nullptr;
@@ -337,6 +351,7 @@ int subby_plan_create(const int32_t *parent, const double *dist, const double *e
   auto *P = new subby_plan();
   P->R = R;
   P->A = A;
+  P->irrev = ir != nullptr;
   cudaGetDevice(&P->device);
   cudaDeviceGetAttribute(&P->nsm, cudaDevAttrMultiProcessorCount, P->device);
   P->root_is_leaf = (R == 1);
@@ -461,7 +476,7 @@ int subby_plan_create(const int32_t *parent, const double *dist, const double *e
           worst = std::max(worst, std::fabs(m - f));
         }
     }
-    P->f81_model = std::isfinite(mu81) && worst < 1e-9;
+    P->f81_model = !ir && std::isfinite(mu81) && worst < 1e-9;
   }
 
   TableOffsets &o = P->off;
@@ -571,11 +586,67 @@ int subby_plan_create(const int32_t *parent, const double *dist, const double *e
       e = cudaMemcpyAsync(P->d_prog, P->prog.data(), sizeof(int4) * P->prog.size(), cudaMemcpyHostToDevice, qs);
     if (e != cudaSuccess) return cleanup(cuda_fail(e, "program upload"));
   }
+  std::vector<float> hMT, hMN;
+  std::vector<float2> hcx;
+  if (ir) {
+    // M_n = Re V diag(e^{mu t_n}) V^-1 and the complex tables, in FP64
+    // (subby/oracle/oracle.py:474-534, 642-693)
+    using cd = std::complex<double>;
+    std::vector<cd> mu(A), V((size_t)A * A), Vi((size_t)A * A), E(A), w(A);
+    for (int k = 0; k < A; ++k) mu[k] = cd(ir->mu[2 * k], ir->mu[2 * k + 1]);
+    for (int i = 0; i < A * A; ++i) {
+      V[i] = cd(ir->V[2 * i], ir->V[2 * i + 1]);
+      Vi[i] = cd(ir->Vi[2 * i], ir->Vi[2 * i + 1]);
+    }
+    hMT.assign((size_t)R * (A + 1) * A, 0.f);
+    hMN.assign((size_t)R * A * A, 0.f);
+    hcx.assign((size_t)(R + 3) * A * A, make_float2(0.f, 0.f));
+    for (int n = 0; n < R; ++n) {
+      const double t = dist[n];
+      for (int k = 0; k < A; ++k) E[k] = std::exp(mu[k] * t);
+      for (int b = 0; b < A; ++b) {
+        for (int k = 0; k < A; ++k) w[k] = V[b * A + k] * E[k];
+        double rs = 0.0;
+        for (int j = 0; j < A; ++j) {
+          cd sum = 0.0;
+          for (int k = 0; k < A; ++k) sum += w[k] * Vi[k * A + j];
+          const double m = sum.real();
+          hMT[((size_t)n * (A + 1) + j) * A + b] = (float)m;
+          hMN[((size_t)n * A + b) * A + j] = (float)m;
+          rs += m;
+        }
+        hMT[((size_t)n * (A + 1) + A) * A + b] = (float)rs;
+      }
+      for (int k = 0; k < A; ++k)
+        for (int l = 0; l < A; ++l) {
+          const cd d = mu[k] - mu[l];
+          const cd J = std::abs(d) < 1e-8 ? t * E[k] : (E[k] - E[l]) / d;
+          hcx[((size_t)n * A + k) * A + l] = make_float2((float)J.real(), (float)J.imag());
+        }
+    }
+    float2 *cV = hcx.data() + (size_t)R * A * A, *cVi = cV + A * A, *cR = cVi + A * A;
+    for (int i = 0; i < A; ++i)
+      for (int j = 0; j < A; ++j) {
+        cd r = 0.0;
+        for (int k = 0; k < A; ++k) r += V[i * A + k] * mu[k] * Vi[k * A + j];
+        cV[i * A + j] = make_float2((float)V[i * A + j].real(), (float)V[i * A + j].imag());
+        cVi[i * A + j] = make_float2((float)Vi[i * A + j].real(), (float)Vi[i * A + j].imag());
+        cR[i * A + j] = make_float2((float)r.real(), (float)r.imag());
+      }
+    e = cudaMemcpyAsync(P->d_tab + o.MT, hMT.data(), hMT.size() * sizeof(float), cudaMemcpyHostToDevice, qs);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(P->d_tab + o.MN, hMN.data(), hMN.size() * sizeof(float), cudaMemcpyHostToDevice, qs);
+    if (e == cudaSuccess) e = pool_alloc((void **)&P->d_cx, hcx.size() * sizeof(float2), P->pool, qs);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(P->d_cx, hcx.data(), hcx.size() * sizeof(float2), cudaMemcpyHostToDevice, qs);
+    if (e != cudaSuccess) return cleanup(cuda_fail(e, "irreversible table upload"));
+  }
   {
     const int tm = R * A;
-    k_compute_M<<<std::max(1, std::min((tm + 127) / 128, 4096)), 128, 0, qs>>>(
-        P->d_tab64, P->d_tab64 + 2 * A * A, P->d_tab64 + 2 * A * A + A, P->d_tab64 + 2 * A * A + A + R, R, A,
-        P->d_tab + o.MT, P->d_tab + o.MN);
+    if (!ir)
+      k_compute_M<<<std::max(1, std::min((tm + 127) / 128, 4096)), 128, 0, qs>>>(
+          P->d_tab64, P->d_tab64 + 2 * A * A, P->d_tab64 + 2 * A * A + A, P->d_tab64 + 2 * A * A + A + R, R, A,
+          P->d_tab + o.MT, P->d_tab + o.MN);
     e = cudaGetLastError();
     if (e != cudaSuccess) return cleanup(cuda_fail(e, "M(t) prologue"));
     const int total = R * A * A;
@@ -608,6 +679,35 @@ int subby_plan_create(const int32_t *parent, const double *dist, const double *e
   return SUBBY_OK;
 }
 
+}  // namespace
+
+extern "C" {
+
+int subby_plan_create(const int32_t *parent, const double *dist, const double *evals,
+                      const double *evecs, const double *pi, int R, int A, subby_plan **out) {
+  return plan_create(parent, dist, evals, evecs, pi, R, A, out, nullptr);
+}
+
+int subby_plan_create_irrev(const int32_t *parent, const double *dist, const double *eigenvalues,
+                            const double *eigenvectors, const double *eigenvectors_inv, const double *pi, int R,
+                            int A, subby_plan **out) {
+  g_last_error.clear();
+  if (!eigenvalues || !eigenvectors || !eigenvectors_inv) return fail(SUBBY_ERR_ARG, "null argument");
+  if (!(A >= 2 && A <= 64)) return fail(SUBBY_ERR_UNSUPPORTED, "alphabet size out of range");
+  for (int i = 0; i < 2 * A; ++i)
+    if (!std::isfinite(eigenvalues[i])) return fail(SUBBY_ERR_ARG, "eigenvalues must be finite");
+  for (int i = 0; i < 2 * A * A; ++i)
+    if (!std::isfinite(eigenvectors[i]) || !std::isfinite(eigenvectors_inv[i]))
+      return fail(SUBBY_ERR_ARG, "eigenvectors must be finite");
+  // the real eigensystem slots of the plan get an inert stand-in (zero
+  // rates, identity vectors); M(t) and the count tables come from the
+  // complex eigensystem
+  std::vector<double> ev0((size_t)A, 0.0), eye((size_t)A * A, 0.0);
+  for (int a = 0; a < A; ++a) eye[(size_t)a * A + a] = 1.0;
+  const IrrevInput ir{eigenvalues, eigenvectors, eigenvectors_inv};
+  return plan_create(parent, dist, ev0.data(), eye.data(), pi, R, A, out, &ir);
+}
+
 int subby_plan_destroy(subby_plan *P) {
   if (!P) return SUBBY_OK;
   int cur = 0;
@@ -619,7 +719,7 @@ int subby_plan_destroy(subby_plan *P) {
   if (s && P->used) cudaStreamWaitEvent(s, P->last_use, 0);
   if (P->s_in) cudaStreamSynchronize(P->s_in);
   if (P->s_out) cudaStreamSynchronize(P->s_out);
-  void *bufs[] = {P->d_tab, P->d_tab64, P->d_steps, P->d_slots, P->d_prog, P->d_tab16, P->d_err};
+  void *bufs[] = {P->d_tab, P->d_tab64, P->d_steps, P->d_slots, P->d_prog, P->d_tab16, P->d_err, P->d_cx};
   for (void *b : bufs)
     if (b) cudaFreeAsync(b, s);
   P->work.release(s);
@@ -1085,6 +1185,69 @@ int run_post(subby_plan *P, const int32_t *d_aln, int C, int node, float *d_node
   return mark_use(P, stream);
 }
 
+// Irreversible models, Counts / BranchCounts: the walk (mode 3) stages
+// D_n s_n and U_n in the raw basis (LogLike / RootProb from its inside
+// pass), k_acc_cx does the complex accumulation and back-transform.
+int run_cx(subby_plan *P, const int32_t *d_aln, int C, float *d_logL, float *d_counts, float *d_root, int mode,
+           int mask_mode, const uint8_t *d_mask, cudaStream_t stream) {
+  const int A = P->A, R = P->R;
+  if (!cx_supported(A) || !post_supported(A))
+    return fail(SUBBY_ERR_UNSUPPORTED, "irreversible counts are implemented for A = 4, 8, 16, 20, 32, 64");
+  if (mode & kModeF81) return fail(SUBBY_ERR_ARG, "the F81 fast path is reversible-only");
+  const bool pb = (mode & kModeBranch) != 0;
+  const bool counts = R > 1;
+  if (!counts && !pb) CU(cudaMemsetAsync(d_counts, 0, (size_t)A * A * C * sizeof(float), stream));
+  KParams k = walk_params(P, d_aln, C, mode & (kModeLogLike | kModeRootProb), mask_mode, d_mask, d_logL, d_counts,
+                          d_root);
+  k.cx = P->d_cx;
+  k.npost = nullptr;
+  k.npost_node = -1;
+  const bool tc = (A == 64) && P->d_tab16 && (g_kernel_sel == 0 || g_kernel_sel == 5);
+  const int tile = big_tile();
+  const int H = (A + 31) / 32;
+  int chunk = C;
+  if (counts) {
+    const size_t per_col = (size_t)2 * (R - 1) * A * sizeof(float);
+    size_t cmax = std::max<size_t>(tile, kStageBudget / per_col);
+    cmax = cmax / tile * tile;
+    const size_t nch = ((size_t)C + cmax - 1) / cmax;
+    const size_t even = ((size_t)C + nch - 1) / nch;
+    chunk = (int)std::min<size_t>((size_t)C, (even + tile - 1) / tile * tile);
+  }
+  const int per_sm = A <= 8 ? 8 : (H == 2 ? 1 : 2);
+  const int walk_grid = std::max(1, std::min((chunk + tile - 1) / tile, P->nsm * per_sm));
+  const size_t slot_floats = (size_t)walk_grid * k.nslots * tile * A;
+  const size_t slot_ints = (size_t)walk_grid * k.nslots * tile;
+  const size_t stage_floats = counts ? (size_t)(R - 1) * chunk * A : 0;
+  auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
+  int rc;
+  if ((rc = P->grow(P->work, al(slot_floats * 4) + al(slot_ints * 4) + 2 * al(stage_floats * 4) + 256, stream)))
+    return rc;
+  char *base = (char *)P->work.p;
+  k.scrV = (float *)base;
+  base += al(slot_floats * 4);
+  k.scrW = (int *)base;
+  base += al(slot_ints * 4);
+  float *sa = counts ? (float *)base : nullptr;
+  base += al(stage_floats * 4);
+  float *sb = counts ? (float *)base : nullptr;
+  const int G = cx_columns_per_cta(A);
+  for (int c0 = 0; c0 < C; c0 += chunk) {
+    const int cc = std::min(chunk, C - c0);
+    int lr = launch_walk_post(k, A, counts ? 3 : 0, tc, sa, sb, c0, cc, walk_grid, stream);
+    if (lr != 0) return fail(SUBBY_ERR_CUDA, std::string("walk launch failed: ") + cudaGetErrorString((cudaError_t)lr));
+    g_launches += 1;
+    if (!counts) continue;
+    const long long groups = (cc + G - 1) / G;
+    const int grid = (int)std::max<long long>(1, std::min<long long>(groups, (long long)P->nsm * 2));
+    lr = launch_acc_cx(k, A, pb, sa, sb, c0, cc, grid, stream);
+    if (lr != 0)
+      return fail(SUBBY_ERR_CUDA, std::string("accumulate launch failed: ") + cudaGetErrorString((cudaError_t)lr));
+    g_launches += 1;
+  }
+  return mark_use(P, stream);
+}
+
 // Columns per chunk of the host-pointer pipeline: whole waves of the
 // one-CTA-per-SM kernels (nsm x 256 columns), about eight chunks for large C,
 // a single chunk below two waves (nothing to overlap).
@@ -1110,6 +1273,11 @@ int ensure_pipeline(subby_plan *P, int nev) {
 int run_common(subby_plan *P, const int32_t *d_aln, int C, float *d_logL, float *d_counts,
                float *d_root, int mode, int mask_mode, const uint8_t *d_mask, const float *d_g,
                double *d_gt, double *d_gC, int *grid_out, cudaStream_t stream) {
+  if (P->irrev) {
+    if (mode & kModeGrad) return fail(SUBBY_ERR_UNSUPPORTED, "gradients of irreversible models are not implemented");
+    if (mode & kModeCounts)
+      return run_cx(P, d_aln, C, d_logL, d_counts, d_root, mode, mask_mode, d_mask, stream);
+  }
   if (mode & kModeBranch) {
     // per-branch counts: the A = 4 tree-program kernel, or the large-alphabet
     // walk with the per-branch accumulation

@@ -65,6 +65,13 @@ def random_tree(n_leaves: int, mean_branch: float, rng: np.random.Generator) -> 
 
 
 def sub_matrices64(model: DiagModel, distances) -> np.ndarray:
+    if hasattr(model, 'eigenvectors_inv'):
+        # irreversible: M = Re V diag(e^{mu t}) V^-1
+        V = np.asarray(model.eigenvectors, dtype=np.complex128)
+        Vi = np.asarray(model.eigenvectors_inv, dtype=np.complex128)
+        E = np.exp(np.asarray(model.eigenvalues, np.complex128)[None, :] * np.asarray(distances)[:, None])
+        M = np.maximum(np.einsum('ik,rk,kj->rij', V, E, Vi).real, 0.0)
+        return M / M.sum(axis=-1, keepdims=True)
     V = np.asarray(model.eigenvectors, dtype=np.float64)
     mu = np.asarray(model.eigenvalues, dtype=np.float64)
     sp = np.sqrt(np.asarray(model.pi, dtype=np.float64))

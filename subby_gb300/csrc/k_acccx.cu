@@ -66,6 +66,7 @@ __global__ void __launch_bounds__(kCxThreads) k_acc_cx(const KParams P, const fl
     sV[e] = Vg[e];
     sVi[e] = Vig[e];
   }
+  __syncthreads();  // V, Vinv visible to every thread before the first projection
   const bool busy = t < Gm::THREADS;
   const int g = busy ? t / TPC : 0, p = busy ? t % TPC : 0;
   const int ngroups = (c_count + G - 1) / G;

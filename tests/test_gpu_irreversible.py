@@ -66,8 +66,9 @@ def test_golden_irreversible(name):
     assert_cols(res['rootProb'], g['root_prob'], ROOTPROB_RTOL, name + " rootProb")
     assert_cols(plan.run(aln, loglike=False, counts=True)['counts'], g['counts_masked'], COUNTS_RTOL,
                 name + " counts masked")
-    assert_cols(_per_branch(plan.branch_counts(aln)), _per_branch(g['branch_counts']), COUNTS_RTOL,
-                name + " branch counts")
+    if 'branch_counts' in g:
+        assert_cols(_per_branch(plan.branch_counts(aln)), _per_branch(g['branch_counts']), COUNTS_RTOL,
+                    name + " branch counts")
     post = plan.posteriors(aln, want_node=True, want_branch=True)
     assert_cols(_nodes(post['node']), _nodes(g['node_posterior']), POSTERIOR_RTOL, name + " node post")
     assert_cols(_nodes(post['branch']), _nodes(g['branch_posterior']), POSTERIOR_RTOL, name + " branch post")

@@ -59,6 +59,9 @@ extern "C" {
 #define SUBBY_DEVICE_PTRS   1      /* alignment/mask/outputs are device pointers */
 #define SUBBY_BT_FP32       2      /* back-transform in FP32 (default: FP64 for A <= 8) */
 #define SUBBY_BT_FP64       4      /* force FP64 back-transform for any A          */
+#define SUBBY_IRREV_EXACT   8      /* irreversible models: counts of M(t) = e^{Qt}
+                                      itself (D~ = D V, U~ = V^-1 U, V^-T C V^T)
+                                      instead of the reference's formula       */
 
 /* mask_mode */
 #define SUBBY_MASK_NONE   0        /* every branch n >= 1 counts                 */

@@ -218,7 +218,26 @@ def _rate_irrev(model):
     V = np.asarray(model['eigenvectors'], dtype=np.complex128)
     Vi = np.asarray(model['eigenvectors_inv'], dtype=np.complex128)
     mu = np.asarray(model['eigenvalues'], dtype=np.complex128)
+    if model.get('_exact'):
+        # rate matrix of the original model; the vectors are swapped below
+        V0, Vi0 = Vi.T, V.T
+        return V, Vi, (V0 * mu[None, :]) @ Vi0
     return V, Vi, (V * mu[None, :]) @ Vi
+
+
+def irrev_exact_model(model):
+    """The model dict whose reference-formula counts are the expected counts
+    of M(t) = e^{Qt} itself: (V, Vinv) replaced by (Vinv^T, V^T), so that
+    D~ = D V, U~ = Vinv U and the back-transform is Vinv^T C V^T, with the
+    off-diagonal factor still Q.  (For non-reversible Q the reference's
+    formula, oracle.py:537-693, gives the counts of the transposed process;
+    tests/test_irrev_math.py checks both against quadrature.)"""
+    m = dict(model)
+    m['eigenvectors'] = np.asarray(model['eigenvectors_inv'], dtype=np.complex128).T
+    m['eigenvectors_inv'] = np.asarray(model['eigenvectors'], dtype=np.complex128).T
+    m['_exact'] = True
+    m['reversible'] = False
+    return m
 
 
 def back_transform_irrev(Ceig, model):
@@ -476,7 +495,7 @@ def LogLike(alignment, tree, model):
     return upward_pass(alignment, tree, M, model['pi'])[2]
 
 
-def Counts(alignment, tree, model, f81_fast=False, branch_mask="auto"):
+def Counts(alignment, tree, model, f81_fast=False, branch_mask="auto", irrev_exact=False):
     """(A, A, C) dwell (diag) + substitution (off-diag) counts; oracle.py:1470-1514."""
     A = len(model['pi'])
     if isinstance(branch_mask, str) and branch_mask == "auto":
@@ -490,17 +509,18 @@ def Counts(alignment, tree, model, f81_fast=False, branch_mask="auto"):
         return f81_counts(U, D, lnU, lnD, lnL, tree.distanceToParent, model['pi'],
                           tree.parentIndex, branch_mask=branch_mask)
     if is_irrev(model):
+        mp = irrev_exact_model(model) if irrev_exact else model
         J = compute_J_complex(model['eigenvalues'], tree.distanceToParent)
-        Ut, Dt = eigenbasis_project_irrev(U, D, model)
+        Ut, Dt = eigenbasis_project_irrev(U, D, mp)
         return back_transform_irrev(
-            accumulate_C_complex(Dt, Ut, J, lnU, lnD, lnL, tree.parentIndex, branch_mask=branch_mask), model)
+            accumulate_C_complex(Dt, Ut, J, lnU, lnD, lnL, tree.parentIndex, branch_mask=branch_mask), mp)
     J = compute_J(model['eigenvalues'], tree.distanceToParent)
     Ut, Dt = eigenbasis_project(U, D, model)
     Ceig = accumulate_C(Dt, Ut, J, lnU, lnD, lnL, tree.parentIndex, branch_mask=branch_mask)
     return back_transform(Ceig, model)
 
 
-def BranchCounts(alignment, tree, model, f81_fast=False, branch_mask=None):
+def BranchCounts(alignment, tree, model, f81_fast=False, branch_mask=None, irrev_exact=False):
     """(R, A, A, C) per-branch dwell/substitution counts, branch 0 zero;
     oracle.py:1517-1568.  The default mask is None, as in subby.jax.BranchCounts
     (subby/jax/__init__.py:450-540), which does not mask."""
@@ -516,11 +536,12 @@ def BranchCounts(alignment, tree, model, f81_fast=False, branch_mask=None):
         return f81_counts_per_branch(U, D, lnU, lnD, lnL, tree.distanceToParent, model['pi'],
                                      tree.parentIndex, branch_mask=branch_mask)
     if is_irrev(model):
+        mp = irrev_exact_model(model) if irrev_exact else model
         J = compute_J_complex(model['eigenvalues'], tree.distanceToParent)
-        Ut, Dt = eigenbasis_project_irrev(U, D, model)
+        Ut, Dt = eigenbasis_project_irrev(U, D, mp)
         return back_transform_irrev_per_branch(
             accumulate_C_complex_per_branch(Dt, Ut, J, lnU, lnD, lnL, tree.parentIndex,
-                                            branch_mask=branch_mask), model)
+                                            branch_mask=branch_mask), mp)
     J = compute_J(model['eigenvalues'], tree.distanceToParent)
     Ut, Dt = eigenbasis_project(U, D, model)
     return back_transform_per_branch(

@@ -13,7 +13,7 @@ from . import _build
 
 OK = 0
 ERR_ARG, ERR_TREE, ERR_UNSUPPORTED, ERR_CUDA, ERR_NOMEM, ERR_TIMEOUT = -1, -2, -3, -4, -5, -6
-DEVICE_PTRS, BT_FP32, BT_FP64 = 1, 2, 4
+DEVICE_PTRS, BT_FP32, BT_FP64, IRREV_EXACT = 1, 2, 4, 8
 MASK_NONE, MASK_AUTO, MASK_GIVEN = 0, 1, 2
 COUNTS_EIGEN, COUNTS_F81 = 0, 1
 

@@ -98,11 +98,14 @@ class Plan:
 
     # ------------------------------------------------------------------ run
     def run(self, alignment, loglike=True, counts=False, rootprob=False, f81=False,
-            branch_mask="auto", bt64=None, out=None, stream=None):
+            branch_mask="auto", bt64=None, out=None, stream=None, exact_irreversible=False):
         """Run the hot path; returns a dict with the requested outputs.
 
         ``branch_mask``: "auto" (Steiner mask, the reference default for
-        Counts), None (unmasked) or an (R, C) bool array.  ``bt64``: None =
+        Counts), None (unmasked) or an (R, C) bool array.  ``exact_irreversible``
+        (irreversible models only): the expected counts of M(t) = e^{Qt}
+        itself instead of the reference's formula, which for a non-reversible
+        Q gives those of the transposed process.  ``bt64``: None =
         FP64 back-transform for A <= 8 and FP32 above; True/False forces it.
         ``out``: optional dict of preallocated output buffers (same keys).
         ``stream``: torch.cuda.Stream for the device-pointer path (default:
@@ -110,7 +113,7 @@ class Plan:
         """
         lib = _lib.load()
         kind = _lib.COUNTS_F81 if f81 else _lib.COUNTS_EIGEN
-        flags = 0
+        flags = _lib.IRREV_EXACT if exact_irreversible else 0
         if bt64 is True:
             flags |= _lib.BT_FP64
         elif bt64 is False:
@@ -187,13 +190,15 @@ class Plan:
                 "subby_plan_run")
         return res
 
-    def branch_counts(self, alignment, f81=False, branch_mask=None, out=None, stream=None):
+    def branch_counts(self, alignment, f81=False, branch_mask=None, out=None, stream=None,
+                      exact_irreversible=False):
         """Per-branch counts (R, A, A, C): dwell times (diagonal) and
         substitution counts (off-diagonal) of every branch (branch 0, the
         root, is zeros).  ``branch_mask`` defaults to None (unmasked), as in
         subby.jax.BranchCounts; "auto" and an (R, C) array are accepted."""
         lib = _lib.load()
         kind = _lib.COUNTS_F81 if f81 else _lib.COUNTS_EIGEN
+        xf = _lib.IRREV_EXACT if exact_irreversible else 0
         if isinstance(branch_mask, str):
             if branch_mask != "auto":
                 raise ValueError('branch_mask must be "auto", None or an (R, C) array')
@@ -218,7 +223,7 @@ class Plan:
             with self._lock, _device_ctx(aln.device):
                 _lib.check(lib.subby_plan_branch_counts(
                     self._handle, ct.c_void_p(aln.data_ptr()), C, ct.c_void_p(res.data_ptr()), kind, mask_mode,
-                    ct.c_void_p(dmask.data_ptr()) if dmask is not None else None, _lib.DEVICE_PTRS,
+                    ct.c_void_p(dmask.data_ptr()) if dmask is not None else None, _lib.DEVICE_PTRS | xf,
                     ct.c_void_p(st)), "subby_plan_branch_counts")
             return res
         aln = _np(alignment, np.int32)
@@ -230,7 +235,7 @@ class Plan:
         with self._lock, _device_ctx(self.device):
             _lib.check(lib.subby_plan_branch_counts(
                 self._handle, _ptr(aln), C, _ptr(res), kind, mask_mode,
-                _ptr(hmask) if hmask is not None else None, 0, None), "subby_plan_branch_counts")
+                _ptr(hmask) if hmask is not None else None, xf, None), "subby_plan_branch_counts")
         return res
 
     def posteriors(self, alignment, node=None, want_node=True, want_branch=False, stream=None):
@@ -406,21 +411,23 @@ def LogLike(alignment, tree: Tree, model, maxChunkSize: int = 128):
 
 
 def Counts(alignment, tree: Tree, model, maxChunkSize: int = 128, f81_fast_flag: bool = False,
-           branch_mask="auto"):
-    """(A, A, C) dwell times (diagonal) and substitution counts; subby/jax/__init__.py:338."""
+           branch_mask="auto", exact_irreversible: bool = False):
+    """(A, A, C) dwell times (diagonal) and substitution counts; subby/jax/__init__.py:338.
+    ``exact_irreversible`` (not in the reference): see ``Plan.run``."""
     del maxChunkSize
     return get_plan(tree, model, _device_of(alignment)).run(
-        alignment, loglike=False, counts=True, f81=f81_fast_flag, branch_mask=branch_mask)['counts']
+        alignment, loglike=False, counts=True, f81=f81_fast_flag, branch_mask=branch_mask,
+        exact_irreversible=exact_irreversible)['counts']
 
 
 def BranchCounts(alignment, tree: Tree, model, maxChunkSize: int = 128, f81_fast_flag: bool = False,
-                 branch_mask=None):
+                 branch_mask=None, exact_irreversible: bool = False):
     """(R, A, A, C) per-branch dwell times and substitution counts, branch 0
     zeros; subby/jax/__init__.py:450 (unmasked there; ``branch_mask`` as in
     the oracle's BranchCounts, subby/oracle/oracle.py:1517)."""
     del maxChunkSize
     return get_plan(tree, model, _device_of(alignment)).branch_counts(
-        alignment, f81=f81_fast_flag, branch_mask=branch_mask)
+        alignment, f81=f81_fast_flag, branch_mask=branch_mask, exact_irreversible=exact_irreversible)
 
 
 def RootProb(alignment, tree: Tree, model, maxChunkSize: int = 128):

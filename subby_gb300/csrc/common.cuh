@@ -23,6 +23,7 @@ enum : int {
   kModeBT64 = 16,        // FP64 back-transform
   kModeGrad = 32,        // gradient accumulation instead of counts output
   kModeBranch = 64,      // per-branch counts (R, A, A, C) instead of their sum
+  kModeIrrevExact = 128, // irreversible counts of M(t) itself, not the reference's formula
 };
 
 enum : int { kMaskNone = 0, kMaskAuto = 1, kMaskGiven = 2 };
@@ -107,8 +108,10 @@ struct KParams {
   // branch joint posteriors (k_tree4, A = 4): (R, 4, 4, C) or the (4, 4, C)
   // of node npost_node
   float *bpost;
-  // irreversible models: complex J (R x A x A), V, Vinv, rate matrix (A x A)
+  // irreversible models: complex tables (k_acccx.cu) and the choice of the
+  // reference's formula (0) or the expected counts of M(t) itself (1)
   const float2 *cx;
+  int cx_exact;
 };
 
 // launchers (k_small.cu / k_warp.cu)
@@ -145,8 +148,11 @@ int launch_tree4(const KParams &p, bool f81, int mask_mode, int grid, int block,
 // over the walk's raw staging; pb: per-branch counts
 bool cx_supported(int A);
 int cx_columns_per_cta(int A);
+bool cx_bt64(int A);  // C buffered and back-transformed in FP64 (k_bt_cx)
 int launch_acc_cx(const KParams &p, int A, bool pb, const float *sa, const float *sb, int c_base, int c_count,
-                  int grid, cudaStream_t s);
+                  int n_lo, int n_hi, float2 *cbuf, int grid, cudaStream_t s);
+int launch_bt_cx(const KParams &p, int A, const float2 *cbuf, int c_base, int c_count, int row, int grid,
+                 cudaStream_t s);
 // A = 4 posteriors (npost / bpost) from the tree-program kernel
 int launch_tree4_post(const KParams &p, int grid, int block, size_t smem, cudaStream_t s);
 // A = 64 F81 accumulation on the tensor cores (k_acctc.cu); groups of 8 columns

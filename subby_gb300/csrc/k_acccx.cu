@@ -15,7 +15,16 @@
 // memory (double-buffered, one barrier per branch) and each thread updates
 // its 16 entries with J_n read through L1.  The epilogue forms T = C Vinv and
 // V T through shared memory.  Complex tables (P.cx): J (R x A x A), V, Vinv,
-// R (A x A each), FP32 pairs.
+// R, Vinv^T, V^T (A x A each), FP32 pairs; then V, Vinv, Vinv^T, V^T in FP64
+// pairs for the FP64 back-transform (k_bt_cx).  P.cx_exact selects the
+// pair (Vinv^T, V^T) in place of (V, Vinv): the expected counts of the
+// process M(t) = e^{Qt} itself (D~ = D V, U~ = Vinv U, Vinv^T C V^T), which
+// differ from the reference's formula for non-reversible Q.
+//
+// A = 64: the back-transform cancels strongly (|C| is a few hundred times
+// the counts when V is far from orthogonal), so k_acc_cx writes C (FP32) to
+// a buffer and k_bt_cx back-transforms it in FP64 with V, Vinv in shared
+// memory.
 #include "common.cuh"
 
 namespace subby {
@@ -46,10 +55,13 @@ constexpr size_t cx_smem() {
   return (size_t)(2 * A * A + 2 * Gm::G * 2 * A + Gm::G * A * A) * sizeof(float2);
 }
 
-// PB: per-branch counts (R, A, A, C) instead of the sum over branches
-template <int A, bool PB>
+// PB: per-branch counts (R, A, A, C) instead of the sum over branches;
+// CBUF: write the summed C of branches [n_lo, n_hi) to cbuf ([column][A*A]
+// complex) instead of back-transforming it
+template <int A, bool PB, bool CBUF>
 __global__ void __launch_bounds__(kCxThreads) k_acc_cx(const KParams P, const float *__restrict__ sa,
-                                                       const float *__restrict__ sb, int c_base, int c_count) {
+                                                       const float *__restrict__ sb, int c_base, int c_count,
+                                                       int n_lo, int n_hi, float2 *__restrict__ cbuf) {
   using Gm = CxGeo<A>;
   constexpr int TPC = Gm::TPC, G = Gm::G;
   extern __shared__ __align__(16) float2 s_cx[];
@@ -58,9 +70,10 @@ __global__ void __launch_bounds__(kCxThreads) k_acc_cx(const KParams P, const fl
   float2 *sP = sVi + A * A;           // [2][G][2A]: D~ (k < A), U~ (A + l)
   float2 *sC = sP + 2 * G * 2 * A;    // [G][A][A]: C, then T = C Vinv
   const float2 *J = P.cx;
-  const float2 *Vg = P.cx + (size_t)P.R * A * A;
+  const float2 *T0 = P.cx + (size_t)P.R * A * A;  // V, Vinv, R, Vinv^T, V^T
+  const float2 *Vg = T0 + (P.cx_exact ? 3 : 0) * A * A;
   const float2 *Vig = Vg + A * A;
-  const float2 *Rg = Vig + A * A;
+  const float2 *Rg = T0 + 2 * A * A;
   const int t = threadIdx.x;
   for (int e = t; e < A * A; e += blockDim.x) {
     sV[e] = Vg[e];
@@ -117,7 +130,7 @@ __global__ void __launch_bounds__(kCxThreads) k_acc_cx(const KParams P, const fl
     float2 acc[kCxE];
 #pragma unroll
     for (int i = 0; i < kCxE; ++i) acc[i] = make_float2(0.f, 0.f);
-    for (int n = 1; n < P.R; ++n) {
+    for (int n = n_lo; n < n_hi; ++n) {
       float2 *buf = sP + ((size_t)(n & 1) * G + g) * 2 * A;
       if (busy) {
         const size_t srow = ((size_t)(n - 1) * c_count + ccl) * A;
@@ -160,25 +173,102 @@ __global__ void __launch_bounds__(kCxThreads) k_acc_cx(const KParams P, const fl
         epilogue(acc, n, valid, col);
       }
     }
-    if constexpr (!PB) epilogue(acc, 0, valid, col);
+    if constexpr (CBUF) {
+      if (valid) {
+        float2 *o = cbuf + (size_t)ccl * A * A + p * kCxE;
+#pragma unroll
+        for (int i = 0; i < kCxE; ++i) o[i] = acc[i];
+      }
+    } else if constexpr (!PB) {
+      epilogue(acc, 0, valid, col);
+    }
   }
 }
 
-template <int A, bool PB>
-int cx_launch(const KParams &p, const float *sa, const float *sb, int c_base, int c_count, int grid,
-              cudaStream_t s) {
+// FP64 back-transform of buffered C (A = 64): per column, T = C Vinv and
+// V T in FP64 with V, Vinv, T in shared memory (224 KB at A = 64); output
+// row `row` of counts.
+template <int A>
+__global__ void __launch_bounds__(kCxThreads) k_bt_cx(const KParams P, const float2 *__restrict__ cbuf, int c_base,
+                                                      int c_count, int row) {
+  extern __shared__ __align__(16) double2 s_bt[];
+  double2 *sV = s_bt;           // A x A
+  double2 *sVi = sV + A * A;    // A x A
+  double2 *sT = sVi + A * A;    // A x A
+  float2 *sCc = reinterpret_cast<float2 *>(sT + A * A);  // A x A
+  const double2 *D0 = reinterpret_cast<const double2 *>(P.cx + (size_t)(P.R + 5) * A * A);  // V, Vinv, Vinv^T, V^T
+  const double2 *Vg = D0 + (P.cx_exact ? 2 : 0) * A * A;
+  const double2 *Vig = Vg + A * A;
+  const float2 *Rg = P.cx + (size_t)(P.R + 2) * A * A;
+  const int t = threadIdx.x;
+  for (int e = t; e < A * A; e += blockDim.x) {
+    sV[e] = Vg[e];
+    sVi[e] = Vig[e];
+  }
+  constexpr int EPT = A * A / kCxThreads > 0 ? A * A / kCxThreads : 1;  // entries per thread
+  const int C = P.C;
+  for (int cc = blockIdx.x; cc < c_count; cc += gridDim.x) {
+    __syncthreads();  // tables loaded / previous column's reads done
+    for (int e = t; e < A * A; e += blockDim.x) sCc[e] = cbuf[(size_t)cc * A * A + e];
+    __syncthreads();
+    for (int e = t; e < A * A; e += blockDim.x) {
+      const int k = e / A, j = e % A;
+      double2 s = make_double2(0.0, 0.0);
+      for (int l = 0; l < A; ++l) {
+        const float2 c = sCc[k * A + l];
+        const double2 v = sVi[l * A + j];
+        s.x = fma((double)c.x, v.x, fma(-(double)c.y, v.y, s.x));
+        s.y = fma((double)c.x, v.y, fma((double)c.y, v.x, s.y));
+      }
+      sT[e] = s;
+    }
+    __syncthreads();
+    float *out = P.counts + (size_t)row * A * A * C + (size_t)c_base + cc;
+    for (int e = t; e < A * A; e += blockDim.x) {
+      const int i = e / A, j = e % A;
+      double2 s = make_double2(0.0, 0.0);
+      for (int k = 0; k < A; ++k) {
+        const double2 v = sV[i * A + k], x = sT[k * A + j];
+        s.x = fma(v.x, x.x, fma(-v.y, x.y, s.x));
+        s.y = fma(v.x, x.y, fma(v.y, x.x, s.y));
+      }
+      double r = s.x;
+      if (i != j) {
+        const float2 q = __ldg(Rg + e);
+        r = (double)q.x * s.x - (double)q.y * s.y;
+      }
+      out[(size_t)e * C] = (float)r;
+    }
+    (void)EPT;
+  }
+}
+
+template <int A, bool PB, bool CBUF>
+int cx_launch(const KParams &p, const float *sa, const float *sb, int c_base, int c_count, int n_lo, int n_hi,
+              float2 *cbuf, int grid, cudaStream_t s) {
   const size_t smem = cx_smem<A>();
-  cudaError_t e = cudaFuncSetAttribute(k_acc_cx<A, PB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaError_t e =
+      cudaFuncSetAttribute(k_acc_cx<A, PB, CBUF>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return (int)e;
-  k_acc_cx<A, PB><<<grid, kCxThreads, smem, s>>>(p, sa, sb, c_base, c_count);
+  k_acc_cx<A, PB, CBUF><<<grid, kCxThreads, smem, s>>>(p, sa, sb, c_base, c_count, n_lo, n_hi, cbuf);
   return (int)cudaGetLastError();
 }
 
 template <int A>
-int cx_launch_pb(const KParams &p, bool pb, const float *sa, const float *sb, int c_base, int c_count, int grid,
-                 cudaStream_t s) {
-  return pb ? cx_launch<A, true>(p, sa, sb, c_base, c_count, grid, s)
-            : cx_launch<A, false>(p, sa, sb, c_base, c_count, grid, s);
+int cx_launch_any(const KParams &p, bool pb, const float *sa, const float *sb, int c_base, int c_count, int n_lo,
+                  int n_hi, float2 *cbuf, int grid, cudaStream_t s) {
+  if (cbuf) return cx_launch<A, false, true>(p, sa, sb, c_base, c_count, n_lo, n_hi, cbuf, grid, s);
+  return pb ? cx_launch<A, true, false>(p, sa, sb, c_base, c_count, n_lo, n_hi, cbuf, grid, s)
+            : cx_launch<A, false, false>(p, sa, sb, c_base, c_count, n_lo, n_hi, cbuf, grid, s);
+}
+
+template <int A>
+int bt_launch(const KParams &p, const float2 *cbuf, int c_base, int c_count, int row, int grid, cudaStream_t s) {
+  const size_t smem = (size_t)3 * A * A * sizeof(double2) + (size_t)A * A * sizeof(float2);
+  cudaError_t e = cudaFuncSetAttribute(k_bt_cx<A>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return (int)e;
+  k_bt_cx<A><<<grid, kCxThreads, smem, s>>>(p, cbuf, c_base, c_count, row);
+  return (int)cudaGetLastError();
 }
 
 }  // namespace
@@ -197,17 +287,25 @@ int cx_columns_per_cta(int A) {
   }
 }
 
+bool cx_bt64(int A) { return A == 64; }
+
 int launch_acc_cx(const KParams &p, int A, bool pb, const float *sa, const float *sb, int c_base, int c_count,
-                  int grid, cudaStream_t s) {
+                  int n_lo, int n_hi, float2 *cbuf, int grid, cudaStream_t s) {
   switch (A) {
-    case 4: return cx_launch_pb<4>(p, pb, sa, sb, c_base, c_count, grid, s);
-    case 8: return cx_launch_pb<8>(p, pb, sa, sb, c_base, c_count, grid, s);
-    case 16: return cx_launch_pb<16>(p, pb, sa, sb, c_base, c_count, grid, s);
-    case 20: return cx_launch_pb<20>(p, pb, sa, sb, c_base, c_count, grid, s);
-    case 32: return cx_launch_pb<32>(p, pb, sa, sb, c_base, c_count, grid, s);
-    case 64: return cx_launch_pb<64>(p, pb, sa, sb, c_base, c_count, grid, s);
+    case 4: return cx_launch_any<4>(p, pb, sa, sb, c_base, c_count, n_lo, n_hi, cbuf, grid, s);
+    case 8: return cx_launch_any<8>(p, pb, sa, sb, c_base, c_count, n_lo, n_hi, cbuf, grid, s);
+    case 16: return cx_launch_any<16>(p, pb, sa, sb, c_base, c_count, n_lo, n_hi, cbuf, grid, s);
+    case 20: return cx_launch_any<20>(p, pb, sa, sb, c_base, c_count, n_lo, n_hi, cbuf, grid, s);
+    case 32: return cx_launch_any<32>(p, pb, sa, sb, c_base, c_count, n_lo, n_hi, cbuf, grid, s);
+    case 64: return cx_launch_any<64>(p, pb, sa, sb, c_base, c_count, n_lo, n_hi, cbuf, grid, s);
     default: return -1;
   }
+}
+
+int launch_bt_cx(const KParams &p, int A, const float2 *cbuf, int c_base, int c_count, int row, int grid,
+                 cudaStream_t s) {
+  if (A == 64) return bt_launch<64>(p, cbuf, c_base, c_count, row, grid, s);
+  return -1;
 }
 
 }  // namespace subby

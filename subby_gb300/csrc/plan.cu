@@ -600,7 +600,9 @@ int plan_create(const int32_t *parent, const double *dist, const double *evals, 
     }
     hMT.assign((size_t)R * (A + 1) * A, 0.f);
     hMN.assign((size_t)R * A * A, 0.f);
-    hcx.assign((size_t)(R + 3) * A * A, make_float2(0.f, 0.f));
+    // float2: J (R A^2), V, Vinv, rate, Vinv^T, V^T; then FP64 pairs: V,
+    // Vinv, Vinv^T, V^T (two float2 slots per value)
+    hcx.assign((size_t)(R + 13) * A * A, make_float2(0.f, 0.f));
     for (int n = 0; n < R; ++n) {
       const double t = dist[n];
       for (int k = 0; k < A; ++k) E[k] = std::exp(mu[k] * t);
@@ -624,14 +626,28 @@ int plan_create(const int32_t *parent, const double *dist, const double *evals, 
           hcx[((size_t)n * A + k) * A + l] = make_float2((float)J.real(), (float)J.imag());
         }
     }
-    float2 *cV = hcx.data() + (size_t)R * A * A, *cVi = cV + A * A, *cR = cVi + A * A;
+    float2 *cV = hcx.data() + (size_t)R * A * A, *cVi = cV + A * A, *cR = cVi + A * A, *cViT = cR + A * A,
+           *cVT = cViT + A * A;
+    double *d64 = reinterpret_cast<double *>(hcx.data() + (size_t)(R + 5) * A * A);  // 4 blocks of A^2 pairs
+    auto f2 = [](cd z) { return make_float2((float)z.real(), (float)z.imag()); };
+    auto put64 = [&](int blk, int e, cd z) {
+      d64[2 * ((size_t)blk * A * A + e)] = z.real();
+      d64[2 * ((size_t)blk * A * A + e) + 1] = z.imag();
+    };
     for (int i = 0; i < A; ++i)
       for (int j = 0; j < A; ++j) {
         cd r = 0.0;
         for (int k = 0; k < A; ++k) r += V[i * A + k] * mu[k] * Vi[k * A + j];
-        cV[i * A + j] = make_float2((float)V[i * A + j].real(), (float)V[i * A + j].imag());
-        cVi[i * A + j] = make_float2((float)Vi[i * A + j].real(), (float)Vi[i * A + j].imag());
-        cR[i * A + j] = make_float2((float)r.real(), (float)r.imag());
+        const int e = i * A + j;
+        cV[e] = f2(V[e]);
+        cVi[e] = f2(Vi[e]);
+        cR[e] = f2(r);
+        cViT[e] = f2(Vi[j * A + i]);
+        cVT[e] = f2(V[j * A + i]);
+        put64(0, e, V[e]);
+        put64(1, e, Vi[e]);
+        put64(2, e, Vi[j * A + i]);
+        put64(3, e, V[j * A + i]);
       }
     e = cudaMemcpyAsync(P->d_tab + o.MT, hMT.data(), hMT.size() * sizeof(float), cudaMemcpyHostToDevice, qs);
     if (e == cudaSuccess)
@@ -1190,6 +1206,8 @@ int run_post(subby_plan *P, const int32_t *d_aln, int C, int node, float *d_node
 // pass), k_acc_cx does the complex accumulation and back-transform.
 int run_cx(subby_plan *P, const int32_t *d_aln, int C, float *d_logL, float *d_counts, float *d_root, int mode,
            int mask_mode, const uint8_t *d_mask, cudaStream_t stream) {
+  // A = 64: C buffered per chunk (per branch for per-branch counts) and
+  // back-transformed in FP64 by k_bt_cx
   const int A = P->A, R = P->R;
   if (!cx_supported(A) || !post_supported(A))
     return fail(SUBBY_ERR_UNSUPPORTED, "irreversible counts are implemented for A = 4, 8, 16, 20, 32, 64");
@@ -1200,8 +1218,10 @@ int run_cx(subby_plan *P, const int32_t *d_aln, int C, float *d_logL, float *d_c
   KParams k = walk_params(P, d_aln, C, mode & (kModeLogLike | kModeRootProb), mask_mode, d_mask, d_logL, d_counts,
                           d_root);
   k.cx = P->d_cx;
+  k.cx_exact = (mode & kModeIrrevExact) != 0;
   k.npost = nullptr;
   k.npost_node = -1;
+  const bool bt64 = cx_bt64(A);
   const bool tc = (A == 64) && P->d_tab16 && (g_kernel_sel == 0 || g_kernel_sel == 5);
   const int tile = big_tile();
   const int H = (A + 31) / 32;
@@ -1219,9 +1239,11 @@ int run_cx(subby_plan *P, const int32_t *d_aln, int C, float *d_logL, float *d_c
   const size_t slot_floats = (size_t)walk_grid * k.nslots * tile * A;
   const size_t slot_ints = (size_t)walk_grid * k.nslots * tile;
   const size_t stage_floats = counts ? (size_t)(R - 1) * chunk * A : 0;
+  const size_t cbuf_bytes = (counts && bt64) ? (size_t)chunk * A * A * sizeof(float2) : 0;
   auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
   int rc;
-  if ((rc = P->grow(P->work, al(slot_floats * 4) + al(slot_ints * 4) + 2 * al(stage_floats * 4) + 256, stream)))
+  if ((rc = P->grow(P->work, al(slot_floats * 4) + al(slot_ints * 4) + 2 * al(stage_floats * 4) + al(cbuf_bytes) + 256,
+                    stream)))
     return rc;
   char *base = (char *)P->work.p;
   k.scrV = (float *)base;
@@ -1231,6 +1253,8 @@ int run_cx(subby_plan *P, const int32_t *d_aln, int C, float *d_logL, float *d_c
   float *sa = counts ? (float *)base : nullptr;
   base += al(stage_floats * 4);
   float *sb = counts ? (float *)base : nullptr;
+  base += al(stage_floats * 4);
+  float2 *cbuf = cbuf_bytes ? (float2 *)base : nullptr;
   const int G = cx_columns_per_cta(A);
   for (int c0 = 0; c0 < C; c0 += chunk) {
     const int cc = std::min(chunk, C - c0);
@@ -1240,10 +1264,22 @@ int run_cx(subby_plan *P, const int32_t *d_aln, int C, float *d_logL, float *d_c
     if (!counts) continue;
     const long long groups = (cc + G - 1) / G;
     const int grid = (int)std::max<long long>(1, std::min<long long>(groups, (long long)P->nsm * 2));
-    lr = launch_acc_cx(k, A, pb, sa, sb, c0, cc, grid, stream);
-    if (lr != 0)
-      return fail(SUBBY_ERR_CUDA, std::string("accumulate launch failed: ") + cudaGetErrorString((cudaError_t)lr));
-    g_launches += 1;
+    if (!bt64) {
+      lr = launch_acc_cx(k, A, pb, sa, sb, c0, cc, 1, R, nullptr, grid, stream);
+      if (lr != 0)
+        return fail(SUBBY_ERR_CUDA, std::string("accumulate launch failed: ") + cudaGetErrorString((cudaError_t)lr));
+      g_launches += 1;
+      continue;
+    }
+    // FP64 back-transform: all branches at once, or branch by branch
+    const int bgrid = std::max(1, std::min(cc, P->nsm));
+    for (int n = pb ? 1 : 0; n < (pb ? R : 1); ++n) {
+      lr = launch_acc_cx(k, A, false, sa, sb, c0, cc, pb ? n : 1, pb ? n + 1 : R, cbuf, grid, stream);
+      if (lr == 0) lr = launch_bt_cx(k, A, cbuf, c0, cc, pb ? n : 0, bgrid, stream);
+      if (lr != 0)
+        return fail(SUBBY_ERR_CUDA, std::string("accumulate launch failed: ") + cudaGetErrorString((cudaError_t)lr));
+      g_launches += 2;
+    }
   }
   return mark_use(P, stream);
 }
@@ -1371,6 +1407,7 @@ int subby_plan_run(subby_plan *P, const int32_t *aln, int C, float *logL, float 
   if (rootProb) mode |= kModeRootProb;
   if (counts) mode |= kModeCounts;
   if (counts && counts_kind == SUBBY_COUNTS_F81) mode |= kModeF81;
+  if (flags & SUBBY_IRREV_EXACT) mode |= kModeIrrevExact;
   const bool bt64 = (flags & SUBBY_BT_FP64) || (!(flags & SUBBY_BT_FP32) && A <= 8);
   if (bt64) mode |= kModeBT64;
   if (!mode) return SUBBY_OK;
@@ -1488,7 +1525,8 @@ int subby_plan_branch_counts(subby_plan *P, const int32_t *aln, int C, float *br
   if (dev != P->device) CU(cudaSetDevice(P->device));
   const int A = P->A, R = P->R;
   CU(cudaStreamWaitEvent(stream, P->ready, 0));
-  const int mode = kModeCounts | kModeBranch | (counts_kind == SUBBY_COUNTS_F81 ? kModeF81 : 0);
+  const int mode = kModeCounts | kModeBranch | (counts_kind == SUBBY_COUNTS_F81 ? kModeF81 : 0) |
+                   ((flags & SUBBY_IRREV_EXACT) ? kModeIrrevExact : 0);
   const size_t b_out = (size_t)R * A * A * C * sizeof(float);
   int rc;
   if (flags & SUBBY_DEVICE_PTRS) {

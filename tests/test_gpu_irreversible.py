@@ -40,11 +40,16 @@ def _check_all(plan, aln, ot, md, what, branch=True):
     assert_cols(res['rootProb'], oracle.RootProb(aln, ot, md), ROOTPROB_RTOL, what + " rootProb")
     c0 = plan.run(aln, loglike=False, counts=True, branch_mask=None)['counts']
     assert_cols(c0, oracle.Counts(aln, ot, md, branch_mask=None), COUNTS_RTOL, what + " counts (no mask)")
+    cx = plan.run(aln, loglike=False, counts=True, exact_irreversible=True)['counts']
+    assert_cols(cx, oracle.Counts(aln, ot, md, irrev_exact=True), COUNTS_RTOL, what + " counts (exact)")
     if branch:
         bc = plan.branch_counts(aln)
         assert_cols(_per_branch(bc), _per_branch(oracle.BranchCounts(aln, ot, md)), COUNTS_RTOL,
                     what + " branch counts")
         np.testing.assert_array_equal(bc[0], 0.0)
+        bx = plan.branch_counts(aln, exact_irreversible=True)
+        assert_cols(_per_branch(bx), _per_branch(oracle.BranchCounts(aln, ot, md, irrev_exact=True)), COUNTS_RTOL,
+                    what + " branch counts (exact)")
     post = plan.posteriors(aln, want_node=True, want_branch=branch)
     assert_cols(_nodes(post['node']), _nodes(oracle.NodePosterior(aln, ot, md)), POSTERIOR_RTOL, what + " node post")
     if branch:
@@ -88,7 +93,7 @@ def test_random_irreversible_vs_oracle(A, leaves, C):
         rng.integers(0, A + 2, size=(len(tree.parentIndex), C)).astype(np.int32)
     ot = oracle.Tree(tree.parentIndex, tree.distanceToParent)
     plan = sg.Plan(tree, m)
-    _check_all(plan, aln, ot, m._asdict(), f"A={A}", branch=(A <= 32))
+    _check_all(plan, aln, ot, m._asdict(), f"A={A}", branch=(A <= 32 or C <= 8))
     plan.close()
 
 
@@ -124,9 +129,27 @@ def test_given_mask_api_functions_and_errors():
     plan.close()
 
 
+def test_per_branch_fp64_back_transform_a64():
+    """A = 64 per-branch counts: C buffered branch by branch and
+    back-transformed in FP64."""
+    rng = np.random.default_rng(99)
+    m = models.random_irreversible(64, rng)
+    tree = synth.random_tree(4, 0.15, rng)
+    aln = rng.integers(0, 66, size=(len(tree.parentIndex), 9)).astype(np.int32)
+    ot = oracle.Tree(tree.parentIndex, tree.distanceToParent)
+    plan = sg.Plan(tree, m)
+    bc = plan.branch_counts(aln)
+    assert_cols(_per_branch(bc), _per_branch(oracle.BranchCounts(aln, ot, m._asdict())), COUNTS_RTOL, "A=64 per-branch")
+    tot = plan.run(aln, loglike=False, counts=True, branch_mask=None)['counts']
+    assert_cols(bc.astype(np.float64).sum(0), tot, COUNTS_RTOL, "A=64 branches sum to Counts")
+    plan.close()
+
+
 def test_reversible_model_as_irreversible_gives_the_same_counts():
     """A reversible model written as V = diag(pi)^-1/2 W, V^-1 = W^T diag(pi)^1/2
-    (real eigenvalues) through the complex path equals the reversible path."""
+    (real eigenvalues) through the complex path with ``exact_irreversible``
+    equals the reversible path (the reference's irreversible formula does
+    not: it gives the transposed process's counts, tests/test_irrev_math.py)."""
     w = synth.plain_small(seed=2, C=200)
     aln, tree, m = w['alignment'], w['tree'], w['model']
     sp = np.sqrt(m.pi)
@@ -135,7 +158,7 @@ def test_reversible_model_as_irreversible_gives_the_same_counts():
     mi = sg.IrrevDiagModel(m.eigenvalues.astype(np.complex128), V.astype(np.complex128),
                            Vi.astype(np.complex128), m.pi)
     a = sg.Plan(tree, m).run(aln, loglike=True, counts=True, rootprob=True)
-    b = sg.Plan(tree, mi).run(aln, loglike=True, counts=True, rootprob=True)
+    b = sg.Plan(tree, mi).run(aln, loglike=True, counts=True, rootprob=True, exact_irreversible=True)
     assert_loglike(b['logLike'], a['logLike'])
     assert_cols(b['counts'], a['counts'], COUNTS_RTOL, "counts")
     assert_cols(b['rootProb'], a['rootProb'], ROOTPROB_RTOL, "rootProb")

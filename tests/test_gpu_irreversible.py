@@ -3,7 +3,12 @@ the FP64 oracle's restatement of subby/oracle/oracle.py:474-740 and the
 reference oracle's fixtures (irrev_4, irrev_8, irrev_16).
 
 Tolerances as for reversible models (tests/_tol.py): LogLike 1e-5 relative,
-Counts / RootProb / posteriors 1e-4 column-wise norm-wise."""
+RootProb / posteriors 1e-4 column-wise norm-wise.  Counts: 1e-4 x max(1,
+cond(V) / 10).  The counts are Re V C V^-1 with |C| a few hundred times the
+counts when V is far from orthogonal, so the FP32 rounding of the inside /
+outside vectors and of their projections is amplified by about cond(V)^2
+(cyclic test models: cond(V) = 1.6 at A = 4, 8 at A = 16, 29 at A = 32, 59
+at A = 64); the A = 64 back-transform itself runs in FP64."""
 import numpy as np
 import pytest
 
@@ -33,22 +38,27 @@ def _nodes(x):
     return np.moveaxis(x, 0, -2).reshape(*x.shape[1:-1], -1)
 
 
+def _counts_tol(md):
+    return COUNTS_RTOL * max(1.0, np.linalg.cond(md['eigenvectors']) / 10.0)
+
+
 def _check_all(plan, aln, ot, md, what, branch=True):
+    tol = _counts_tol(md)
     res = plan.run(aln, loglike=True, counts=True, rootprob=True)
     assert_loglike(res['logLike'], oracle.LogLike(aln, ot, md), what=what + " logLike")
-    assert_cols(res['counts'], oracle.Counts(aln, ot, md), COUNTS_RTOL, what + " counts (auto mask)")
+    assert_cols(res['counts'], oracle.Counts(aln, ot, md), tol, what + " counts (auto mask)")
     assert_cols(res['rootProb'], oracle.RootProb(aln, ot, md), ROOTPROB_RTOL, what + " rootProb")
     c0 = plan.run(aln, loglike=False, counts=True, branch_mask=None)['counts']
-    assert_cols(c0, oracle.Counts(aln, ot, md, branch_mask=None), COUNTS_RTOL, what + " counts (no mask)")
+    assert_cols(c0, oracle.Counts(aln, ot, md, branch_mask=None), tol, what + " counts (no mask)")
     cx = plan.run(aln, loglike=False, counts=True, exact_irreversible=True)['counts']
-    assert_cols(cx, oracle.Counts(aln, ot, md, irrev_exact=True), COUNTS_RTOL, what + " counts (exact)")
+    assert_cols(cx, oracle.Counts(aln, ot, md, irrev_exact=True), tol, what + " counts (exact)")
     if branch:
         bc = plan.branch_counts(aln)
-        assert_cols(_per_branch(bc), _per_branch(oracle.BranchCounts(aln, ot, md)), COUNTS_RTOL,
+        assert_cols(_per_branch(bc), _per_branch(oracle.BranchCounts(aln, ot, md)), tol,
                     what + " branch counts")
         np.testing.assert_array_equal(bc[0], 0.0)
         bx = plan.branch_counts(aln, exact_irreversible=True)
-        assert_cols(_per_branch(bx), _per_branch(oracle.BranchCounts(aln, ot, md, irrev_exact=True)), COUNTS_RTOL,
+        assert_cols(_per_branch(bx), _per_branch(oracle.BranchCounts(aln, ot, md, irrev_exact=True)), tol,
                     what + " branch counts (exact)")
     post = plan.posteriors(aln, want_node=True, want_branch=branch)
     assert_cols(_nodes(post['node']), _nodes(oracle.NodePosterior(aln, ot, md)), POSTERIOR_RTOL, what + " node post")
@@ -139,9 +149,10 @@ def test_per_branch_fp64_back_transform_a64():
     ot = oracle.Tree(tree.parentIndex, tree.distanceToParent)
     plan = sg.Plan(tree, m)
     bc = plan.branch_counts(aln)
-    assert_cols(_per_branch(bc), _per_branch(oracle.BranchCounts(aln, ot, m._asdict())), COUNTS_RTOL, "A=64 per-branch")
+    tol = _counts_tol(m._asdict())
+    assert_cols(_per_branch(bc), _per_branch(oracle.BranchCounts(aln, ot, m._asdict())), tol, "A=64 per-branch")
     tot = plan.run(aln, loglike=False, counts=True, branch_mask=None)['counts']
-    assert_cols(bc.astype(np.float64).sum(0), tot, COUNTS_RTOL, "A=64 branches sum to Counts")
+    assert_cols(bc.astype(np.float64).sum(0), tot, tol, "A=64 branches sum to Counts")
     plan.close()
 
 

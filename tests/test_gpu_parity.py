@@ -75,7 +75,7 @@ def _check_all(aln, tree, model, f81=False, masked=True, rp=True, bt64=None):
 def test_golden(name, kernel):
     g = _golden.load(name)
     tree = sg.Tree(g['parentIndex'], g['distanceToParent'])
-    model = sg.DiagModel(g['eigenvalues'], g['eigenvectors'], g['pi'])
+    model = sg.models.ensure_diag(_golden.model_dict(g))   # IrrevDiagModel for the irrev_* fixtures
     plan = sg.Plan(tree, model)
     r = plan.run(g['alignment'], loglike=True, counts=True, rootprob=True, branch_mask=None)
     assert_loglike(r['logLike'], g['logLike'])

@@ -135,6 +135,16 @@ int subby_plan_branch_counts(subby_plan *plan, const int32_t *alignment, int C, 
  */
 int subby_plan_posteriors(subby_plan *plan, const int32_t *alignment, int C, int node, float *nodePost,
                           float *branchPost, int flags, void *stream);
+/*
+ * Posterior over mixture components per column: out[k][c] = softmax_k of
+ * logL[k][c] + log_weights[k] (logL, out (K, C) float32; log_weights (K,)
+ * host float64).  Replaces MixturePosterior's final step
+ * (subby/jax/mixture.py:6-28, subby/jax/__init__.py:653-678; oracle
+ * subby/oracle/oracle.py:1334-1365); the K log-likelihoods come from one
+ * plan per component.
+ */
+int subby_mixture_posterior(const float *logL, const double *log_weights, int K, int C, float *out, int flags,
+                            void *stream);
 /* Wait for the plan's enqueued work and report SUBBY_ERR_TIMEOUT if a
  * bounded device wait (tensor-core kernels) gave up since the last check
  * (device-pointer runs return before their kernels finish, so they report

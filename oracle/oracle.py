@@ -697,3 +697,81 @@ def loglike_fd_grad(alignment, tree, log_exch, pi, h=1e-4, wrt="distances"):
         lm[i] -= h
         g[i] = (total(dist, lp) - total(dist, lm)) / (2 * h)
     return g
+
+
+# ---------------------------------------------------------------------------
+# Batched models — rate categories, mixtures, per-column model lists
+# ---------------------------------------------------------------------------
+
+def gamma_rate_categories(alpha, K):
+    """Yang (1994) discrete gamma: quantile medians by 64 bisection steps,
+    mean-normalised rates, uniform weights; oracle.py:208-241."""
+    from scipy.special import gammainc
+    mids = 0.5 * (np.linspace(0, 1, K + 1)[:-1] + np.linspace(0, 1, K + 1)[1:])
+    rates = np.zeros(K)
+    for i, p in enumerate(mids):
+        lo, hi = 0.0, max(50.0, 10.0 / alpha)
+        for _ in range(64):
+            mid = 0.5 * (lo + hi)
+            if float(gammainc(alpha, mid * alpha)) < p:
+                lo = mid
+            else:
+                hi = mid
+        rates[i] = 0.5 * (lo + hi)
+    return rates * K / np.sum(rates), np.ones(K) / K
+
+
+def scale_model(model, rate_multiplier):
+    """Eigenvalues times the rate; oracle.py:244-262."""
+    m = dict(model)
+    m['eigenvalues'] = np.asarray(model['eigenvalues']) * rate_multiplier
+    return m
+
+
+def mixture_posterior(log_likes, log_weights):
+    """softmax_k(log_likes[k, c] + log_weights[k]); oracle.py:1334-1365."""
+    lj = np.asarray(log_likes, dtype=np.float64) + np.asarray(log_weights, dtype=np.float64)[:, None]
+    lj = lj - np.max(lj, axis=0, keepdims=True)
+    e = np.exp(lj)
+    return e / np.sum(e, axis=0, keepdims=True)
+
+
+def MixturePosterior(alignment, tree, models, log_weights):
+    """(K, C) posterior over mixture components; oracle.py:1598-1615."""
+    return mixture_posterior(np.stack([LogLike(alignment, tree, m) for m in models]), log_weights)
+
+
+def LogLike_per_column(alignment, tree, models):
+    """Per-column models (subby/jax/__init__.py:267-277): column c uses
+    models[c]'s M(t); the root prior is models[0]'s pi for every column."""
+    alignment = np.asarray(alignment)
+    out = np.zeros(alignment.shape[1])
+    for c in range(alignment.shape[1]):
+        M = _sub_matrices(models[c], tree.distanceToParent)
+        out[c] = upward_pass(alignment[:, c:c + 1], tree, M, models[0]['pi'])[2][0]
+    return out
+
+
+def RootProb_per_column(alignment, tree, models):
+    """subby/jax/__init__.py:617-633: pi_c * U_root e^{lnU - lnL}, with lnL
+    from the root prior models[0]['pi'] (columns need not sum to one when
+    the pis differ)."""
+    alignment = np.asarray(alignment)
+    A = len(models[0]['pi'])
+    out = np.zeros((A, alignment.shape[1]))
+    for c in range(alignment.shape[1]):
+        M = _sub_matrices(models[c], tree.distanceToParent)
+        U, lnU, lnL = upward_pass(alignment[:, c:c + 1], tree, M, models[0]['pi'])
+        out[:, c] = np.asarray(models[c]['pi']) * U[0, 0] * np.exp(lnU[0, 0] - lnL[0])
+    return out
+
+
+def Counts_per_column(alignment, tree, models, f81_fast=False, branch_mask="auto"):
+    """subby/jax/__init__.py:396-411: column by column with its own model."""
+    alignment = np.asarray(alignment)
+    cols = []
+    for c in range(alignment.shape[1]):
+        bm = branch_mask if (branch_mask is None or isinstance(branch_mask, str)) else \
+            np.asarray(branch_mask)[:, c:c + 1]
+        cols.append(Counts(alignment[:, c:c + 1], tree, models[c], f81_fast=f81_fast, branch_mask=bm))
+    return np.concatenate(cols, axis=-1)

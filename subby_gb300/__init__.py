@@ -6,13 +6,13 @@ root posteriors.  Drop-in for the single-model entry points of ``subby.jax``.
 from .types import Tree, DiagModel, IrrevDiagModel, RateModel
 from .models import (hky85_diag, jukes_cantor_model, f81_model, diagonalize_rate_matrix,
                      reversible_rate_matrix, random_reversible, irrev_model_from_rate_matrix,
-                     diagonalize_irreversible)
-from .api import (LogLike, Counts, BranchCounts, RootProb, LogLikeCustomGrad, InsideOutside, Plan, get_plan,
-                  clear_plan_cache)
+                     diagonalize_irreversible, gamma_rate_categories, scale_model)
+from .api import (LogLike, Counts, BranchCounts, RootProb, MixturePosterior, LogLikeCustomGrad, InsideOutside, Plan,
+                  get_plan, clear_plan_cache)
 from . import _lib
 
 __all__ = ["BranchCounts", "Tree", "DiagModel", "IrrevDiagModel", "RateModel", "irrev_model_from_rate_matrix",
-           "diagonalize_irreversible", "hky85_diag", "jukes_cantor_model", "f81_model",
+           "diagonalize_irreversible", "gamma_rate_categories", "scale_model", "MixturePosterior", "hky85_diag", "jukes_cantor_model", "f81_model",
            "diagonalize_rate_matrix", "reversible_rate_matrix", "random_reversible", "LogLike",
            "Counts", "RootProb", "LogLikeCustomGrad", "InsideOutside", "Plan", "get_plan", "clear_plan_cache"]
 

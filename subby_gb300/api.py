@@ -24,7 +24,7 @@ from collections import OrderedDict
 
 import numpy as np
 
-from . import _lib
+from . import _lib, batch
 from .models import ensure_diag
 from .types import IrrevDiagModel, Tree
 
@@ -404,20 +404,41 @@ def _device_of(x):
     return None
 
 
+def _grid_unsupported():
+    raise NotImplementedError("model grids (per-branch models) are not supported")
+
+
 def LogLike(alignment, tree: Tree, model, maxChunkSize: int = 128):
-    """Per-column log-likelihoods (C,); subby/jax/__init__.py:207."""
+    """Per-column log-likelihoods (C,); subby/jax/__init__.py:207.  A ``*H``
+    batched model gives (*H, C); a list of C models one model per column."""
     del maxChunkSize  # columns are tiled on the device
-    return get_plan(tree, model, _device_of(alignment)).run(alignment, loglike=True)['logLike']
+    k = batch.kind(model)
+    if k == 'grid':
+        _grid_unsupported()
+    if k == 'list':
+        return batch.loglike_list(alignment, tree, model, get_plan)
+    dev = _device_of(alignment)
+    one = lambda m: get_plan(tree, m, dev).run(alignment, loglike=True)['logLike']  # noqa: E731
+    return batch.map_h(model, one) if k == 'H' else one(model)
 
 
 def Counts(alignment, tree: Tree, model, maxChunkSize: int = 128, f81_fast_flag: bool = False,
            branch_mask="auto", exact_irreversible: bool = False):
     """(A, A, C) dwell times (diagonal) and substitution counts; subby/jax/__init__.py:338.
+    ``*H`` batches and per-column model lists as for ``LogLike``.
     ``exact_irreversible`` (not in the reference): see ``Plan.run``."""
     del maxChunkSize
-    return get_plan(tree, model, _device_of(alignment)).run(
+    k = batch.kind(model)
+    if k == 'grid':
+        _grid_unsupported()
+    if k == 'list':
+        return batch.counts_list(alignment, tree, model, get_plan, f81=f81_fast_flag, branch_mask=branch_mask,
+                                 exact_irreversible=exact_irreversible)
+    dev = _device_of(alignment)
+    one = lambda m: get_plan(tree, m, dev).run(  # noqa: E731
         alignment, loglike=False, counts=True, f81=f81_fast_flag, branch_mask=branch_mask,
         exact_irreversible=exact_irreversible)['counts']
+    return batch.map_h(model, one) if k == 'H' else one(model)
 
 
 def BranchCounts(alignment, tree: Tree, model, maxChunkSize: int = 128, f81_fast_flag: bool = False,
@@ -426,15 +447,48 @@ def BranchCounts(alignment, tree: Tree, model, maxChunkSize: int = 128, f81_fast
     zeros; subby/jax/__init__.py:450 (unmasked there; ``branch_mask`` as in
     the oracle's BranchCounts, subby/oracle/oracle.py:1517)."""
     del maxChunkSize
-    return get_plan(tree, model, _device_of(alignment)).branch_counts(
+    k = batch.kind(model)
+    if k == 'grid':
+        _grid_unsupported()
+    if k == 'list':
+        return batch.counts_list(alignment, tree, model, get_plan, f81=f81_fast_flag, branch_mask=branch_mask,
+                                 exact_irreversible=exact_irreversible, per_branch=True)
+    dev = _device_of(alignment)
+    one = lambda m: get_plan(tree, m, dev).branch_counts(  # noqa: E731
         alignment, f81=f81_fast_flag, branch_mask=branch_mask, exact_irreversible=exact_irreversible)
+    return batch.map_h(model, one) if k == 'H' else one(model)
 
 
 def RootProb(alignment, tree: Tree, model, maxChunkSize: int = 128):
     """(A, C) posterior root distribution; subby/jax/__init__.py:543."""
     del maxChunkSize
-    return get_plan(tree, model, _device_of(alignment)).run(
-        alignment, loglike=False, rootprob=True)['rootProb']
+    k = batch.kind(model)
+    if k == 'grid':
+        _grid_unsupported()
+    if k == 'list':
+        return batch.rootprob_list(alignment, tree, model, get_plan)
+    dev = _device_of(alignment)
+    one = lambda m: get_plan(tree, m, dev).run(alignment, loglike=False, rootprob=True)['rootProb']  # noqa: E731
+    return batch.map_h(model, one) if k == 'H' else one(model)
+
+
+def MixturePosterior(alignment, tree: Tree, models, log_weights, maxChunkSize: int = 128):
+    """(K, C) posterior over the K mixture components per column;
+    subby/jax/__init__.py:653-678 (log-likelihoods of batched components
+    are summed over their ``*H`` dimensions, as there)."""
+    del maxChunkSize
+    lls = []
+    for m in models:
+        ll = LogLike(alignment, tree, m)
+        while ll.ndim > 1:
+            ll = ll.sum(0)
+        lls.append(ll)
+    if _is_torch(lls[0]):
+        import torch
+        stacked = torch.stack(lls)
+    else:
+        stacked = np.stack(lls)
+    return batch.mixture_posterior(stacked, log_weights)
 
 
 def LogLikeCustomGrad(alignment, tree: Tree, model, maxChunkSize: int = 128, method: str = 'eigen'):

@@ -16,6 +16,10 @@ Irreversible models: ``irrev_model_from_rate_matrix`` /
 ``diagonalize_irreversible`` (subby/jax/diagonalize.py:49-138; oracle
 subby/oracle/oracle.py:265-301: numpy ``eig`` and ``inv`` in complex128) and
 ``random_irreversible`` (synthetic, with complex eigenvalue pairs).
+
+Rate heterogeneity: ``gamma_rate_categories`` (Yang 1994 quantile medians,
+subby/jax/models.py:126-158) and ``scale_model`` (subby/jax/models.py:
+160-186; a (K,) multiplier adds a leading batch dimension).
 """
 from __future__ import annotations
 
@@ -225,3 +229,50 @@ def near_degenerate_reversible(A: int, rng: np.random.Generator, target_fraction
     w = widths.min()
     model, log_exch = build(probe * split_max / max(w, 1e-300))
     return model, log_exch, pi, (d - 1) * (d - 2) // 2
+
+
+def gamma_rate_categories(alpha: float, K: int):
+    """(rates, weights), each (K,): quantile medians of Gamma(alpha, 1/alpha)
+    at the midpoints of K equal-probability bins, by 64 bisection steps,
+    normalised to mean rate 1; uniform weights."""
+    from scipy.special import gammainc
+    edges = np.linspace(0.0, 1.0, K + 1)
+    mids = 0.5 * (edges[:-1] + edges[1:])
+    lo = np.zeros(K)
+    hi = np.full(K, max(50.0, 10.0 / alpha))
+    for _ in range(64):
+        mid = 0.5 * (lo + hi)
+        below = gammainc(alpha, mid * alpha) < mids
+        lo = np.where(below, mid, lo)
+        hi = np.where(below, hi, mid)
+    rates = 0.5 * (lo + hi)
+    return rates * K / np.sum(rates), np.full(K, 1.0 / K)
+
+
+def scale_model(model, rate_multiplier):
+    """Eigenvalues times the rate multiplier; a (K,) multiplier gives a model
+    with a leading batch dimension K (eigenvectors and pi broadcast)."""
+    m = ensure_diag(model)
+    r = np.asarray(rate_multiplier, dtype=np.float64)
+    if r.ndim == 0:
+        return m._replace(eigenvalues=np.asarray(m.eigenvalues) * r)
+    K = r.shape[0]
+    ev = np.asarray(m.eigenvalues)[None, ...] * r.reshape((K,) + (1,) * np.ndim(m.eigenvalues))
+    fields = {f: np.broadcast_to(np.asarray(getattr(m, f))[None, ...], (K,) + np.shape(getattr(m, f)))
+              for f in m._fields if f != 'eigenvalues'}
+    return type(m)(eigenvalues=ev, **fields)
+
+
+def batch_shape(model):
+    """Leading batch dimensions *H of a (possibly batched) diagonal model."""
+    m = ensure_diag(model)
+    return tuple(np.shape(m.eigenvalues)[:-1])
+
+
+def unbatch(model):
+    """(*H, list of the single models in C order)."""
+    m = ensure_diag(model)
+    H = batch_shape(m)
+    if not H:
+        return H, [m]
+    return H, [type(m)(**{f: np.asarray(getattr(m, f))[idx] for f in m._fields}) for idx in np.ndindex(*H)]

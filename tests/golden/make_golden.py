@@ -171,6 +171,38 @@ def main():
         run_case(oracle, RTree, f"irrev_{A}", aln, tr.parentIndex, tr.distanceToParent,
                  m._asdict(), False)
 
+    # mixtures of rate-scaled models (subby/oracle/oracle.py:208-262, 1334-1365,
+    # 1598-1615): the reference's 7node_mixture_jc4 inputs and a discrete-gamma
+    # HKY85 case; written to golden/mixture/ (not a single-model case)
+    mdir = os.path.join(HERE, "mixture")
+    os.makedirs(mdir, exist_ok=True)
+    with open(os.path.join(gdir, "7node_mixture_jc4.json")) as f:
+        inp = json.load(f)['inputs']
+    cases = [("ref_7node_mixture_jc4", np.asarray(inp['alignment'], np.int32), np.asarray(inp['parentIndex']),
+              np.asarray(inp['distanceToParent']), {k: np.asarray(v, np.float64) for k, v in inp['base_model'].items()},
+              np.asarray(inp['rates'], np.float64), np.asarray(inp['log_weights'], np.float64))]
+    rng = np.random.default_rng(21)
+    tr = synth.random_tree(12, 0.2, rng)
+    base = models.hky85_diag(2.5, [0.3, 0.2, 0.2, 0.3])
+    rates, weights = oracle.gamma_rate_categories(0.5, 4)
+    aln = synth.simulated_alignment(tr, base, 48, 0.1, rng)
+    cases.append(("gamma4_hky", aln, tr.parentIndex, tr.distanceToParent, base._asdict(), np.asarray(rates),
+                  np.log(np.asarray(weights))))
+    for name, aln, parent, dist, bm, rates, lw in cases:
+        tree = RTree(parentIndex=np.asarray(parent, np.int32), distanceToParent=np.asarray(dist, np.float64))
+        bm = {k: np.asarray(bm[k], np.float64) for k in ('eigenvalues', 'eigenvectors', 'pi')}
+        ms = [oracle.scale_model(bm, r) for r in rates]
+        ll = np.stack([oracle.LogLike(aln, tree, m) for m in ms])
+        post = oracle.MixturePosterior(aln, tree, ms, lw)
+        np.savez_compressed(os.path.join(mdir, name + ".npz"), alignment=aln, parentIndex=np.asarray(parent, np.int32),
+                            distanceToParent=np.asarray(dist, np.float64), rates=rates, log_weights=lw,
+                            log_likes=ll, posteriors=post, **bm)
+        print(f"  mixture/{name}: K={len(rates)} C={aln.shape[1]}")
+    g_rates, g_w = oracle.gamma_rate_categories(0.5, 4)
+    np.savez_compressed(os.path.join(mdir, "gamma_categories.npz"), alpha=np.array([0.5, 1.0, 2.0]),
+                        rates=np.stack([oracle.gamma_rate_categories(a, 4)[0] for a in (0.5, 1.0, 2.0)]),
+                        weights=g_w)
+
 
 if __name__ == "__main__":
     main()

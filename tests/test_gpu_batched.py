@@ -1,0 +1,122 @@
+"""Batched models on the GPU: ``*H`` batches (discrete-gamma rate
+categories), per-column model lists and MixturePosterior, vs the FP64
+oracle (subby/oracle/oracle.py:208-262, 1334-1365, 1598-1615 restated;
+per-column list semantics of subby/jax/__init__.py:267-277, 396-411,
+617-633) and the reference oracle's mixture fixtures; the identities of the
+reference's own tests (tests/test_api.py TestPerColumnModel: a list of one
+model equals that model; a list of rate-scaled models equals the column-by-
+column result).  Tolerances as everywhere (tests/_tol.py); mixture
+posteriors 1e-4 absolute."""
+import os
+
+import numpy as np
+import pytest
+
+import oracle
+from tests._tol import COUNTS_RTOL, ROOTPROB_RTOL, assert_cols, assert_loglike
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+if not torch.cuda.is_available():  # pragma: no cover
+    pytest.skip("needs a CUDA GPU", allow_module_level=True)
+
+import subby_gb300 as sg  # noqa: E402
+from subby_gb300 import synth, models  # noqa: E402
+
+MIX = os.path.join(os.path.dirname(__file__), "golden", "mixture")
+
+
+@pytest.mark.parametrize("name", ["ref_7node_mixture_jc4", "gamma4_hky"])
+def test_mixture_fixtures(name):
+    with np.load(os.path.join(MIX, name + ".npz")) as z:
+        g = {k: z[k] for k in z.files}
+    tree = sg.Tree(g['parentIndex'], g['distanceToParent'])
+    base = sg.DiagModel(g['eigenvalues'], g['eigenvectors'], g['pi'])
+    ms = [sg.scale_model(base, r) for r in g['rates']]
+    post = sg.MixturePosterior(g['alignment'], tree, ms, g['log_weights'])
+    np.testing.assert_allclose(post, g['posteriors'], atol=1e-4)
+    # the same through one batched model: LogLike (K, C)
+    ll = sg.LogLike(g['alignment'], tree, sg.scale_model(base, g['rates']))
+    assert ll.shape == g['log_likes'].shape
+    assert_loglike(ll, g['log_likes'])
+
+
+def test_h_batch_all_outputs_and_device():
+    w = synth.plain_small(seed=11, C=257)
+    aln, tree, base = w['alignment'], w['tree'], w['model']
+    rates, _ = sg.gamma_rate_categories(0.7, 4)
+    mb = sg.scale_model(base, rates)
+    ot = oracle.Tree(tree.parentIndex, tree.distanceToParent)
+    ll = sg.LogLike(aln, tree, mb)
+    cnt = sg.Counts(aln, tree, mb)
+    rp = sg.RootProb(aln, tree, mb)
+    bc = sg.BranchCounts(aln, tree, mb)
+    assert ll.shape == (4, 257) and cnt.shape == (4, 4, 4, 257) and rp.shape == (4, 4, 257)
+    assert bc.shape == (4, len(tree.parentIndex), 4, 4, 257)
+    for k, r in enumerate(rates):
+        md = oracle.scale_model(base._asdict(), r)
+        assert_loglike(ll[k], oracle.LogLike(aln, ot, md))
+        assert_cols(cnt[k], oracle.Counts(aln, ot, md), COUNTS_RTOL, f"counts k={k}")
+        assert_cols(rp[k], oracle.RootProb(aln, ot, md), ROOTPROB_RTOL, f"rootprob k={k}")
+    dev = sg.LogLike(torch.as_tensor(aln).cuda(), tree, mb)
+    torch.cuda.synchronize()
+    assert dev.is_cuda and tuple(dev.shape) == (4, 257)
+    np.testing.assert_array_equal(dev.cpu().numpy(), ll)
+
+
+def test_per_column_lists_vs_oracle():
+    rng = np.random.default_rng(12)
+    tree = synth.random_tree(12, 0.2, rng)
+    base = models.hky85_diag(2.0, [0.25, 0.25, 0.25, 0.25])
+    C = 60
+    aln = synth.simulated_alignment(tree, base, C, 0.1, rng)
+    ot = oracle.Tree(tree.parentIndex, tree.distanceToParent)
+    # three distinct models over the columns, different pi (root prior rule)
+    palette = [models.hky85_diag(2.0, [0.25] * 4), models.hky85_diag(3.0, [0.1, 0.2, 0.3, 0.4]),
+               models.scale_model(models.hky85_diag(1.5, [0.4, 0.3, 0.2, 0.1]), 1.7)]
+    ms = [palette[rng.integers(0, 3)] for _ in range(C)]
+    ms[0] = palette[1]
+    mds = [m._asdict() for m in ms]
+    assert_loglike(sg.LogLike(aln, tree, ms), oracle.LogLike_per_column(aln, ot, mds))
+    assert_cols(sg.RootProb(aln, tree, ms), oracle.RootProb_per_column(aln, ot, mds), ROOTPROB_RTOL, "rootprob")
+    cnt = sg.Counts(aln, tree, ms)
+    assert_cols(cnt, oracle.Counts_per_column(aln, ot, mds), COUNTS_RTOL, "counts")
+    assert_cols(sg.Counts(aln, tree, ms, branch_mask=None), oracle.Counts_per_column(aln, ot, mds, branch_mask=None),
+                COUNTS_RTOL, "counts unmasked")
+    bc = sg.BranchCounts(aln, tree, ms, branch_mask="auto")
+    assert_cols(bc.astype(np.float64).sum(0), cnt, COUNTS_RTOL, "branches sum to counts")
+    # device inputs: same results, results on the device
+    dl = sg.LogLike(torch.as_tensor(aln).cuda(), tree, ms)
+    torch.cuda.synchronize()
+    assert dl.is_cuda
+    assert_loglike(dl.cpu().numpy(), oracle.LogLike_per_column(aln, ot, mds))
+
+
+def test_reference_identities():
+    """[model] * C equals the single model; rate-scaled models per column equal
+    the column-by-column computation (tests/test_api.py:397-430 of ihh/subby)."""
+    w = synth.plain_small(seed=13, C=40)
+    aln, tree, base = w['alignment'], w['tree'], w['model']
+    np.testing.assert_allclose(sg.LogLike(aln, tree, [base] * 40), sg.LogLike(aln, tree, base), atol=1e-6)
+    ms = [sg.scale_model(base, r) for r in np.linspace(0.5, 2.0, 40)]
+    by_col = np.array([sg.LogLike(aln[:, c:c + 1], tree, ms[c])[0] for c in range(40)])
+    np.testing.assert_allclose(sg.LogLike(aln, tree, ms), by_col, atol=1e-5)
+    with pytest.raises(NotImplementedError):
+        sg.LogLike(aln, tree, [[base] * len(tree.parentIndex)])
+
+
+def test_mixture_posterior_device_and_oracle():
+    w = synth.plain_small(seed=14, C=500)
+    aln, tree, base = w['alignment'], w['tree'], w['model']
+    rates, weights = sg.gamma_rate_categories(0.4, 6)
+    ms = [sg.scale_model(base, r) for r in rates]
+    lw = np.log(weights)
+    ot = oracle.Tree(tree.parentIndex, tree.distanceToParent)
+    ref = oracle.MixturePosterior(aln, ot, [oracle.scale_model(base._asdict(), r) for r in rates], lw)
+    host = sg.MixturePosterior(aln, tree, ms, lw)
+    np.testing.assert_allclose(host, ref, atol=1e-4)
+    np.testing.assert_allclose(host.sum(0), 1.0, atol=1e-5)
+    dev = sg.MixturePosterior(torch.as_tensor(aln).cuda(), tree, ms, lw)
+    torch.cuda.synchronize()
+    np.testing.assert_allclose(dev.cpu().numpy(), host, atol=1e-6)

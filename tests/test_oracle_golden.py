@@ -97,3 +97,38 @@ def test_validate_binary_tree_rejects():
     with pytest.raises(ValueError):
         oracle.validate_binary_tree([-1, 0, 0, 0])
     oracle.validate_binary_tree([-1, 0, 0, 1, 1])
+
+
+MIXTURE_DIR = os.path.join(os.path.dirname(__file__), "golden", "mixture")
+
+
+@pytest.mark.parametrize("name", ["ref_7node_mixture_jc4", "gamma4_hky"])
+def test_mixture_matches_reference_oracle(name):
+    with np.load(os.path.join(MIXTURE_DIR, name + ".npz")) as z:
+        g = {k: z[k] for k in z.files}
+    tree = oracle.Tree(g['parentIndex'], g['distanceToParent'])
+    base = {k: g[k] for k in ('eigenvalues', 'eigenvectors', 'pi')}
+    ms = [oracle.scale_model(base, r) for r in g['rates']]
+    np.testing.assert_allclose(np.stack([oracle.LogLike(g['alignment'], tree, m) for m in ms]), g['log_likes'],
+                               rtol=1e-12, atol=1e-12)
+    np.testing.assert_allclose(oracle.MixturePosterior(g['alignment'], tree, ms, g['log_weights']),
+                               g['posteriors'], rtol=1e-12, atol=1e-14)
+
+
+def test_gamma_rate_categories_match_reference_oracle():
+    with np.load(os.path.join(MIXTURE_DIR, "gamma_categories.npz")) as z:
+        for a, r in zip(z['alpha'], z['rates']):
+            np.testing.assert_allclose(oracle.gamma_rate_categories(float(a), 4)[0], r, rtol=1e-14)
+
+
+@pytest.mark.skipif(not os.path.isdir(REF_GOLDEN), reason="reference tree not mounted")
+def test_reference_mixture_json():
+    with open(os.path.join(REF_GOLDEN, "7node_mixture_jc4.json")) as f:
+        gj = json.load(f)
+    inp, out = gj['inputs'], gj['outputs']
+    base = {k: np.asarray(v) for k, v in inp['base_model'].items()}
+    ms = [oracle.scale_model(base, r) for r in inp['rates']]
+    tree = oracle.Tree(inp['parentIndex'], inp['distanceToParent'])
+    aln = np.asarray(inp['alignment'], dtype=np.int32)
+    np.testing.assert_allclose(oracle.MixturePosterior(aln, tree, ms, np.asarray(inp['log_weights'])),
+                               np.asarray(out['posteriors']), rtol=1e-12, atol=1e-14)

@@ -107,6 +107,18 @@ int subby_plan_create(const int32_t *parent_index, const double *distances,
 int subby_plan_create_irrev(const int32_t *parent_index, const double *distances, const double *eigenvalues,
                             const double *eigenvectors, const double *eigenvectors_inv, const double *pi, int R,
                             int A, subby_plan **out);
+/*
+ * Per-branch models (the reference's (1, R) model grid,
+ * subby/jax/__init__.py:74-152): node n's reversible system
+ * eigenvalues[n*A ..], eigenvectors[n*A*A ..] (row-major), pi[n*A ..] gives
+ * M_n; the root prior is node 0's pi.  LogLike, RootProb and posteriors run
+ * the usual kernels on the per-node M(t); Counts and per-branch counts run
+ * the complex accumulation once per group of branches sharing a system
+ * (each branch projected and back-transformed in its own eigenbasis).  The
+ * F81 fast path and the gradient return errors.
+ */
+int subby_plan_create_rows(const int32_t *parent_index, const double *distances, const double *eigenvalues,
+                           const double *eigenvectors, const double *pi, int R, int A, subby_plan **out);
 int subby_plan_destroy(subby_plan *plan);
 /* Bytes of device memory the plan currently holds (tables + workspace). */
 size_t subby_plan_device_bytes(const subby_plan *plan);

@@ -775,3 +775,54 @@ def Counts_per_column(alignment, tree, models, f81_fast=False, branch_mask="auto
             np.asarray(branch_mask)[:, c:c + 1]
         cols.append(Counts(alignment[:, c:c + 1], tree, models[c], f81_fast=f81_fast, branch_mask=bm))
     return np.concatenate(cols, axis=-1)
+
+
+def _rows_sub_matrices(models_row, distances):
+    """M_n from node n's own model (subby/jax/__init__.py:74-101)."""
+    d = np.asarray(distances, dtype=np.float64)
+    return np.stack([_sub_matrices(models_row[n], d[n:n + 1])[0] for n in range(len(d))])
+
+
+def LogLike_rows(alignment, tree, models_row):
+    """Per-branch models, the (1, R) model grid (subby/jax/__init__.py:
+    230-244): root prior models_row[0]['pi']."""
+    M = _rows_sub_matrices(models_row, tree.distanceToParent)
+    return upward_pass(alignment, tree, M, models_row[0]['pi'])[2]
+
+
+def RootProb_rows(alignment, tree, models_row):
+    M = _rows_sub_matrices(models_row, tree.distanceToParent)
+    pi0 = np.asarray(models_row[0]['pi'])
+    U, lnU, lnL = upward_pass(alignment, tree, M, pi0)
+    return (pi0[None, :] * U[0] * np.exp(lnU[0] - lnL)[:, None]).T
+
+
+def BranchCounts_rows(alignment, tree, models_row):
+    """Per-branch counts, each branch in its own model's eigenbasis, unmasked
+    (subby/jax/__init__.py:104-152)."""
+    M = _rows_sub_matrices(models_row, tree.distanceToParent)
+    U, lnU, lnL = upward_pass(alignment, tree, M, models_row[0]['pi'])
+    D, lnD = downward_pass(U, lnU, tree, M, models_row[0]['pi'], alignment)
+    R, C, A = U.shape
+    out = np.zeros((R, A, A, C))
+    d = tree.distanceToParent
+    for n in range(1, R):
+        m = models_row[n]
+        J = compute_J(m['eigenvalues'], d[n:n + 1])[0]
+        Ut, Dt = eigenbasis_project(U[n], D[n], m)
+        s = np.exp(lnD[n] + lnU[n] - lnL)
+        Cn = np.einsum('ck,kl,cl->klc', Dt * s[:, None], J, Ut)
+        out[n] = back_transform(Cn, m)
+    return out
+
+
+def Counts_rows(alignment, tree, models_row, branch_mask="auto"):
+    """Per-branch counts times the mask, summed (subby/jax/__init__.py:
+    356-369)."""
+    bc = BranchCounts_rows(alignment, tree, models_row)
+    A = bc.shape[1]
+    if isinstance(branch_mask, str) and branch_mask == "auto":
+        branch_mask = compute_branch_mask(alignment, tree.parentIndex, A)
+    if branch_mask is not None:
+        bc = bc * np.asarray(branch_mask)[:, None, None, :]
+    return bc.sum(0)

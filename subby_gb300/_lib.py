@@ -19,7 +19,7 @@ COUNTS_EIGEN, COUNTS_F81 = 0, 1
 
 # Exported symbols, as declared in include/subby_gb300.h.
 EXPORTS = (
-    "subby_version", "subby_strerror", "subby_last_error", "subby_plan_create", "subby_plan_create_irrev",
+    "subby_version", "subby_strerror", "subby_last_error", "subby_plan_create", "subby_plan_create_irrev", "subby_plan_create_rows",
     "subby_plan_destroy", "subby_plan_device_bytes", "subby_plan_trim", "subby_plan_branch_counts",
     "subby_plan_posteriors", "subby_plan_status", "subby_plan_run", "subby_plan_grad",
     "subby_loglike", "subby_counts", "subby_rootprob", "subby_last_launch_count",
@@ -57,6 +57,8 @@ def _declare(lib):
     lib.subby_debug_set_kernel.argtypes = [ct.c_int]
     lib.subby_plan_create.restype = ct.c_int
     lib.subby_plan_create.argtypes = [_p, _p, _p, _p, _p, ct.c_int, ct.c_int, ct.POINTER(ct.c_void_p)]
+    lib.subby_plan_create_rows.restype = ct.c_int
+    lib.subby_plan_create_rows.argtypes = [_p, _p, _p, _p, _p, ct.c_int, ct.c_int, ct.POINTER(ct.c_void_p)]
     lib.subby_plan_create_irrev.restype = ct.c_int
     lib.subby_plan_create_irrev.argtypes = [_p, _p, _p, _p, _p, _p, ct.c_int, ct.c_int, ct.POINTER(ct.c_void_p)]
     lib.subby_plan_destroy.restype = ct.c_int

@@ -59,6 +59,9 @@ class Plan:
 
     def __init__(self, tree, model, device=None):
         lib = _lib.load()
+        if isinstance(model, (list, tuple)) and not hasattr(model, '_fields'):
+            self._init_rows(tree, model, device)
+            return
         m = ensure_diag(model)
         self.parentIndex = _np(tree.parentIndex, np.int32)
         self.distances = _np(tree.distanceToParent, np.float64)
@@ -95,6 +98,32 @@ class Plan:
                     _ptr(self.parentIndex), _ptr(self.distances), _ptr(self.eigenvalues),
                     _ptr(self.eigenvectors), _ptr(self.pi), self.R, self.A, ct.byref(self._handle)),
                     "subby_plan_create")
+
+    def _init_rows(self, tree, models_row, device):
+        """Per-branch models: one reversible model per node (node 0's pi is
+        the root prior)."""
+        lib = _lib.load()
+        ms = [ensure_diag(m) for m in models_row]
+        if any(isinstance(m, IrrevDiagModel) for m in ms):
+            raise NotImplementedError("per-branch irreversible models are not supported")
+        self.parentIndex = _np(tree.parentIndex, np.int32)
+        self.distances = _np(tree.distanceToParent, np.float64)
+        self.R = int(self.parentIndex.shape[0])
+        if len(ms) != self.R:
+            raise ValueError(f"expected {self.R} per-branch models, got {len(ms)}")
+        self.irreversible = False
+        self.eigenvalues = np.ascontiguousarray(np.stack([np.asarray(m.eigenvalues, np.float64) for m in ms]))
+        self.eigenvectors = np.ascontiguousarray(np.stack([np.asarray(m.eigenvectors, np.float64) for m in ms]))
+        self.pi = np.ascontiguousarray(np.stack([np.asarray(m.pi, np.float64) for m in ms]))
+        self.A = int(self.pi.shape[1])
+        self.device = device
+        self._handle = ct.c_void_p()
+        self._lock = threading.Lock()
+        with _device_ctx(device):
+            _lib.check(lib.subby_plan_create_rows(
+                _ptr(self.parentIndex), _ptr(self.distances), _ptr(self.eigenvalues), _ptr(self.eigenvectors),
+                _ptr(self.pi), self.R, self.A, ct.byref(self._handle)), "subby_plan_create_rows")
+        self.pi = self.pi[0]
 
     # ------------------------------------------------------------------ run
     def run(self, alignment, loglike=True, counts=False, rootprob=False, f81=False,
@@ -404,8 +433,51 @@ def _device_of(x):
     return None
 
 
-def _grid_unsupported():
-    raise NotImplementedError("model grids (per-branch models) are not supported")
+def _rows_plan(tree, models_row, device):
+    """Cached plan for per-branch models (the (1, R) model grid)."""
+    ms = [ensure_diag(m) for m in models_row]
+    h = hashlib.sha1()
+    for m in ms:
+        h.update(batch._key(m).encode())
+    k = _key(tree, ms[0], device) + "/rows/" + h.hexdigest()
+    with _cache_lock:
+        p = _cache.get(k)
+        if p is not None:
+            _cache.move_to_end(k)
+            return p
+    p = Plan(tree, ms, device)
+    with _cache_lock:
+        _cache[k] = p
+        while len(_cache) > _PLAN_CACHE_SIZE:
+            _cache.popitem(last=False)[1].close()
+    return p
+
+
+def _grid(alignment, tree, grid, fn, out_shape):
+    """Model grid: (1, R) per-branch models for every column, or (C, R) per
+    column (columns grouped by identical rows).  fn(plan, sub_alignment,
+    column indices) -> result for those columns."""
+    dev = _device_of(alignment)
+    C = int(alignment.shape[1])
+    if len(grid) == 1:
+        return fn(_rows_plan(tree, grid[0], dev), alignment, None)
+    if len(grid) != C:
+        raise ValueError(f"model grid has {len(grid)} columns but the alignment has {C}")
+    groups = OrderedDict()
+    for c, row in enumerate(grid):
+        key = "/".join(batch._key(ensure_diag(m)) for m in row)
+        groups.setdefault(key, (row, []))[1].append(c)
+    out = batch._new(alignment, out_shape)
+    for row, idx in groups.values():
+        bm_idx = idx
+        batch._put(out, idx, fn(_rows_plan(tree, row, dev), batch._take(alignment, idx), bm_idx))
+    return out
+
+
+def _slice_mask(branch_mask, idx):
+    if idx is None or branch_mask is None or isinstance(branch_mask, str):
+        return branch_mask
+    return batch._take(branch_mask, idx)
 
 
 def LogLike(alignment, tree: Tree, model, maxChunkSize: int = 128):
@@ -414,7 +486,8 @@ def LogLike(alignment, tree: Tree, model, maxChunkSize: int = 128):
     del maxChunkSize  # columns are tiled on the device
     k = batch.kind(model)
     if k == 'grid':
-        _grid_unsupported()
+        return _grid(alignment, tree, model, lambda p, a, idx: p.run(a, loglike=True)['logLike'],
+                     (int(alignment.shape[1]),))
     if k == 'list':
         return batch.loglike_list(alignment, tree, model, get_plan)
     dev = _device_of(alignment)
@@ -430,7 +503,10 @@ def Counts(alignment, tree: Tree, model, maxChunkSize: int = 128, f81_fast_flag:
     del maxChunkSize
     k = batch.kind(model)
     if k == 'grid':
-        _grid_unsupported()
+        A = len(ensure_diag(model[0][0]).pi)
+        return _grid(alignment, tree, model, lambda p, a, idx: p.run(
+            a, loglike=False, counts=True, f81=f81_fast_flag, branch_mask=_slice_mask(branch_mask, idx))['counts'],
+            (A, A, int(alignment.shape[1])))
     if k == 'list':
         return batch.counts_list(alignment, tree, model, get_plan, f81=f81_fast_flag, branch_mask=branch_mask,
                                  exact_irreversible=exact_irreversible)
@@ -449,7 +525,10 @@ def BranchCounts(alignment, tree: Tree, model, maxChunkSize: int = 128, f81_fast
     del maxChunkSize
     k = batch.kind(model)
     if k == 'grid':
-        _grid_unsupported()
+        A = len(ensure_diag(model[0][0]).pi)
+        return _grid(alignment, tree, model, lambda p, a, idx: p.branch_counts(
+            a, f81=f81_fast_flag, branch_mask=_slice_mask(branch_mask, idx)),
+            (int(alignment.shape[0]), A, A, int(alignment.shape[1])))
     if k == 'list':
         return batch.counts_list(alignment, tree, model, get_plan, f81=f81_fast_flag, branch_mask=branch_mask,
                                  exact_irreversible=exact_irreversible, per_branch=True)
@@ -464,7 +543,9 @@ def RootProb(alignment, tree: Tree, model, maxChunkSize: int = 128):
     del maxChunkSize
     k = batch.kind(model)
     if k == 'grid':
-        _grid_unsupported()
+        A = len(ensure_diag(model[0][0]).pi)
+        return _grid(alignment, tree, model, lambda p, a, idx: p.run(a, loglike=False, rootprob=True)['rootProb'],
+                     (A, int(alignment.shape[1])))
     if k == 'list':
         return batch.rootprob_list(alignment, tree, model, get_plan)
     dev = _device_of(alignment)

@@ -10,7 +10,10 @@ The reference accepts, besides one model (subby/jax/__init__.py:53-205):
   column (subby/jax/__init__.py:267-277), RootProb multiplies by each
   column's own pi (:617-633), Counts and BranchCounts run column by column
   with the column's own model (:396-411, :497-512);
-* ``MixturePosterior`` over K models (:653-678).
+* ``MixturePosterior`` over K models (:653-678);
+* a model grid: ``[[m_0, ..., m_{R-1}]]`` gives node n (the branch above
+  it) its own model for every column, ``[[...], ...]`` (C rows) such a list
+  per column (:74-152, :225-261).
 
 Here a ``*H`` batch runs one resident plan per batch member, each over all
 columns, with the results stacked on the device (no host round trip for
@@ -20,7 +23,10 @@ and the results are scattered back — K distinct models cost K fused launches
 instead of the reference's per-column loop.  The first-model root prior of
 LogLike / RootProb is applied exactly from the group's own LogLike and root
 posterior: with q = pi_g U / P_g, P_0 / P_g = sum_a q_a pi0_a / pi_g,a.
-Model grids (per-branch models) raise ``NotImplementedError``.
+A model grid runs a per-branch plan (``subby_plan_create_rows``): M_n from
+node n's model, the complex accumulation once per group of branches that
+share a model, each branch in its own eigenbasis; a (C, R) grid groups the
+columns by identical rows.
 """
 from __future__ import annotations
 

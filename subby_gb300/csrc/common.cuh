@@ -112,6 +112,9 @@ struct KParams {
   // reference's formula (0) or the expected counts of M(t) itself (1)
   const float2 *cx;
   int cx_exact;
+  const float2 *cx_tab;   // the system's tables (V, Vinv, rate, Vinv^T, V^T, FP64 copies)
+  const int *cx_br;       // branches of this system; the kernels take list slots [n_lo, n_hi)
+  int cx_accum;           // add the summed counts to the output instead of storing
 };
 
 // launchers (k_small.cu / k_warp.cu)

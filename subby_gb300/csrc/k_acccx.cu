@@ -9,6 +9,9 @@
 //   counts_ij = Re (V C Vinv)_ij on the diagonal, Re R_ij (V C Vinv)_ij off
 //   it, R = V diag(mu) Vinv.
 //
+// Per-branch models run one launch per group of branches sharing a system
+// (P.cx_tab, P.cx_br), the summed counts accumulating in the output.
+//
 // Layout: a CTA of 256 threads holds G columns; the A^2 complex entries of a
 // column's C are split over TPC = A^2 / 16 threads (16 entries each, in
 // registers).  Per branch the CTA projects its columns' D and U into shared
@@ -55,9 +58,10 @@ constexpr size_t cx_smem() {
   return (size_t)(2 * A * A + 2 * Gm::G * 2 * A + Gm::G * A * A) * sizeof(float2);
 }
 
-// PB: per-branch counts (R, A, A, C) instead of the sum over branches;
-// CBUF: write the summed C of branches [n_lo, n_hi) to cbuf ([column][A*A]
-// complex) instead of back-transforming it
+// Branches: P.cx_br[n_lo .. n_hi) (the branches of one system).  PB:
+// per-branch counts (R, A, A, C) instead of their sum; CBUF: write the
+// summed C to cbuf ([column][A*A] complex) instead of back-transforming it;
+// P.cx_accum: add the summed counts to the output.
 template <int A, bool PB, bool CBUF>
 __global__ void __launch_bounds__(kCxThreads) k_acc_cx(const KParams P, const float *__restrict__ sa,
                                                        const float *__restrict__ sb, int c_base, int c_count,
@@ -70,7 +74,7 @@ __global__ void __launch_bounds__(kCxThreads) k_acc_cx(const KParams P, const fl
   float2 *sP = sVi + A * A;           // [2][G][2A]: D~ (k < A), U~ (A + l)
   float2 *sC = sP + 2 * G * 2 * A;    // [G][A][A]: C, then T = C Vinv
   const float2 *J = P.cx;
-  const float2 *T0 = P.cx + (size_t)P.R * A * A;  // V, Vinv, R, Vinv^T, V^T
+  const float2 *T0 = P.cx_tab;  // V, Vinv, R, Vinv^T, V^T
   const float2 *Vg = T0 + (P.cx_exact ? 3 : 0) * A * A;
   const float2 *Vig = Vg + A * A;
   const float2 *Rg = T0 + 2 * A * A;
@@ -117,7 +121,9 @@ __global__ void __launch_bounds__(kCxThreads) k_acc_cx(const KParams P, const fl
         float2 s = make_float2(0.f, 0.f);
 #pragma unroll 4
         for (int k = 0; k < A; ++k) s = cfma(sV[ii * A + k], myC[k * A + j], s);
-        out[(size_t)e * C] = (ii == j) ? s.x : cmul(__ldg(Rg + e), s).x;
+        const float v = (ii == j) ? s.x : cmul(__ldg(Rg + e), s).x;
+        if (!PB && P.cx_accum) out[(size_t)e * C] += v;
+        else out[(size_t)e * C] = v;
       }
     }
   };
@@ -130,8 +136,9 @@ __global__ void __launch_bounds__(kCxThreads) k_acc_cx(const KParams P, const fl
     float2 acc[kCxE];
 #pragma unroll
     for (int i = 0; i < kCxE; ++i) acc[i] = make_float2(0.f, 0.f);
-    for (int n = n_lo; n < n_hi; ++n) {
-      float2 *buf = sP + ((size_t)(n & 1) * G + g) * 2 * A;
+    for (int bi = n_lo; bi < n_hi; ++bi) {
+      const int n = __ldg(P.cx_br + bi);
+      float2 *buf = sP + ((size_t)(bi & 1) * G + g) * 2 * A;
       if (busy) {
         const size_t srow = ((size_t)(n - 1) * c_count + ccl) * A;
         for (int o = p; o < 2 * A; o += TPC) {
@@ -196,10 +203,10 @@ __global__ void __launch_bounds__(kCxThreads) k_bt_cx(const KParams P, const flo
   double2 *sVi = sV + A * A;    // A x A
   double2 *sT = sVi + A * A;    // A x A
   float2 *sCc = reinterpret_cast<float2 *>(sT + A * A);  // A x A
-  const double2 *D0 = reinterpret_cast<const double2 *>(P.cx + (size_t)(P.R + 5) * A * A);  // V, Vinv, Vinv^T, V^T
+  const double2 *D0 = reinterpret_cast<const double2 *>(P.cx_tab + (size_t)5 * A * A);  // V, Vinv, Vinv^T, V^T
   const double2 *Vg = D0 + (P.cx_exact ? 2 : 0) * A * A;
   const double2 *Vig = Vg + A * A;
-  const float2 *Rg = P.cx + (size_t)(P.R + 2) * A * A;
+  const float2 *Rg = P.cx_tab + (size_t)2 * A * A;
   const int t = threadIdx.x;
   for (int e = t; e < A * A; e += blockDim.x) {
     sV[e] = Vg[e];

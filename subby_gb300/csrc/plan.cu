@@ -245,6 +245,13 @@ struct subby_plan {
   // the complex tables of the counts (J (R x A x A), V, V^-1, rate matrix)
   bool irrev = false;
   float2 *d_cx = nullptr;
+  // per-branch models (rows): the tree's branches grouped by distinct model;
+  // group g's complex tables at d_cx + (R + 13 g) A^2, its branches at
+  // d_grp_br[grp_off[g] .. grp_off[g + 1]); counts use the exact formula
+  bool rows = false;
+  int ngroups = 1;
+  std::vector<int> grp_off;
+  int *d_grp_br = nullptr;
   TableOffsets off{};
   float *d_tab = nullptr;
   double *d_tab64 = nullptr;
@@ -326,9 +333,12 @@ int subby_last_launch_count(void) { return g_launches; }
 
 namespace {
 
-// Irreversible input: complex eigenvalues, V and V^-1 (interleaved re, im).
+// Complex-eigensystem input: eigenvalues, V and V^-1 (interleaved re, im),
+// one system for every branch, or (per_row) one per node n at offsets
+// n A / n A^2 (complex values).
 struct IrrevInput {
   const double *mu, *V, *Vi;
+  int per_row;
 };
 
 int plan_create(const int32_t *parent, const double *dist, const double *evals, const double *evecs,
@@ -352,6 +362,7 @@ int plan_create(const int32_t *parent, const double *dist, const double *evals, 
   P->R = R;
   P->A = A;
   P->irrev = ir != nullptr;
+  P->rows = ir && ir->per_row;
   cudaGetDevice(&P->device);
   cudaDeviceGetAttribute(&P->nsm, cudaDevAttrMultiProcessorCount, P->device);
   P->root_is_leaf = (R == 1);
@@ -588,30 +599,70 @@ int plan_create(const int32_t *parent, const double *dist, const double *evals, 
   }
   std::vector<float> hMT, hMN;
   std::vector<float2> hcx;
+  std::vector<int> grp_br;
   if (ir) {
     // M_n = Re V diag(e^{mu t_n}) V^-1 and the complex tables, in FP64
-    // (subby/oracle/oracle.py:474-534, 642-693)
+    // (subby/oracle/oracle.py:474-534, 642-693); per-row systems for
+    // per-branch models
     using cd = std::complex<double>;
-    std::vector<cd> mu(A), V((size_t)A * A), Vi((size_t)A * A), E(A), w(A);
-    for (int k = 0; k < A; ++k) mu[k] = cd(ir->mu[2 * k], ir->mu[2 * k + 1]);
-    for (int i = 0; i < A * A; ++i) {
-      V[i] = cd(ir->V[2 * i], ir->V[2 * i + 1]);
-      Vi[i] = cd(ir->Vi[2 * i], ir->Vi[2 * i + 1]);
+    const size_t AA = (size_t)A * A;
+    auto mu_of = [&](int n, int k) {
+      const size_t q = (ir->per_row ? (size_t)n * A : 0) + k;
+      return cd(ir->mu[2 * q], ir->mu[2 * q + 1]);
+    };
+    auto V_of = [&](int n, size_t e) {
+      const size_t q = (ir->per_row ? (size_t)n * AA : 0) + e;
+      return cd(ir->V[2 * q], ir->V[2 * q + 1]);
+    };
+    auto Vi_of = [&](int n, size_t e) {
+      const size_t q = (ir->per_row ? (size_t)n * AA : 0) + e;
+      return cd(ir->Vi[2 * q], ir->Vi[2 * q + 1]);
+    };
+    // groups of branches with identical systems (one group for a single model)
+    std::vector<int> grp_of(R, 0), rep;  // rep[g]: a node of group g
+    if (ir->per_row && R > 1) {
+      for (int n = 1; n < R; ++n) {
+        int g = -1;
+        for (int h = 0; h < (int)rep.size() && g < 0; ++h) {
+          const int m = rep[h];
+          bool same = std::memcmp(ir->mu + 2 * (size_t)n * A, ir->mu + 2 * (size_t)m * A, 2 * A * sizeof(double)) == 0 &&
+                      std::memcmp(ir->V + 2 * (size_t)n * AA, ir->V + 2 * (size_t)m * AA, 2 * AA * sizeof(double)) == 0 &&
+                      std::memcmp(ir->Vi + 2 * (size_t)n * AA, ir->Vi + 2 * (size_t)m * AA, 2 * AA * sizeof(double)) == 0;
+          if (same) g = h;
+        }
+        if (g < 0) {
+          g = (int)rep.size();
+          rep.push_back(n);
+        }
+        grp_of[n] = g;
+      }
+    } else {
+      rep.push_back(R > 1 ? 1 : 0);
+    }
+    P->ngroups = (int)rep.size();
+    P->grp_off.assign(P->ngroups + 1, 0);
+    for (int n = 1; n < R; ++n) P->grp_off[grp_of[n] + 1]++;
+    for (int g = 0; g < P->ngroups; ++g) P->grp_off[g + 1] += P->grp_off[g];
+    grp_br.assign(std::max(R - 1, 1), 0);
+    {
+      std::vector<int> fill(P->grp_off.begin(), P->grp_off.end() - 1);
+      for (int n = 1; n < R; ++n) grp_br[fill[grp_of[n]]++] = n;
     }
     hMT.assign((size_t)R * (A + 1) * A, 0.f);
     hMN.assign((size_t)R * A * A, 0.f);
-    // float2: J (R A^2), V, Vinv, rate, Vinv^T, V^T; then FP64 pairs: V,
-    // Vinv, Vinv^T, V^T (two float2 slots per value)
-    hcx.assign((size_t)(R + 13) * A * A, make_float2(0.f, 0.f));
+    // float2: J (R A^2), then per group 13 A^2: V, Vinv, rate, Vinv^T, V^T;
+    // FP64 pairs of V, Vinv, Vinv^T, V^T (two float2 slots per value)
+    hcx.assign((size_t)(R + 13 * P->ngroups) * AA, make_float2(0.f, 0.f));
+    std::vector<cd> E(A), w(A);
     for (int n = 0; n < R; ++n) {
       const double t = dist[n];
-      for (int k = 0; k < A; ++k) E[k] = std::exp(mu[k] * t);
+      for (int k = 0; k < A; ++k) E[k] = std::exp(mu_of(n, k) * t);
       for (int b = 0; b < A; ++b) {
-        for (int k = 0; k < A; ++k) w[k] = V[b * A + k] * E[k];
+        for (int k = 0; k < A; ++k) w[k] = V_of(n, (size_t)b * A + k) * E[k];
         double rs = 0.0;
         for (int j = 0; j < A; ++j) {
           cd sum = 0.0;
-          for (int k = 0; k < A; ++k) sum += w[k] * Vi[k * A + j];
+          for (int k = 0; k < A; ++k) sum += w[k] * Vi_of(n, (size_t)k * A + j);
           const double m = sum.real();
           hMT[((size_t)n * (A + 1) + j) * A + b] = (float)m;
           hMN[((size_t)n * A + b) * A + j] = (float)m;
@@ -621,40 +672,46 @@ int plan_create(const int32_t *parent, const double *dist, const double *evals, 
       }
       for (int k = 0; k < A; ++k)
         for (int l = 0; l < A; ++l) {
-          const cd d = mu[k] - mu[l];
+          const cd d = mu_of(n, k) - mu_of(n, l);
           const cd J = std::abs(d) < 1e-8 ? t * E[k] : (E[k] - E[l]) / d;
           hcx[((size_t)n * A + k) * A + l] = make_float2((float)J.real(), (float)J.imag());
         }
     }
-    float2 *cV = hcx.data() + (size_t)R * A * A, *cVi = cV + A * A, *cR = cVi + A * A, *cViT = cR + A * A,
-           *cVT = cViT + A * A;
-    double *d64 = reinterpret_cast<double *>(hcx.data() + (size_t)(R + 5) * A * A);  // 4 blocks of A^2 pairs
     auto f2 = [](cd z) { return make_float2((float)z.real(), (float)z.imag()); };
-    auto put64 = [&](int blk, int e, cd z) {
-      d64[2 * ((size_t)blk * A * A + e)] = z.real();
-      d64[2 * ((size_t)blk * A * A + e) + 1] = z.imag();
-    };
-    for (int i = 0; i < A; ++i)
-      for (int j = 0; j < A; ++j) {
-        cd r = 0.0;
-        for (int k = 0; k < A; ++k) r += V[i * A + k] * mu[k] * Vi[k * A + j];
-        const int e = i * A + j;
-        cV[e] = f2(V[e]);
-        cVi[e] = f2(Vi[e]);
-        cR[e] = f2(r);
-        cViT[e] = f2(Vi[j * A + i]);
-        cVT[e] = f2(V[j * A + i]);
-        put64(0, e, V[e]);
-        put64(1, e, Vi[e]);
-        put64(2, e, Vi[j * A + i]);
-        put64(3, e, V[j * A + i]);
-      }
+    for (int g = 0; g < P->ngroups; ++g) {
+      const int n = rep[g];
+      float2 *cV = hcx.data() + (size_t)(R + 13 * g) * AA, *cVi = cV + AA, *cR = cVi + AA, *cViT = cR + AA,
+             *cVT = cViT + AA;
+      double *d64 = reinterpret_cast<double *>(cV + 5 * AA);  // 4 blocks of A^2 pairs
+      auto put64 = [&](int blk, size_t e, cd z) {
+        d64[2 * ((size_t)blk * AA + e)] = z.real();
+        d64[2 * ((size_t)blk * AA + e) + 1] = z.imag();
+      };
+      for (int i = 0; i < A; ++i)
+        for (int j = 0; j < A; ++j) {
+          cd r = 0.0;
+          for (int k = 0; k < A; ++k) r += V_of(n, (size_t)i * A + k) * mu_of(n, k) * Vi_of(n, (size_t)k * A + j);
+          const size_t e = (size_t)i * A + j, et = (size_t)j * A + i;
+          cV[e] = f2(V_of(n, e));
+          cVi[e] = f2(Vi_of(n, e));
+          cR[e] = f2(r);
+          cViT[e] = f2(Vi_of(n, et));
+          cVT[e] = f2(V_of(n, et));
+          put64(0, e, V_of(n, e));
+          put64(1, e, Vi_of(n, e));
+          put64(2, e, Vi_of(n, et));
+          put64(3, e, V_of(n, et));
+        }
+    }
     e = cudaMemcpyAsync(P->d_tab + o.MT, hMT.data(), hMT.size() * sizeof(float), cudaMemcpyHostToDevice, qs);
     if (e == cudaSuccess)
       e = cudaMemcpyAsync(P->d_tab + o.MN, hMN.data(), hMN.size() * sizeof(float), cudaMemcpyHostToDevice, qs);
     if (e == cudaSuccess) e = pool_alloc((void **)&P->d_cx, hcx.size() * sizeof(float2), P->pool, qs);
     if (e == cudaSuccess)
       e = cudaMemcpyAsync(P->d_cx, hcx.data(), hcx.size() * sizeof(float2), cudaMemcpyHostToDevice, qs);
+    if (e == cudaSuccess) e = pool_alloc((void **)&P->d_grp_br, grp_br.size() * sizeof(int), P->pool, qs);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(P->d_grp_br, grp_br.data(), grp_br.size() * sizeof(int), cudaMemcpyHostToDevice, qs);
     if (e != cudaSuccess) return cleanup(cuda_fail(e, "irreversible table upload"));
   }
   {
@@ -720,7 +777,34 @@ int subby_plan_create_irrev(const int32_t *parent, const double *dist, const dou
   // complex eigensystem
   std::vector<double> ev0((size_t)A, 0.0), eye((size_t)A * A, 0.0);
   for (int a = 0; a < A; ++a) eye[(size_t)a * A + a] = 1.0;
-  const IrrevInput ir{eigenvalues, eigenvectors, eigenvectors_inv};
+  const IrrevInput ir{eigenvalues, eigenvectors, eigenvectors_inv, 0};
+  return plan_create(parent, dist, ev0.data(), eye.data(), pi, R, A, out, &ir);
+}
+
+int subby_plan_create_rows(const int32_t *parent, const double *dist, const double *eigenvalues,
+                           const double *eigenvectors, const double *pi, int R, int A, subby_plan **out) {
+  g_last_error.clear();
+  if (!parent || !dist || !eigenvalues || !eigenvectors || !pi || !out) return fail(SUBBY_ERR_ARG, "null argument");
+  if (!(A >= 2 && A <= 64) || R < 1) return fail(SUBBY_ERR_UNSUPPORTED, "alphabet size out of range");
+  // node n's reversible system as V = diag(pi)^-1/2 W, V^-1 = W^T diag(pi)^1/2
+  const size_t AA = (size_t)A * A;
+  std::vector<double> mu((size_t)2 * R * A, 0.0), V(2 * R * AA, 0.0), Vi(2 * R * AA, 0.0);
+  for (int n = 0; n < R; ++n) {
+    const double *W = eigenvectors + (size_t)n * AA, *p = pi + (size_t)n * A;
+    for (int a = 0; a < A; ++a) {
+      if (!(p[a] > 0.0)) return fail(SUBBY_ERR_ARG, "pi must be strictly positive");
+      mu[2 * ((size_t)n * A + a)] = eigenvalues[(size_t)n * A + a];
+    }
+    for (int i = 0; i < A; ++i)
+      for (int k = 0; k < A; ++k) {
+        V[2 * ((size_t)n * AA + (size_t)i * A + k)] = W[(size_t)i * A + k] / std::sqrt(p[i]);
+        Vi[2 * ((size_t)n * AA + (size_t)k * A + i)] = W[(size_t)i * A + k] * std::sqrt(p[i]);
+      }
+  }
+  std::vector<double> ev0((size_t)A, 0.0), eye(AA, 0.0);
+  for (int a = 0; a < A; ++a) eye[(size_t)a * A + a] = 1.0;
+  const IrrevInput ir{mu.data(), V.data(), Vi.data(), 1};
+  // the root prior is node 0's pi
   return plan_create(parent, dist, ev0.data(), eye.data(), pi, R, A, out, &ir);
 }
 
@@ -735,7 +819,8 @@ int subby_plan_destroy(subby_plan *P) {
   if (s && P->used) cudaStreamWaitEvent(s, P->last_use, 0);
   if (P->s_in) cudaStreamSynchronize(P->s_in);
   if (P->s_out) cudaStreamSynchronize(P->s_out);
-  void *bufs[] = {P->d_tab, P->d_tab64, P->d_steps, P->d_slots, P->d_prog, P->d_tab16, P->d_err, P->d_cx};
+  void *bufs[] = {P->d_tab, P->d_tab64, P->d_steps, P->d_slots, P->d_prog, P->d_tab16, P->d_err, P->d_cx,
+                  P->d_grp_br};
   for (void *b : bufs)
     if (b) cudaFreeAsync(b, s);
   P->work.release(s);
@@ -1218,10 +1303,10 @@ int run_cx(subby_plan *P, const int32_t *d_aln, int C, float *d_logL, float *d_c
   KParams k = walk_params(P, d_aln, C, mode & (kModeLogLike | kModeRootProb), mask_mode, d_mask, d_logL, d_counts,
                           d_root);
   k.cx = P->d_cx;
-  k.cx_exact = (mode & kModeIrrevExact) != 0;
+  k.cx_exact = P->rows || (mode & kModeIrrevExact) != 0;
   k.npost = nullptr;
   k.npost_node = -1;
-  const bool bt64 = cx_bt64(A);
+  const bool bt64 = cx_bt64(A) && !P->rows;   // per-branch reversible systems are well conditioned
   const bool tc = (A == 64) && P->d_tab16 && (g_kernel_sel == 0 || g_kernel_sel == 5);
   const int tile = big_tile();
   const int H = (A + 31) / 32;
@@ -1265,16 +1350,29 @@ int run_cx(subby_plan *P, const int32_t *d_aln, int C, float *d_logL, float *d_c
     const long long groups = (cc + G - 1) / G;
     const int grid = (int)std::max<long long>(1, std::min<long long>(groups, (long long)P->nsm * 2));
     if (!bt64) {
-      lr = launch_acc_cx(k, A, pb, sa, sb, c0, cc, 1, R, nullptr, grid, stream);
-      if (lr != 0)
-        return fail(SUBBY_ERR_CUDA, std::string("accumulate launch failed: ") + cudaGetErrorString((cudaError_t)lr));
-      g_launches += 1;
+      // one launch per group of branches sharing a system; the summed
+      // counts of later groups add to the earlier ones
+      for (int g = 0; g < P->ngroups; ++g) {
+        KParams kg = k;
+        kg.cx_tab = P->d_cx + (size_t)(R + 13 * g) * A * A;
+        kg.cx_br = P->d_grp_br + P->grp_off[g];
+        kg.cx_accum = g > 0;
+        const int nb = P->grp_off[g + 1] - P->grp_off[g];
+        lr = launch_acc_cx(kg, A, pb, sa, sb, c0, cc, 0, nb, nullptr, grid, stream);
+        if (lr != 0)
+          return fail(SUBBY_ERR_CUDA, std::string("accumulate launch failed: ") + cudaGetErrorString((cudaError_t)lr));
+        g_launches += 1;
+      }
       continue;
     }
+    k.cx_tab = P->d_cx + (size_t)R * A * A;
+    k.cx_br = P->d_grp_br;
+    k.cx_accum = 0;
     // FP64 back-transform: all branches at once, or branch by branch
     const int bgrid = std::max(1, std::min(cc, P->nsm));
     for (int n = pb ? 1 : 0; n < (pb ? R : 1); ++n) {
-      lr = launch_acc_cx(k, A, false, sa, sb, c0, cc, pb ? n : 1, pb ? n + 1 : R, cbuf, grid, stream);
+      // branch list d_grp_br holds 1 .. R-1 in order for a single system
+      lr = launch_acc_cx(k, A, false, sa, sb, c0, cc, pb ? n - 1 : 0, pb ? n : R - 1, cbuf, grid, stream);
       if (lr == 0) lr = launch_bt_cx(k, A, cbuf, c0, cc, pb ? n : 0, bgrid, stream);
       if (lr != 0)
         return fail(SUBBY_ERR_CUDA, std::string("accumulate launch failed: ") + cudaGetErrorString((cudaError_t)lr));

@@ -102,8 +102,9 @@ def test_reference_identities():
     ms = [sg.scale_model(base, r) for r in np.linspace(0.5, 2.0, 40)]
     by_col = np.array([sg.LogLike(aln[:, c:c + 1], tree, ms[c])[0] for c in range(40)])
     np.testing.assert_allclose(sg.LogLike(aln, tree, ms), by_col, atol=1e-5)
-    with pytest.raises(NotImplementedError):
-        sg.LogLike(aln, tree, [[base] * len(tree.parentIndex)])
+    # a (1, R) grid of one model is that model
+    np.testing.assert_allclose(sg.LogLike(aln, tree, [[base] * len(tree.parentIndex)]), sg.LogLike(aln, tree, base),
+                               atol=1e-5)
 
 
 def test_mixture_posterior_device_and_oracle():
@@ -120,3 +121,57 @@ def test_mixture_posterior_device_and_oracle():
     dev = sg.MixturePosterior(torch.as_tensor(aln).cuda(), tree, ms, lw)
     torch.cuda.synchronize()
     np.testing.assert_allclose(dev.cpu().numpy(), host, atol=1e-6)
+
+
+def _hky_rows(R, rng):
+    return [models.hky85_diag(float(rng.uniform(1.0, 4.0)), rng.dirichlet(np.full(4, 5.0))) for _ in range(R)]
+
+
+def test_per_branch_models_vs_oracle():
+    """(1, R) model grid: each branch its own HKY85 model (three distinct
+    models over the branches), A = 4; identical rows equal the single model."""
+    rng = np.random.default_rng(15)
+    tree = synth.random_tree(10, 0.2, rng)
+    R = len(tree.parentIndex)
+    palette = _hky_rows(3, rng)
+    rows = [palette[rng.integers(0, 3)] for _ in range(R)]
+    aln = synth.simulated_alignment(tree, palette[0], 90, 0.1, rng)
+    ot = oracle.Tree(tree.parentIndex, tree.distanceToParent)
+    rd = [m._asdict() for m in rows]
+    assert_loglike(sg.LogLike(aln, tree, [rows]), oracle.LogLike_rows(aln, ot, rd))
+    assert_cols(sg.RootProb(aln, tree, [rows]), oracle.RootProb_rows(aln, ot, rd), ROOTPROB_RTOL, "rootprob")
+    cnt = sg.Counts(aln, tree, [rows])
+    assert_cols(cnt, oracle.Counts_rows(aln, ot, rd), COUNTS_RTOL, "counts")
+    assert_cols(sg.Counts(aln, tree, [rows], branch_mask=None), oracle.Counts_rows(aln, ot, rd, branch_mask=None),
+                COUNTS_RTOL, "counts unmasked")
+    bc = sg.BranchCounts(aln, tree, [rows])
+    ref = oracle.BranchCounts_rows(aln, ot, rd)
+    assert_cols(bc.transpose(1, 2, 0, 3).reshape(4, 4, -1), ref.transpose(1, 2, 0, 3).reshape(4, 4, -1),
+                COUNTS_RTOL, "branch counts")
+    # identical rows: the single-model results
+    same = [rows[0]] * R
+    assert_loglike(sg.LogLike(aln, tree, [same]), sg.LogLike(aln, tree, rows[0]))
+    assert_cols(sg.Counts(aln, tree, [same]), sg.Counts(aln, tree, rows[0]), COUNTS_RTOL, "same rows")
+
+
+def test_per_branch_models_large_alphabet_and_column_grid():
+    rng = np.random.default_rng(16)
+    tree = synth.random_tree(7, 0.15, rng)
+    R = len(tree.parentIndex)
+    pal = [models.random_reversible(20, rng, 0.5, 2.0)[0] for _ in range(2)]
+    rows = [pal[n % 2] for n in range(R)]
+    aln = rng.integers(0, 22, size=(R, 37)).astype(np.int32)
+    ot = oracle.Tree(tree.parentIndex, tree.distanceToParent)
+    rd = [m._asdict() for m in rows]
+    assert_loglike(sg.LogLike(aln, tree, [rows]), oracle.LogLike_rows(aln, ot, rd))
+    assert_cols(sg.Counts(aln, tree, [rows]), oracle.Counts_rows(aln, ot, rd), COUNTS_RTOL, "A=20 rows counts")
+    # (C, R): two row sets over the columns
+    rows2 = [pal[(n + 1) % 2] for n in range(R)]
+    grid = [rows if c % 3 else rows2 for c in range(37)]
+    ll = sg.LogLike(aln, tree, grid)
+    ref = np.array([oracle.LogLike_rows(aln[:, c:c + 1], ot, [m._asdict() for m in grid[c]])[0] for c in range(37)])
+    assert_loglike(ll, ref)
+    cnt = sg.Counts(aln, tree, grid)
+    refc = np.concatenate([oracle.Counts_rows(aln[:, c:c + 1], ot, [m._asdict() for m in grid[c]])
+                           for c in range(37)], axis=-1)
+    assert_cols(cnt, refc, COUNTS_RTOL, "column grid counts")

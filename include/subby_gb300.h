@@ -157,6 +157,16 @@ int subby_plan_posteriors(subby_plan *plan, const int32_t *alignment, int C, int
  */
 int subby_mixture_posterior(const float *logL, const double *log_weights, int K, int C, float *out, int flags,
                             void *stream);
+/*
+ * Tokenise n characters on the device: out[i] = lut[chars[i]] (lut: 256
+ * device int32 entries, -1 = not in the alphabet); *first_bad (device int64,
+ * preset to -1 by the caller) receives the smallest index of a byte mapped
+ * to -1.  chars and out 16-byte aligned, device pointers; enqueued on
+ * `stream`.  The character tokenisation of subby/formats.py:228-625 for
+ * large alignments (1 byte per cell over the host link instead of 4).
+ */
+int subby_tokenize(const uint8_t *chars, int64_t n, const int32_t *lut, int32_t *out, int64_t *first_bad,
+                   void *stream);
 /* Wait for the plan's enqueued work and report SUBBY_ERR_TIMEOUT if a
  * bounded device wait (tensor-core kernels) gave up since the last check
  * (device-pointer runs return before their kernels finish, so they report

@@ -23,7 +23,7 @@ EXPORTS = (
     "subby_plan_destroy", "subby_plan_device_bytes", "subby_plan_trim", "subby_plan_branch_counts",
     "subby_plan_posteriors", "subby_plan_status", "subby_plan_run", "subby_plan_grad",
     "subby_loglike", "subby_counts", "subby_rootprob", "subby_last_launch_count",
-    "subby_debug_set_kernel", "subby_counts_noalloc", "subby_mixture_posterior",
+    "subby_debug_set_kernel", "subby_counts_noalloc", "subby_mixture_posterior", "subby_tokenize",
 )
 
 _lock = threading.Lock()
@@ -71,6 +71,8 @@ def _declare(lib):
     lib.subby_plan_status.argtypes = [_p]
     lib.subby_plan_branch_counts.restype = ct.c_int
     lib.subby_plan_branch_counts.argtypes = [_p, _p, ct.c_int, _p, ct.c_int, ct.c_int, _p, ct.c_int, _p]
+    lib.subby_tokenize.restype = ct.c_int
+    lib.subby_tokenize.argtypes = [_p, ct.c_int64, _p, _p, _p, _p]
     lib.subby_mixture_posterior.restype = ct.c_int
     lib.subby_mixture_posterior.argtypes = [_p, _p, ct.c_int, ct.c_int, _p, ct.c_int, _p]
     lib.subby_plan_posteriors.restype = ct.c_int

@@ -1,0 +1,65 @@
+// Character -> token mapping of the front-end parsers (subby/formats.py:
+// 228-625 tokenise sequence characters: alphabet index, A+1 for '-' / '.'):
+// a 256-entry table in shared memory applied to a device byte buffer, 16
+// bytes per thread per step (one 16-byte load, four 16-byte stores); bytes
+// the table maps to -1 record their smallest index in *first_bad.
+// HBM-bound: 1 byte read + 4 bytes written per cell.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+
+#include "common.cuh"
+#include "subby_gb300.h"
+
+namespace subby {
+namespace {
+
+__global__ void k_tokenize(const uint8_t *__restrict__ in, long long n, const int32_t *__restrict__ lut,
+                           int32_t *__restrict__ out, unsigned long long *first_bad) {
+  __shared__ int32_t s_lut[256];
+  for (int i = threadIdx.x; i < 256; i += blockDim.x) s_lut[i] = lut[i];
+  __syncthreads();
+  const long long nvec = n / 16;
+  unsigned long long bad = ~0ull;
+  for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < nvec;
+       v += (long long)gridDim.x * blockDim.x) {
+    const uint4 w = reinterpret_cast<const uint4 *>(in)[v];
+    const uint32_t words[4] = {w.x, w.y, w.z, w.w};
+    int32_t t[16];
+#pragma unroll
+    for (int q = 0; q < 16; ++q) {
+      t[q] = s_lut[(words[q >> 2] >> (8 * (q & 3))) & 0xffu];
+      if (t[q] < 0) bad = min(bad, (unsigned long long)(v * 16 + q));
+    }
+    int4 *o = reinterpret_cast<int4 *>(out + v * 16);
+#pragma unroll
+    for (int q = 0; q < 4; ++q) o[q] = make_int4(t[4 * q], t[4 * q + 1], t[4 * q + 2], t[4 * q + 3]);
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    for (long long i = nvec * 16; i < n; ++i) {
+      const int32_t t = s_lut[in[i]];
+      out[i] = t;
+      if (t < 0) bad = min(bad, (unsigned long long)i);
+    }
+  }
+  if (bad != ~0ull) atomicMin(first_bad, bad);
+}
+
+}  // namespace
+}  // namespace subby
+
+extern "C" int subby_tokenize(const uint8_t *chars, int64_t n, const int32_t *lut, int32_t *out,
+                              int64_t *first_bad, void *stream_) {
+  if (!chars || !lut || !out || !first_bad || n < 0) return SUBBY_ERR_ARG;
+  if ((reinterpret_cast<uintptr_t>(chars) & 15) || (reinterpret_cast<uintptr_t>(out) & 15)) return SUBBY_ERR_ARG;
+  if (n == 0) return SUBBY_OK;
+  cudaStream_t s = (cudaStream_t)stream_;
+  int dev = 0, nsm = 1;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  const int block = 256;
+  const long long nvec = std::max<long long>(1, n / 16);
+  const int grid = (int)std::min<long long>((nvec + block - 1) / block, (long long)nsm * 8);
+  subby::k_tokenize<<<grid, block, 0, s>>>(chars, n, lut, out, reinterpret_cast<unsigned long long *>(first_bad));
+  return cudaGetLastError() == cudaSuccess ? SUBBY_OK : SUBBY_ERR_CUDA;
+}

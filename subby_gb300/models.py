@@ -276,3 +276,19 @@ def unbatch(model):
     if not H:
         return H, [m]
     return H, [type(m)(**{f: np.asarray(getattr(m, f))[idx] for f in m._fields}) for idx in np.ndindex(*H)]
+
+
+def check_detailed_balance(subRate, pi, tol: float = 1e-10) -> bool:
+    """pi_i R_ij == pi_j R_ji within tol for every pair."""
+    R = np.asarray(subRate, dtype=np.float64)
+    p = np.asarray(pi, dtype=np.float64)
+    F = p[:, None] * R
+    return bool(np.all(np.abs(F - F.T) <= tol))
+
+
+def model_from_rate_matrix(subRate, pi, reversible=None, tol: float = 1e-10):
+    """DiagModel when reversible (detailed balance checked when None), else
+    IrrevDiagModel."""
+    if reversible is None:
+        reversible = check_detailed_balance(subRate, pi, tol)
+    return diagonalize_rate_matrix(subRate, pi) if reversible else diagonalize_irreversible(subRate, pi)

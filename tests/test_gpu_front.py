@@ -1,0 +1,67 @@
+"""Front-end on the GPU: the device tokeniser (subby_tokenize) against the
+host lookup, its first-bad-character report, and JSON requests
+(subby_gb300.io.run) against the reference's own io.run outputs (FP64
+oracle) stored in tests/golden/formats/formats.json.  Tolerances as
+everywhere (tests/_tol.py)."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from tests._tol import COUNTS_RTOL, ROOTPROB_RTOL, assert_cols, assert_loglike
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+if not torch.cuda.is_available():  # pragma: no cover
+    pytest.skip("needs a CUDA GPU", allow_module_level=True)
+
+from subby_gb300 import formats, io  # noqa: E402
+
+with open(os.path.join(os.path.dirname(__file__), "golden", "formats", "formats.json")) as f:
+    G = json.load(f)
+
+
+@pytest.mark.parametrize("shape", [(3, 17), (7, 1000), (64, 4099), (1, 1)])
+def test_device_tokenizer_matches_host(shape):
+    rng = np.random.default_rng(shape[1])
+    alphabet = list("ACGT")
+    chars = rng.choice(np.frombuffer(b"ACGTacgt-.", dtype=np.uint8), size=shape)
+    host = formats.tokenize(chars, alphabet)
+    dev = formats.tokenize(torch.as_tensor(chars).cuda(), alphabet)
+    torch.cuda.synchronize()
+    np.testing.assert_array_equal(dev.cpu().numpy(), host)
+    assert host.max() == 5 and host.min() == 0
+
+
+def test_device_tokenizer_reports_first_bad_character():
+    chars = np.frombuffer(b"ACGT" * 100, dtype=np.uint8).copy().reshape(4, 100)
+    chars[2, 37] = ord("X")
+    chars[3, 90] = ord("Z")
+    with pytest.raises(ValueError, match=r"Unknown character 'X' at row 2, col 37"):
+        formats.tokenize(torch.as_tensor(chars).cuda(), list("ACGT"))
+
+
+def test_large_device_tokenization():
+    n_rows, C = 255, 1 << 20
+    rng = np.random.default_rng(1)
+    chars = torch.as_tensor(rng.choice(np.frombuffer(b"ACGT-", dtype=np.uint8), size=(n_rows, C))).cuda()
+    tok = formats.tokenize(chars, list("ACGT"))
+    torch.cuda.synchronize()
+    sample = chars[:, ::4099].cpu().numpy()
+    np.testing.assert_array_equal(tok[:, ::4099].cpu().numpy(), formats.tokenize(sample, list("ACGT")))
+
+
+@pytest.mark.parametrize("case", G["requests"], ids=lambda c: c["request"]["model"].get("name", "subRate"))
+def test_requests_match_reference_io(case):
+    got = io.run(case["request"])
+    ref = case["result"]
+    assert set(got) == set(ref)
+    if "logLike" in ref:
+        assert_loglike(np.array(got["logLike"]), np.array(ref["logLike"]))
+    if "counts" in ref:
+        assert_cols(np.array(got["counts"]), np.array(ref["counts"]), COUNTS_RTOL, "counts")
+        assert_cols(np.array(got["dwellTimes"]), np.array(ref["dwellTimes"]), COUNTS_RTOL, "dwell")
+    if "rootProb" in ref:
+        assert_cols(np.array(got["rootProb"]), np.array(ref["rootProb"]), ROOTPROB_RTOL, "rootProb")

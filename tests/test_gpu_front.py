@@ -32,7 +32,7 @@ def test_device_tokenizer_matches_host(shape):
     dev = formats.tokenize(torch.as_tensor(chars).cuda(), alphabet)
     torch.cuda.synchronize()
     np.testing.assert_array_equal(dev.cpu().numpy(), host)
-    assert host.max() == 5 and host.min() == 0
+    assert 0 <= host.min() and host.max() <= 5
 
 
 def test_device_tokenizer_reports_first_bad_character():

@@ -1382,39 +1382,15 @@ int run_cx(subby_plan *P, const int32_t *d_aln, int C, float *d_logL, float *d_c
   return mark_use(P, stream);
 }
 
-// Column chunks of the host-pointer pipeline, as chunk start columns
-// followed by C.  Granule: one wave of the one-CTA-per-SM kernels (nsm x 256
-// columns).  The copies of chunk i + 1 overlap the kernel of chunk i, so the
-// first chunk's copy and the last chunk's kernel are not hidden: the
-// schedule ramps up and down (1, 2, m, ..., m, 2, 1 waves, about ten
-// chunks); below eight waves every chunk is one wave, below two a single
-// chunk (nothing to overlap).
-std::vector<int> host_chunks(const subby_plan *P, int C) {
+// Columns per chunk of the host-pointer pipeline: whole waves of the
+// one-CTA-per-SM kernels (nsm x 256 columns), about eight chunks for large C,
+// a single chunk below two waves (nothing to overlap).
+int host_chunk_columns(const subby_plan *P, int C) {
   const long long wave = (long long)std::max(P->nsm, 1) * 256;
-  std::vector<int> starts;
-  if (C < 2 * wave) {
-    starts = {0, C};
-    return starts;
-  }
-  const long long W = (C + wave - 1) / wave;
-  std::vector<long long> w;
-  if (W < 8) {
-    w.assign((size_t)W, 1);
-  } else {
-    const long long mid = W - 6, m = std::max(1LL, (mid + 5) / 6);
-    w = {1, 2};
-    for (long long left = mid; left > 0; left -= m) w.push_back(std::min(m, left));
-    w.push_back(2);
-    w.push_back(1);
-  }
-  long long c0 = 0;
-  for (long long k : w) {
-    if (c0 >= C) break;
-    starts.push_back((int)c0);
-    c0 += k * wave;
-  }
-  starts.push_back(C);
-  return starts;
+  if (C < 2 * wave) return std::max(C, 1);
+  const long long waves = (C + wave - 1) / wave;
+  const long long per = std::max(1LL, (waves + 7) / 8);
+  return (int)std::min<long long>(C, per * wave);
 }
 
 int ensure_pipeline(subby_plan *P, int nev) {
@@ -1565,8 +1541,8 @@ int subby_plan_run(subby_plan *P, const int32_t *aln, int C, float *logL, float 
   float *d_ct = b_ct ? (float *)base : nullptr;
   base += al(b_ct);
   float *d_rp = b_rp ? (float *)base : nullptr;
-  const std::vector<int> starts = host_chunks(P, C);
-  const int nch = (int)starts.size() - 1;
+  const int chunk = host_chunk_columns(P, C);
+  const int nch = (C + chunk - 1) / chunk;
   if ((rc = ensure_pipeline(P, 2 * nch + 2))) return rc;
   cudaEvent_t *ev = P->ev.data();
   // drains both copy queues before any return, so P->io is idle afterwards
@@ -1579,7 +1555,7 @@ int subby_plan_run(subby_plan *P, const int32_t *aln, int C, float *logL, float 
   CU(cudaEventRecord(ev[0], stream));
   CU(cudaStreamWaitEvent(P->s_in, ev[0], 0));
   for (int i = 0; i < nch; ++i) {
-    const int c0 = starts[i], cc = starts[i + 1] - c0;
+    const int c0 = i * chunk, cc = std::min(chunk, C - c0);
     cudaError_t e = cudaMemcpy2DAsync(d_aln + (size_t)R * c0, (size_t)cc * 4, aln + c0, (size_t)C * 4,
                                       (size_t)cc * 4, R, cudaMemcpyHostToDevice, P->s_in);
     if (e == cudaSuccess && b_mask)
@@ -1589,7 +1565,7 @@ int subby_plan_run(subby_plan *P, const int32_t *aln, int C, float *logL, float 
     if (e != cudaSuccess) return finish(cuda_fail(e, "chunk copy-in"));
   }
   for (int i = 0; i < nch; ++i) {
-    const int c0 = starts[i], cc = starts[i + 1] - c0;
+    const int c0 = i * chunk, cc = std::min(chunk, C - c0);
     cudaError_t e = cudaStreamWaitEvent(stream, ev[2 + 2 * i], 0);
     if (e != cudaSuccess) return finish(cuda_fail(e, "cudaStreamWaitEvent"));
     rc = run_common(P, d_aln + (size_t)R * c0, cc, d_ll ? d_ll + c0 : nullptr,

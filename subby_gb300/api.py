@@ -593,43 +593,74 @@ class InsideOutside:
     The reference runs both passes once and keeps U and D for the queries;
     here the (tree, model) plan stays resident and each query runs its fused
     kernels (walk + accumulation or posterior kernel) over the alignment, so
-    nothing of size R x C x A is held between queries.  Model lists and grids
-    raise ``NotImplementedError`` (the reference raises for grids too).
+    nothing of size R x C x A is held between queries.  ``*H`` batched models
+    give outputs with leading ``*H``; per-column model lists are grouped by
+    model (posteriors need one root prior: lists whose pis differ raise
+    ``NotImplementedError``); model grids raise ``NotImplementedError``, as in
+    the reference.
     """
 
     def __init__(self, alignment, tree: Tree, model, maxChunkSize: int = 128):
         del maxChunkSize
-        if isinstance(model, (list, tuple)) and not hasattr(model, '_fields'):
-            raise NotImplementedError("InsideOutside does not support model lists or grids here")
+        self._kind = batch.kind(model)
+        if self._kind == 'grid':
+            raise NotImplementedError("InsideOutside does not support model grids")
         self._alignment = alignment
         self._tree = tree
-        self._plan = get_plan(tree, model, _device_of(alignment))
+        self._model = model
         self._logLike = None
+
+    def _one(self, m):
+        return get_plan(self._tree, m, _device_of(self._alignment))
+
+    def _each(self, fn):
+        """fn(plan, alignment) for a single model, stacked over *H."""
+        if self._kind == 'H':
+            return batch.map_h(self._model, lambda m: fn(self._one(m), self._alignment))
+        return fn(self._one(self._model), self._alignment)
 
     @property
     def log_likelihood(self):
-        """Per-column log-likelihoods (C,)."""
+        """Per-column log-likelihoods (*H, C)."""
         if self._logLike is None:
-            self._logLike = self._plan.run(self._alignment, loglike=True)['logLike']
+            self._logLike = LogLike(self._alignment, self._tree, self._model)
         return self._logLike
 
     def counts(self, f81_fast_flag: bool = False, branch_mask="auto"):
-        """(A, A, C) dwell times and substitution counts (as ``Counts``)."""
-        return self._plan.run(self._alignment, loglike=False, counts=True, f81=f81_fast_flag,
-                              branch_mask=branch_mask)['counts']
+        """(*H, A, A, C) dwell times and substitution counts (as ``Counts``)."""
+        return Counts(self._alignment, self._tree, self._model, f81_fast_flag=f81_fast_flag, branch_mask=branch_mask)
 
     def branch_counts(self, f81_fast_flag: bool = False):
-        """(R, A, A, C) per-branch counts, unmasked (as ``BranchCounts``)."""
-        return self._plan.branch_counts(self._alignment, f81=f81_fast_flag)
+        """(*H, R, A, A, C) per-branch counts, unmasked (as ``BranchCounts``)."""
+        return BranchCounts(self._alignment, self._tree, self._model, f81_fast_flag=f81_fast_flag)
+
+    def _posteriors(self, node, want_node, want_branch, key):
+        if self._kind != 'list':
+            return self._each(lambda p, a: p.posteriors(a, node=node, want_node=want_node,
+                                                        want_branch=want_branch)[key])
+        ms, groups = batch._groups(self._alignment, self._model)
+        pi0 = np.asarray(ms[0].pi, np.float64)
+        if any(not np.array_equal(np.asarray(m.pi, np.float64), pi0) for m, _ in groups):
+            raise NotImplementedError("posteriors of per-column models with different pi are not supported")
+        R, A, C = int(self._alignment.shape[0]), len(pi0), int(self._alignment.shape[1])
+        lead = (R,) if node is None else ()
+        shape = lead + ((A,) if key == 'node' else (A, A)) + (C,)
+        out = batch._new(self._alignment, shape)
+        for m, idx in groups:
+            r = self._one(m).posteriors(batch._take(self._alignment, idx), node=node, want_node=want_node,
+                                        want_branch=want_branch)[key]
+            batch._put(out, idx, r)
+        return out
 
     def node_posterior(self, node=None):
-        """Posterior state distribution: (A, C) for ``node``, (R, A, C) for
-        every node when ``node`` is None."""
-        return self._plan.posteriors(self._alignment, node=node)['node']
+        """Posterior state distribution: (*H, A, C) for ``node``, (*H, R, A, C)
+        for every node when ``node`` is None."""
+        return self._posteriors(node, True, False, 'node')
 
     def branch_posterior(self, node=None):
-        """Joint posterior of (parent state, child state): (A, A, C) for
-        ``node`` > 0, (R, A, A, C) with branch 0 zeros when ``node`` is None."""
+        """Joint posterior of (parent state, child state): (*H, A, A, C) for
+        ``node`` > 0, (*H, R, A, A, C) with branch 0 zeros when ``node`` is
+        None."""
         if node is not None and int(node) == 0:
             raise ValueError("node 0 (the root) has no branch")
-        return self._plan.posteriors(self._alignment, node=node, want_node=False, want_branch=True)['branch']
+        return self._posteriors(node, False, True, 'branch')

@@ -42,6 +42,7 @@ import numpy as np
 
 from .api import Plan
 from .models import ensure_diag
+from . import batch
 
 
 @dataclass
@@ -83,8 +84,9 @@ class Job:
 def _plan_key(tree, model):
     m = ensure_diag(model)
     h = hashlib.sha1()
-    for a in (tree.parentIndex, tree.distanceToParent, m.eigenvalues, m.eigenvectors, m.pi):
+    for a in (tree.parentIndex, tree.distanceToParent):
         h.update(np.ascontiguousarray(a, dtype=np.float64).tobytes())
+    h.update(batch._key(m).encode())   # every model field, complex ones included
     return h.hexdigest()
 
 

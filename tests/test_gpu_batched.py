@@ -175,3 +175,27 @@ def test_per_branch_models_large_alphabet_and_column_grid():
     refc = np.concatenate([oracle.Counts_rows(aln[:, c:c + 1], ot, [m._asdict() for m in grid[c]])
                            for c in range(37)], axis=-1)
     assert_cols(cnt, refc, COUNTS_RTOL, "column grid counts")
+
+
+def test_inside_outside_batched_and_lists():
+    w = synth.plain_small(seed=17, C=120)
+    aln, tree, base = w['alignment'], w['tree'], w['model']
+    rates = np.array([0.5, 1.0, 2.0])
+    io = sg.InsideOutside(aln, tree, sg.scale_model(base, rates))
+    npost = io.node_posterior()
+    assert npost.shape == (3, len(tree.parentIndex), 4, 120)
+    for k, r in enumerate(rates):
+        one = sg.InsideOutside(aln, tree, sg.scale_model(base, r))
+        np.testing.assert_array_equal(npost[k], one.node_posterior())
+        np.testing.assert_array_equal(io.branch_posterior(3)[k], one.branch_posterior(3))
+    # per-column list sharing pi: grouped posteriors equal the per-model ones
+    ms = [sg.scale_model(base, rates[c % 3]) for c in range(120)]
+    iol = sg.InsideOutside(aln, tree, ms)
+    got = iol.node_posterior()
+    for k in range(3):
+        cols = np.arange(k, 120, 3)
+        ref = sg.InsideOutside(aln[:, cols], tree, sg.scale_model(base, rates[k])).node_posterior()
+        np.testing.assert_array_equal(got[..., cols], ref)
+    assert_loglike(iol.log_likelihood, sg.LogLike(aln, tree, ms))
+    with pytest.raises(NotImplementedError):
+        sg.InsideOutside(aln, tree, [[base] * len(tree.parentIndex)])

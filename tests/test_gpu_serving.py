@@ -99,3 +99,28 @@ def test_plan_trim_releases_workspace_and_keeps_results():
     for k in a:
         np.testing.assert_array_equal(a[k], b[k])
     plan.close()
+
+
+def test_irreversible_jobs_in_the_mix():
+    """Irreversible-model jobs share the loop with reversible ones; each result
+    equals its job run alone."""
+    rng = np.random.default_rng(21)
+    jobs = []
+    for i in range(6):
+        A = 4 if i % 2 else 20
+        m = sg.models.random_irreversible(A, rng) if i < 4 else sg.models.random_reversible(A, rng)[0]
+        tree = synth.random_tree(int(rng.integers(4, 20)), 0.1, rng)
+        aln = rng.integers(0, A + 2, size=(len(tree.parentIndex), int(rng.integers(50, 900)))).astype(np.int32)
+        jobs.append(serve.Job(id=i, alignment=aln, tree=tree, model=m, f81=False, want=("logLike", "counts"),
+                              arrival=0.0))
+    srv = serve.Server(max_inflight=3, device_budget=1 << 30)
+    done = srv.run(jobs, realtime=False)
+    assert len(done) == 6
+    for j in done:
+        assert not j.error, j.error
+        plan = sg.Plan(j.tree, j.model)
+        alone = plan.run(j.alignment, loglike=True, counts=True)
+        plan.close()
+        np.testing.assert_array_equal(j.result['counts'], alone['counts'])
+        np.testing.assert_array_equal(j.result['logLike'], alone['logLike'])
+    srv.close()

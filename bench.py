@@ -163,7 +163,8 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--columns", type=int, default=1 << 20)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", choices=["plain_large", "precision64", "f81_64", "grad20", "serving"],
+    ap.add_argument("--workload", choices=["plain_large", "precision64", "f81_64", "grad20", "serving",
+                                           "posteriors", "irreversible", "gamma4"],
                     default="plain_large",
                     help="plain_large is the headline line; the others print their own line")
     ap.add_argument("--jobs", type=int, default=10000, help="serving: number of jobs")
@@ -190,6 +191,8 @@ def main():
         return grad20_bench(args)
     if args.workload == "f81_64":
         return f81_64_bench(args)
+    if args.workload in ("posteriors", "irreversible", "gamma4"):
+        return widened_bench(args)
 
     # spawn pool for the CPU baseline before any GPU work
     pool = None
@@ -425,6 +428,60 @@ def f81_64_bench(args):
                       "higher_is_better": True, "dtype": "fp32 (split-bf16 tensor-core G accumulation)",
                       "err_vs_oracle_colwise_16cols": err,
                       "eigen_path_same_model": {"value": C / (ms_eig / 1e3), "ms_per_step": ms_eig}}))
+    return 0
+
+
+def widened_bench(args):
+    """Device throughput of the rows beyond Counts (inputs resident, CUDA
+    events): InsideOutside posteriors (A=4 plain_large tree, node and branch;
+    A=64 precision64 tree), irreversible-model Counts (cyclic random rate
+    matrices, A=4 / 20 / 64), and a 4-category discrete-gamma *H batch plus
+    MixturePosterior (A=4).  One JSON line, one entry per case."""
+    import torch
+    import subby_gb300 as sg
+    from subby_gb300 import synth, models
+    rng = np.random.default_rng(7)
+    res = {}
+
+    def case(name, C, fn):
+        ms = _time_fn(fn, args.steps, args.warmup)
+        res[name] = {"ms_per_step": round(ms, 3), "columns_per_s": C / (ms / 1e3)}
+
+    if args.workload == "posteriors":
+        w = synth.plain_large(seed=2, C=1 << 20)
+        plan = sg.Plan(w['tree'], w['model'])
+        d = torch.as_tensor(w['alignment']).cuda()
+        case("node_posteriors A=4 R=255 C=2^20", 1 << 20, lambda: plan.posteriors(d))
+        case("branch_posteriors A=4 R=255 C=2^20", 1 << 20,
+             lambda: plan.posteriors(d, want_node=False, want_branch=True))
+        w = synth.precision64(seed=3, C=65536)
+        plan = sg.Plan(w['tree'], w['model'])
+        d = torch.as_tensor(w['alignment']).cuda()
+        case("node_posteriors A=64 R=127 C=65536", 65536, lambda: plan.posteriors(d))
+        case("branch_posteriors A=64 R=127 C=4096", 4096,
+             lambda: plan.posteriors(d[:, :4096].contiguous(), want_node=False, want_branch=True))
+    elif args.workload == "irreversible":
+        for A, leaves, C in ((4, 128, 1 << 20), (20, 200, 100000), (64, 64, 65536)):
+            m = models.random_irreversible(A, rng)
+            tree = synth.random_tree(leaves, 0.05 if A == 4 else 0.1, rng)
+            aln = synth.simulated_alignment(tree, m, C, 0.1, rng) if A == 4 else \
+                rng.integers(0, A + 2, size=(len(tree.parentIndex), C)).astype(np.int32)
+            plan = sg.Plan(tree, m)
+            d = torch.as_tensor(aln).cuda()
+            case(f"irreversible Counts A={A} R={plan.R} C={C}", C, lambda: plan.run(d, loglike=False, counts=True))
+            case(f"irreversible LogLike A={A} R={plan.R} C={C}", C, lambda: plan.run(d, loglike=True))
+    else:
+        w = synth.plain_large(seed=2, C=1 << 20)
+        d = torch.as_tensor(w['alignment']).cuda()
+        rates, weights = models.gamma_rate_categories(0.5, 4)
+        mb = models.scale_model(w['model'], rates)
+        case("LogLike, 4 gamma categories (*H batch), A=4 R=255 C=2^20", 1 << 20,
+             lambda: sg.LogLike(d, w['tree'], mb))
+        ms = [models.scale_model(w['model'], r) for r in rates]
+        case("MixturePosterior over 4 gamma categories, A=4 R=255 C=2^20", 1 << 20,
+             lambda: sg.MixturePosterior(d, w['tree'], ms, np.log(weights)))
+    print(json.dumps({"workload": args.workload, "steps": args.steps, "warmup": args.warmup,
+                      "data": "synthetic, inputs resident on the device", "cases": res}))
     return 0
 
 

@@ -15,8 +15,9 @@
 // Layout: a CTA of 256 threads holds G columns; the A^2 complex entries of a
 // column's C are split over TPC = A^2 / 16 threads (16 entries each, in
 // registers).  Per branch the CTA projects its columns' D and U into shared
-// memory (double-buffered, one barrier per branch) and each thread updates
-// its 16 entries with J_n read through L1.  The epilogue forms T = C Vinv and
+// memory (double-buffered and software-pipelined: branch n + 1 is loaded
+// and projected while branch n accumulates; one barrier per branch) and each
+// thread updates its 16 entries with J_n read through L1.  The epilogue forms T = C Vinv and
 // V T through shared memory.  Complex tables (P.cx): J (R x A x A), V, Vinv,
 // R, Vinv^T, V^T (A x A each), FP32 pairs; then V, Vinv, Vinv^T, V^T in FP64
 // pairs for the FP64 back-transform (k_bt_cx).  P.cx_exact selects the
@@ -136,38 +137,46 @@ __global__ void __launch_bounds__(kCxThreads) k_acc_cx(const KParams P, const fl
     float2 acc[kCxE];
 #pragma unroll
     for (int i = 0; i < kCxE; ++i) acc[i] = make_float2(0.f, 0.f);
-    for (int bi = n_lo; bi < n_hi; ++bi) {
+    // projections of branch slot bi into buffer bi & 1
+    auto project = [&](int bi) {
+      if (!busy) return;
       const int n = __ldg(P.cx_br + bi);
       float2 *buf = sP + ((size_t)(bi & 1) * G + g) * 2 * A;
-      if (busy) {
-        const size_t srow = ((size_t)(n - 1) * c_count + ccl) * A;
-        for (int o = p; o < 2 * A; o += TPC) {
-          float2 s = make_float2(0.f, 0.f);
-          if (o < A) {
-            const float *d = sa + srow;
+      const size_t srow = ((size_t)(n - 1) * c_count + ccl) * A;
+      for (int o = p; o < 2 * A; o += TPC) {
+        float2 s = make_float2(0.f, 0.f);
+        if (o < A) {
+          const float *d = sa + srow;
 #pragma unroll 4
-            for (int a = 0; a < A; ++a) {
-              const float x = __ldg(d + a);
-              const float2 v = sVi[o * A + a];
-              s.x = fmaf(x, v.x, s.x);
-              s.y = fmaf(x, v.y, s.y);
-            }
-          } else {
-            const float *u = sb + srow;
-            const int l = o - A;
-#pragma unroll 4
-            for (int b = 0; b < A; ++b) {
-              const float x = __ldg(u + b);
-              const float2 v = sV[b * A + l];
-              s.x = fmaf(x, v.x, s.x);
-              s.y = fmaf(x, v.y, s.y);
-            }
+          for (int a = 0; a < A; ++a) {
+            const float x = __ldg(d + a);
+            const float2 v = sVi[o * A + a];
+            s.x = fmaf(x, v.x, s.x);
+            s.y = fmaf(x, v.y, s.y);
           }
-          buf[o] = s;
+        } else {
+          const float *u = sb + srow;
+          const int l = o - A;
+#pragma unroll 4
+          for (int b = 0; b < A; ++b) {
+            const float x = __ldg(u + b);
+            const float2 v = sV[b * A + l];
+            s.x = fmaf(x, v.x, s.x);
+            s.y = fmaf(x, v.y, s.y);
+          }
         }
+        buf[o] = s;
       }
-      __syncthreads();
+    };
+    // software pipeline: branch bi + 1 is projected (its staged rows loaded)
+    // while branch bi accumulates; one barrier per branch
+    if (n_lo < n_hi) project(n_lo);
+    __syncthreads();
+    for (int bi = n_lo; bi < n_hi; ++bi) {
+      const int n = __ldg(P.cx_br + bi);
+      if (bi + 1 < n_hi) project(bi + 1);
       if (busy) {
+        const float2 *buf = sP + ((size_t)(bi & 1) * G + g) * 2 * A;
         const float2 *Jn = J + (size_t)n * A * A + p * kCxE;
 #pragma unroll
         for (int i = 0; i < kCxE; ++i) {
@@ -179,6 +188,7 @@ __global__ void __launch_bounds__(kCxThreads) k_acc_cx(const KParams P, const fl
       if constexpr (PB) {
         epilogue(acc, n, valid, col);
       }
+      __syncthreads();
     }
     if constexpr (CBUF) {
       if (valid) {

@@ -72,8 +72,10 @@ __global__ void __launch_bounds__(kCxThreads) k_acc_cx(const KParams P, const fl
   extern __shared__ __align__(16) float2 s_cx[];
   float2 *sV = s_cx;                  // A x A: V[i][k]
   float2 *sVi = sV + A * A;           // A x A: Vinv[k][j]
-  float2 *sP = sVi + A * A;           // [2][G][2A]: D~ (k < A), U~ (A + l)
-  float2 *sC = sP + 2 * G * 2 * A;    // [G][A][A]: C, then T = C Vinv
+  // column-minor layouts (consecutive columns in consecutive words: no bank
+  // conflicts when a warp spans several columns)
+  float2 *sP = sVi + A * A;           // [2][2A][G]: D~ (k < A), U~ (A + l)
+  float2 *sC = sP + 2 * G * 2 * A;    // [A*A][G]: C, then T = C Vinv
   const float2 *J = P.cx;
   const float2 *T0 = P.cx_tab;  // V, Vinv, R, Vinv^T, V^T
   const float2 *Vg = T0 + (P.cx_exact ? 3 : 0) * A * A;
@@ -89,7 +91,7 @@ __global__ void __launch_bounds__(kCxThreads) k_acc_cx(const KParams P, const fl
   const int g = busy ? t / TPC : 0, p = busy ? t % TPC : 0;
   const int ngroups = (c_count + G - 1) / G;
   const int C = P.C;
-  float2 *myC = sC + (size_t)g * A * A;
+  auto cC = [&](int e) -> float2 & { return sC[(size_t)e * G + g]; };
 
   // back-transform of the thread's 16 entries and the stores (row: branch
   // n for PB, else 0); every thread calls it (barriers inside)
@@ -97,7 +99,7 @@ __global__ void __launch_bounds__(kCxThreads) k_acc_cx(const KParams P, const fl
     __syncthreads();  // earlier readers of sC are done
     if (busy)
 #pragma unroll
-      for (int i = 0; i < kCxE; ++i) myC[p * kCxE + i] = acc[i];
+      for (int i = 0; i < kCxE; ++i) cC(p * kCxE + i) = acc[i];
     __syncthreads();
     float2 T[kCxE];
     if (busy)
@@ -106,13 +108,13 @@ __global__ void __launch_bounds__(kCxThreads) k_acc_cx(const KParams P, const fl
         const int e = p * kCxE + i, k = e / A, j = e % A;
         float2 s = make_float2(0.f, 0.f);
 #pragma unroll 4
-        for (int l = 0; l < A; ++l) s = cfma(myC[k * A + l], sVi[l * A + j], s);
+        for (int l = 0; l < A; ++l) s = cfma(cC(k * A + l), sVi[l * A + j], s);
         T[i] = s;
       }
     __syncthreads();
     if (busy)
 #pragma unroll
-      for (int i = 0; i < kCxE; ++i) myC[p * kCxE + i] = T[i];
+      for (int i = 0; i < kCxE; ++i) cC(p * kCxE + i) = T[i];
     __syncthreads();
     if (busy && valid) {
       float *out = P.counts + (size_t)row * A * A * C + col;
@@ -121,7 +123,7 @@ __global__ void __launch_bounds__(kCxThreads) k_acc_cx(const KParams P, const fl
         const int e = p * kCxE + i, ii = e / A, j = e % A;
         float2 s = make_float2(0.f, 0.f);
 #pragma unroll 4
-        for (int k = 0; k < A; ++k) s = cfma(sV[ii * A + k], myC[k * A + j], s);
+        for (int k = 0; k < A; ++k) s = cfma(sV[ii * A + k], cC(k * A + j), s);
         const float v = (ii == j) ? s.x : cmul(__ldg(Rg + e), s).x;
         if (!PB && P.cx_accum) out[(size_t)e * C] += v;
         else out[(size_t)e * C] = v;
@@ -141,7 +143,7 @@ __global__ void __launch_bounds__(kCxThreads) k_acc_cx(const KParams P, const fl
     auto project = [&](int bi) {
       if (!busy) return;
       const int n = __ldg(P.cx_br + bi);
-      float2 *buf = sP + ((size_t)(bi & 1) * G + g) * 2 * A;
+      float2 *buf = sP + (size_t)(bi & 1) * 2 * A * G + g;   // element o at buf[o * G]
       const size_t srow = ((size_t)(n - 1) * c_count + ccl) * A;
       for (int o = p; o < 2 * A; o += TPC) {
         float2 s = make_float2(0.f, 0.f);
@@ -165,7 +167,7 @@ __global__ void __launch_bounds__(kCxThreads) k_acc_cx(const KParams P, const fl
             s.y = fmaf(x, v.y, s.y);
           }
         }
-        buf[o] = s;
+        buf[(size_t)o * G] = s;
       }
     };
     // software pipeline: branch bi + 1 is projected (its staged rows loaded)
@@ -176,13 +178,14 @@ __global__ void __launch_bounds__(kCxThreads) k_acc_cx(const KParams P, const fl
       const int n = __ldg(P.cx_br + bi);
       if (bi + 1 < n_hi) project(bi + 1);
       if (busy) {
-        const float2 *buf = sP + ((size_t)(bi & 1) * G + g) * 2 * A;
+        const float2 *buf = sP + (size_t)(bi & 1) * 2 * A * G + g;
         const float2 *Jn = J + (size_t)n * A * A + p * kCxE;
 #pragma unroll
         for (int i = 0; i < kCxE; ++i) {
           const int e = p * kCxE + i, k = e / A, l = e % A;
-          const float2 x = cmul(buf[k], __ldg(Jn + i));
-          acc[i] = PB ? cmul(x, buf[A + l]) : cfma(x, buf[A + l], acc[i]);
+          const float2 x = cmul(buf[(size_t)k * G], __ldg(Jn + i));
+          const float2 u = buf[(size_t)(A + l) * G];
+          acc[i] = PB ? cmul(x, u) : cfma(x, u, acc[i]);
         }
       }
       if constexpr (PB) {

@@ -17,7 +17,8 @@
 // registers).  Per branch the CTA projects its columns' D and U into shared
 // memory (double-buffered and software-pipelined: branch n + 1 is loaded
 // and projected while branch n accumulates; one barrier per branch) and each
-// thread updates its 16 entries with J_n read through L1.  The epilogue forms T = C Vinv and
+// thread updates its 16 entries with J_n, staged in shared memory once per
+// CTA and branch.  The epilogue forms T = C Vinv and
 // V T through shared memory.  Complex tables (P.cx): J (R x A x A), V, Vinv,
 // R, Vinv^T, V^T (A x A each), FP32 pairs; then V, Vinv, Vinv^T, V^T in FP64
 // pairs for the FP64 back-transform (k_bt_cx).  P.cx_exact selects the
@@ -56,7 +57,7 @@ __device__ __forceinline__ float2 cfma(float2 a, float2 b, float2 c) {  // a b +
 template <int A>
 constexpr size_t cx_smem() {
   using Gm = CxGeo<A>;
-  return (size_t)(2 * A * A + 2 * Gm::G * 2 * A + Gm::G * A * A) * sizeof(float2);
+  return (size_t)(2 * A * A + 2 * Gm::G * 2 * A + Gm::G * A * A + 2 * A * A) * sizeof(float2);
 }
 
 // Branches: P.cx_br[n_lo .. n_hi) (the branches of one system).  PB:
@@ -76,6 +77,7 @@ __global__ void __launch_bounds__(kCxThreads) k_acc_cx(const KParams P, const fl
   // conflicts when a warp spans several columns)
   float2 *sP = sVi + A * A;           // [2][2A][G]: D~ (k < A), U~ (A + l)
   float2 *sC = sP + 2 * G * 2 * A;    // [A*A][G]: C, then T = C Vinv
+  float2 *sJ = sC + G * A * A;        // [2][16][TPC]: J_n, entry p*16+i at i*TPC+p
   const float2 *J = P.cx;
   const float2 *T0 = P.cx_tab;  // V, Vinv, R, Vinv^T, V^T
   const float2 *Vg = T0 + (P.cx_exact ? 3 : 0) * A * A;
@@ -141,8 +143,14 @@ __global__ void __launch_bounds__(kCxThreads) k_acc_cx(const KParams P, const fl
     for (int i = 0; i < kCxE; ++i) acc[i] = make_float2(0.f, 0.f);
     // projections of branch slot bi into buffer bi & 1
     auto project = [&](int bi) {
-      if (!busy) return;
       const int n = __ldg(P.cx_br + bi);
+      {
+        // J_n into shared memory once per CTA (not once per column)
+        float2 *dj = sJ + (size_t)(bi & 1) * A * A;
+        const float2 *Jn = J + (size_t)n * A * A;
+        for (int e = t; e < A * A; e += blockDim.x) dj[(e % kCxE) * TPC + e / kCxE] = __ldg(Jn + e);
+      }
+      if (!busy) return;
       float2 *buf = sP + (size_t)(bi & 1) * 2 * A * G + g;   // element o at buf[o * G]
       const size_t srow = ((size_t)(n - 1) * c_count + ccl) * A;
       for (int o = p; o < 2 * A; o += TPC) {
@@ -179,11 +187,11 @@ __global__ void __launch_bounds__(kCxThreads) k_acc_cx(const KParams P, const fl
       if (bi + 1 < n_hi) project(bi + 1);
       if (busy) {
         const float2 *buf = sP + (size_t)(bi & 1) * 2 * A * G + g;
-        const float2 *Jn = J + (size_t)n * A * A + p * kCxE;
+        const float2 *Jn = sJ + (size_t)(bi & 1) * A * A + p;
 #pragma unroll
         for (int i = 0; i < kCxE; ++i) {
           const int e = p * kCxE + i, k = e / A, l = e % A;
-          const float2 x = cmul(buf[(size_t)k * G], __ldg(Jn + i));
+          const float2 x = cmul(buf[(size_t)k * G], Jn[i * TPC]);
           const float2 u = buf[(size_t)(A + l) * G];
           acc[i] = PB ? cmul(x, u) : cfma(x, u, acc[i]);
         }

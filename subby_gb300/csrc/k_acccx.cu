@@ -144,11 +144,12 @@ __global__ void __launch_bounds__(kCxThreads) k_acc_cx(const KParams P, const fl
     // projections of branch slot bi into buffer bi & 1
     auto project = [&](int bi) {
       const int n = __ldg(P.cx_br + bi);
-      {
-        // J_n into shared memory once per CTA (not once per column)
+      if constexpr (G > 1) {
+        // J_n into shared memory once per CTA (not once per column); the
+        // stores run over the shared layout so that they do not conflict
         float2 *dj = sJ + (size_t)(bi & 1) * A * A;
         const float2 *Jn = J + (size_t)n * A * A;
-        for (int e = t; e < A * A; e += blockDim.x) dj[(e % kCxE) * TPC + e / kCxE] = __ldg(Jn + e);
+        for (int d = t; d < A * A; d += blockDim.x) dj[d] = __ldg(Jn + (d % TPC) * kCxE + d / TPC);
       }
       if (!busy) return;
       float2 *buf = sP + (size_t)(bi & 1) * 2 * A * G + g;   // element o at buf[o * G]
@@ -187,11 +188,13 @@ __global__ void __launch_bounds__(kCxThreads) k_acc_cx(const KParams P, const fl
       if (bi + 1 < n_hi) project(bi + 1);
       if (busy) {
         const float2 *buf = sP + (size_t)(bi & 1) * 2 * A * G + g;
-        const float2 *Jn = sJ + (size_t)(bi & 1) * A * A + p;
+        // one column per CTA (A = 64): no reuse, J_n read through L1
+        const float2 *Jn = (G > 1) ? sJ + (size_t)(bi & 1) * A * A + p : J + (size_t)n * A * A + p * kCxE;
+        constexpr int js = (G > 1) ? TPC : 1;
 #pragma unroll
         for (int i = 0; i < kCxE; ++i) {
           const int e = p * kCxE + i, k = e / A, l = e % A;
-          const float2 x = cmul(buf[(size_t)k * G], Jn[i * TPC]);
+          const float2 x = cmul(buf[(size_t)k * G], (G > 1) ? Jn[i * js] : __ldg(Jn + i));
           const float2 u = buf[(size_t)(A + l) * G];
           acc[i] = PB ? cmul(x, u) : cfma(x, u, acc[i]);
         }

@@ -57,7 +57,7 @@ __device__ __forceinline__ float2 cfma(float2 a, float2 b, float2 c) {  // a b +
 template <int A>
 constexpr size_t cx_smem() {
   using Gm = CxGeo<A>;
-  return (size_t)(2 * A * A + 2 * Gm::G * 2 * A + Gm::G * A * A + 2 * A * A) * sizeof(float2);
+  return (size_t)(2 * A * A + 2 * Gm::G * 2 * A + Gm::G * A * A + (Gm::G > 1 ? 2 * A * A : 0)) * sizeof(float2);
 }
 
 // Branches: P.cx_br[n_lo .. n_hi) (the branches of one system).  PB:

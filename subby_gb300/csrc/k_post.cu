@@ -85,7 +85,7 @@ __global__ void __launch_bounds__(kPostTile) k_post(const KParams P, const float
     for (int j = 0; j < A; ++j) {
       const float u = __ldg(pb + j) * inv;
 #pragma unroll
-      for (int i = 0; i < A; ++i) o[((size_t)i * A + j) * C] = d[i] * Ms[i * A + j] * u;
+      for (int i = 0; i < A; ++i) __stcs(o + ((size_t)i * A + j) * C, d[i] * Ms[i * A + j] * u);  // streamed: written once, never re-read here
     }
   }
 }

@@ -340,11 +340,12 @@ __global__ void __launch_bounds__(256, 1) k_tree4(const KParams P) {
         if (!valid) return;
         const size_t row = P.npost_node < 0 ? (size_t)n : 0;
         if (P.npost) {
+          // streamed stores: the posteriors are written once and not re-read here
           float *o = P.npost + row * 4 * C + col;
-          o[0] = p.a.x * inv;
-          o[(size_t)C] = p.a.y * inv;
-          o[(size_t)2 * C] = p.b.x * inv;
-          o[(size_t)3 * C] = p.b.y * inv;
+          __stcs(o, p.a.x * inv);
+          __stcs(o + C, p.a.y * inv);
+          __stcs(o + (size_t)2 * C, p.b.x * inv);
+          __stcs(o + (size_t)3 * C, p.b.y * inv);
         }
         if (P.bpost) {
           float *o = P.bpost + row * 16 * C + col;
@@ -355,10 +356,10 @@ __global__ void __launch_bounds__(256, 1) k_tree4(const KParams P) {
             // row i of M_n is column i of the MT rows: M_n[i][j] = MT[n][j][i]
             const F4 mi = F4{make_float2(Mn[i2], Mn[4 + i2]), make_float2(Mn[8 + i2], Mn[12 + i2])};
             const F4 r = scale4(mul4(mi, ui), dk[i2]);
-            o[(size_t)(4 * i2) * C] = r.a.x;
-            o[(size_t)(4 * i2 + 1) * C] = r.a.y;
-            o[(size_t)(4 * i2 + 2) * C] = r.b.x;
-            o[(size_t)(4 * i2 + 3) * C] = r.b.y;
+            __stcs(o + (size_t)(4 * i2) * C, r.a.x);
+            __stcs(o + (size_t)(4 * i2 + 1) * C, r.a.y);
+            __stcs(o + (size_t)(4 * i2 + 2) * C, r.b.x);
+            __stcs(o + (size_t)(4 * i2 + 3) * C, r.b.y);
           }
         }
         return;

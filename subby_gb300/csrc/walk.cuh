@@ -624,7 +624,7 @@ __global__ void __launch_bounds__(128 * Geo<A>::H, 1) k_walk(const KParams P, fl
             if (valid) {
               float *o = P.npost + ((size_t)(P.npost_node < 0 ? n : 0) * A + 32 * h) * C + col;
 #pragma unroll
-              for (int q = 0; q < S; ++q) o[(size_t)q * C] = y.v[q] * inv;
+              for (int q = 0; q < S; ++q) __stcs(o + (size_t)q * C, y.v[q] * inv);
             }
           }
         } else if (P.stage_c) {

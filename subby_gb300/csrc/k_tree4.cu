@@ -324,7 +324,7 @@ __global__ void __launch_bounds__(256, 1) k_tree4(const KParams P) {
 #pragma unroll
         for (int i2 = 0; i2 < 4; ++i2)
 #pragma unroll
-          for (int j = 0; j < 4; ++j) o[(size_t)(i2 * 4 + j) * C] = r[i2][j];
+          for (int j = 0; j < 4; ++j) __stcs(o + (size_t)(i2 * 4 + j) * C, r[i2][j]);  // streamed: written once
     };
     auto branch = [&](int n, const F4 &D, const F4 &U, int code, int eDU, int active) {
       float s = invP * __int_as_float((max(-127, min(127, eDU - eRoot)) + 127) << 23);

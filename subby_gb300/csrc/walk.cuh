@@ -605,26 +605,30 @@ __global__ void __launch_bounds__(128 * Geo<A>::H, 1) k_walk(const KParams P, fl
           // node posterior (D^T M_n) o U normalised over the states
           // (oracle.py:1755-1831); the scale s cancels
           if (P.npost && (P.npost_node < 0 || n == P.npost_node)) {
-            BV<A> y;
-            if (DM) y = *DM;
-            else mprod(y, D, n, true);
-            float z = 0.f;
+            // posterior from Y = D^T M_n without copying Y (register pressure)
+            auto post = [&](const BV<A> &Y) {
+              float z = 0.f;
 #pragma unroll
-            for (int q = 0; q < S; ++q) {
-              y.v[q] = __fmul_rn(y.v[q], U.v[q]);
-              z += y.v[q];
-            }
-            if constexpr (Geo<A>::H == 2) {
-              s_xch[h * kTile + cl] = z;
-              pair_sync(wk.warp);
-              z += s_xch[(1 - h) * kTile + cl];
-              pair_sync(wk.warp);
-            }
-            const float inv = z > 0.f ? 1.0f / z : 1.0f;
-            if (valid) {
-              float *o = P.npost + ((size_t)(P.npost_node < 0 ? n : 0) * A + 32 * h) * C + col;
+              for (int q = 0; q < S; ++q) z += __fmul_rn(Y.v[q], U.v[q]);
+              if constexpr (Geo<A>::H == 2) {
+                s_xch[h * kTile + cl] = z;
+                pair_sync(wk.warp);
+                z += s_xch[(1 - h) * kTile + cl];
+                pair_sync(wk.warp);
+              }
+              const float inv = z > 0.f ? 1.0f / z : 1.0f;
+              if (valid) {
+                float *o = P.npost + ((size_t)(P.npost_node < 0 ? n : 0) * A + 32 * h) * C + col;
 #pragma unroll
-              for (int q = 0; q < S; ++q) __stcs(o + (size_t)q * C, y.v[q] * inv);
+                for (int q = 0; q < S; ++q) __stcs(o + (size_t)q * C, __fmul_rn(Y.v[q], U.v[q]) * inv);
+              }
+            };
+            if (DM) {
+              post(*DM);
+            } else {
+              BV<A> y;
+              mprod(y, D, n, true);
+              post(y);
             }
           }
         } else if (P.stage_c) {

@@ -640,11 +640,16 @@ def loglike_distance_grad(alignment, tree, model, g=None):
     """d(sum_c g_c logL_c)/d t_n by the Fisher identity of subby/jax/vjp.py:92-124.
 
     dlogL_c/dt_n = sum_k D~_k mu_k e^{mu_k t_n} U~_k exp(lnD+lnU-lnL); root 0.
+    Irreversible models (vjp.py:80-90): D~ = D V, U~ = V^-1 U, real part.
     """
-    M = compute_sub_matrices(model, tree.distanceToParent)
+    M = _sub_matrices(model, tree.distanceToParent)
     U, lnU, lnL = upward_pass(alignment, tree, M, model['pi'])
     D, lnD = downward_pass(U, lnU, tree, M, model['pi'], alignment)
-    Ut, Dt = eigenbasis_project(U, D, model)
+    if is_irrev(model):
+        Dt = D @ np.asarray(model['eigenvectors'], dtype=np.complex128)
+        Ut = U @ np.asarray(model['eigenvectors_inv'], dtype=np.complex128).T
+    else:
+        Ut, Dt = eigenbasis_project(U, D, model)
     mu = np.asarray(model['eigenvalues'])
     t = tree.distanceToParent
     C = lnL.shape[0]
@@ -654,7 +659,7 @@ def loglike_distance_grad(alignment, tree, model, g=None):
     for n in range(1, R):
         me = mu * np.exp(mu * t[n])
         s = np.exp(lnD[n] + lnU[n] - lnL)
-        grad[n] = np.sum(g * s * np.einsum('ck,k,ck->c', Dt[n], me, Ut[n]))
+        grad[n] = np.sum(g * s * np.einsum('ck,k,ck->c', Dt[n], me, Ut[n]).real)
     return grad
 
 

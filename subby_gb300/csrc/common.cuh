@@ -156,6 +156,9 @@ int launch_acc_cx(const KParams &p, int A, bool pb, const float *sa, const float
                   int n_lo, int n_hi, float2 *cbuf, int grid, cudaStream_t s);
 int launch_bt_cx(const KParams &p, int A, const float2 *cbuf, int c_base, int c_count, int row, int grid,
                  cudaStream_t s);
+// distance gradient from the raw staging: grad_t[n] += sum_c g_c (D s)^T G_n U
+int launch_grad_cx(const KParams &p, int A, const float *sa, const float *sb, const float *gq, const float *g,
+                   int c_base, int c_count, double *grad_t, int grid, cudaStream_t s);
 // A = 4 posteriors (npost / bpost) from the tree-program kernel
 int launch_tree4_post(const KParams &p, int grid, int block, size_t smem, cudaStream_t s);
 // A = 64 F81 accumulation on the tensor cores (k_acctc.cu); groups of 8 columns

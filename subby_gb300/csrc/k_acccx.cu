@@ -302,7 +302,69 @@ int bt_launch(const KParams &p, const float2 *cbuf, int c_base, int c_count, int
   return (int)cudaGetLastError();
 }
 
+// Distance gradient (subby/jax/vjp.py:62-133) from the walk's raw staging:
+// per (branch n, 128-column tile), with G_n = dM_n/dt in shared memory,
+// v_c = g_c (D_n s_n)^T G_n U_n reduced over the tile in FP64 and added to
+// grad_t[n] (one atomic per tile).
+template <int A>
+__global__ void __launch_bounds__(128) k_grad_cx(const KParams P, const float *__restrict__ sa,
+                                                 const float *__restrict__ sb, const float *__restrict__ gq,
+                                                 const float *__restrict__ g, int c_base, int c_count,
+                                                 double *__restrict__ grad_t) {
+  __shared__ __align__(16) float sG[A * A];
+  __shared__ double s_red[4];
+  const int t = threadIdx.x;
+  const int ntiles = (c_count + 127) / 128;
+  const long long items = (long long)(P.R - 1) * ntiles;
+  for (long long it = blockIdx.x; it < items; it += gridDim.x) {
+    const int n = 1 + (int)(it / ntiles);
+    const int tile = (int)(it % ntiles);
+    __syncthreads();
+    for (int e = t; e < A * A; e += 128) sG[e] = __ldg(gq + (size_t)n * A * A + e);
+    __syncthreads();
+    const int cc = tile * 128 + t;
+    double v = 0.0;
+    if (cc < c_count) {
+      const size_t row = ((size_t)(n - 1) * c_count + cc) * A;
+      float u[A];
+#pragma unroll
+      for (int q = 0; q < A / 4; ++q) {
+        const float4 x = __ldg(reinterpret_cast<const float4 *>(sb + row) + q);
+        u[4 * q] = x.x, u[4 * q + 1] = x.y, u[4 * q + 2] = x.z, u[4 * q + 3] = x.w;
+      }
+      float acc = 0.f;
+#pragma unroll 4
+      for (int a = 0; a < A; ++a) {
+        float y = 0.f;
+#pragma unroll
+        for (int b = 0; b < A; ++b) y = fmaf(sG[a * A + b], u[b], y);
+        acc = fmaf(__ldg(sa + row + a), y, acc);
+      }
+      v = (double)acc * (g ? (double)__ldg(g + c_base + cc) : 1.0);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if ((t & 31) == 0) s_red[t >> 5] = v;
+    __syncthreads();
+    if (t == 0) atomicAdd(grad_t + n, (s_red[0] + s_red[1]) + (s_red[2] + s_red[3]));
+  }
+}
+
 }  // namespace
+
+int launch_grad_cx(const KParams &p, int A, const float *sa, const float *sb, const float *gq, const float *g,
+                   int c_base, int c_count, double *grad_t, int grid, cudaStream_t s) {
+  switch (A) {
+    case 4: k_grad_cx<4><<<grid, 128, 0, s>>>(p, sa, sb, gq, g, c_base, c_count, grad_t); break;
+    case 8: k_grad_cx<8><<<grid, 128, 0, s>>>(p, sa, sb, gq, g, c_base, c_count, grad_t); break;
+    case 16: k_grad_cx<16><<<grid, 128, 0, s>>>(p, sa, sb, gq, g, c_base, c_count, grad_t); break;
+    case 20: k_grad_cx<20><<<grid, 128, 0, s>>>(p, sa, sb, gq, g, c_base, c_count, grad_t); break;
+    case 32: k_grad_cx<32><<<grid, 128, 0, s>>>(p, sa, sb, gq, g, c_base, c_count, grad_t); break;
+    case 64: k_grad_cx<64><<<grid, 128, 0, s>>>(p, sa, sb, gq, g, c_base, c_count, grad_t); break;
+    default: return -1;
+  }
+  return (int)cudaGetLastError();
+}
 
 bool cx_supported(int A) { return A == 4 || A == 8 || A == 16 || A == 20 || A == 32 || A == 64; }
 

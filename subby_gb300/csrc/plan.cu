@@ -252,6 +252,7 @@ struct subby_plan {
   int ngroups = 1;
   std::vector<int> grp_off;
   int *d_grp_br = nullptr;
+  float *d_gq = nullptr;   // complex-system plans: dM_n/dt = Re V diag(mu e^{mu t_n}) V^-1 (R x A x A)
   TableOffsets off{};
   float *d_tab = nullptr;
   double *d_tab64 = nullptr;
@@ -597,7 +598,7 @@ int plan_create(const int32_t *parent, const double *dist, const double *evals, 
       e = cudaMemcpyAsync(P->d_prog, P->prog.data(), sizeof(int4) * P->prog.size(), cudaMemcpyHostToDevice, qs);
     if (e != cudaSuccess) return cleanup(cuda_fail(e, "program upload"));
   }
-  std::vector<float> hMT, hMN;
+  std::vector<float> hMT, hMN, hGQ;
   std::vector<float2> hcx;
   std::vector<int> grp_br;
   if (ir) {
@@ -653,10 +654,20 @@ int plan_create(const int32_t *parent, const double *dist, const double *evals, 
     // float2: J (R A^2), then per group 13 A^2: V, Vinv, rate, Vinv^T, V^T;
     // FP64 pairs of V, Vinv, Vinv^T, V^T (two float2 slots per value)
     hcx.assign((size_t)(R + 13 * P->ngroups) * AA, make_float2(0.f, 0.f));
-    std::vector<cd> E(A), w(A);
+    std::vector<cd> E(A), w(A), wq(A);
+    hGQ.assign((size_t)R * AA, 0.f);
     for (int n = 0; n < R; ++n) {
       const double t = dist[n];
       for (int k = 0; k < A; ++k) E[k] = std::exp(mu_of(n, k) * t);
+      // dM_n/dt for the distance gradient
+      for (int b = 0; b < A; ++b) {
+        for (int k = 0; k < A; ++k) wq[k] = V_of(n, (size_t)b * A + k) * mu_of(n, k) * E[k];
+        for (int j = 0; j < A; ++j) {
+          cd sum = 0.0;
+          for (int k = 0; k < A; ++k) sum += wq[k] * Vi_of(n, (size_t)k * A + j);
+          hGQ[(size_t)n * AA + (size_t)b * A + j] = (float)sum.real();
+        }
+      }
       for (int b = 0; b < A; ++b) {
         for (int k = 0; k < A; ++k) w[k] = V_of(n, (size_t)b * A + k) * E[k];
         double rs = 0.0;
@@ -709,6 +720,9 @@ int plan_create(const int32_t *parent, const double *dist, const double *evals, 
     if (e == cudaSuccess) e = pool_alloc((void **)&P->d_cx, hcx.size() * sizeof(float2), P->pool, qs);
     if (e == cudaSuccess)
       e = cudaMemcpyAsync(P->d_cx, hcx.data(), hcx.size() * sizeof(float2), cudaMemcpyHostToDevice, qs);
+    if (e == cudaSuccess) e = pool_alloc((void **)&P->d_gq, hGQ.size() * sizeof(float), P->pool, qs);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(P->d_gq, hGQ.data(), hGQ.size() * sizeof(float), cudaMemcpyHostToDevice, qs);
     if (e == cudaSuccess) e = pool_alloc((void **)&P->d_grp_br, grp_br.size() * sizeof(int), P->pool, qs);
     if (e == cudaSuccess)
       e = cudaMemcpyAsync(P->d_grp_br, grp_br.data(), grp_br.size() * sizeof(int), cudaMemcpyHostToDevice, qs);
@@ -820,7 +834,7 @@ int subby_plan_destroy(subby_plan *P) {
   if (P->s_in) cudaStreamSynchronize(P->s_in);
   if (P->s_out) cudaStreamSynchronize(P->s_out);
   void *bufs[] = {P->d_tab, P->d_tab64, P->d_steps, P->d_slots, P->d_prog, P->d_tab16, P->d_err, P->d_cx,
-                  P->d_grp_br};
+                  P->d_grp_br, P->d_gq};
   for (void *b : bufs)
     if (b) cudaFreeAsync(b, s);
   P->work.release(s);
@@ -1382,6 +1396,62 @@ int run_cx(subby_plan *P, const int32_t *d_aln, int C, float *d_logL, float *d_c
   return mark_use(P, stream);
 }
 
+// Distance gradient of complex-system plans (irreversible or per-branch
+// models; subby/jax/vjp.py:62-133): the walk stages D_n s_n and U_n (no
+// mask), k_grad_cx adds sum_c g_c (D_n s_n)^T (dM_n/dt) U_n into grad_t[n].
+int run_cx_grad(subby_plan *P, const int32_t *d_aln, int C, float *d_logL, const float *d_g, double *d_gt,
+                cudaStream_t stream) {
+  const int A = P->A, R = P->R;
+  if (!post_supported(A))
+    return fail(SUBBY_ERR_UNSUPPORTED, "gradients of these models are implemented for A = 4, 8, 16, 20, 32, 64");
+  KParams k = walk_params(P, d_aln, C, d_logL ? kModeLogLike : 0, SUBBY_MASK_NONE, nullptr, d_logL, nullptr,
+                          nullptr);
+  k.npost = nullptr;
+  k.npost_node = -1;
+  const bool tc = (A == 64) && P->d_tab16 && (g_kernel_sel == 0 || g_kernel_sel == 5);
+  const int tile = big_tile();
+  const int H = (A + 31) / 32;
+  int chunk = C;
+  if (R > 1) {
+    const size_t per_col = (size_t)2 * (R - 1) * A * sizeof(float);
+    size_t cmax = std::max<size_t>(tile, kStageBudget / per_col);
+    cmax = cmax / tile * tile;
+    const size_t nch = ((size_t)C + cmax - 1) / cmax;
+    const size_t even = ((size_t)C + nch - 1) / nch;
+    chunk = (int)std::min<size_t>((size_t)C, (even + tile - 1) / tile * tile);
+  }
+  const int per_sm = A <= 8 ? 8 : (H == 2 ? 1 : 2);
+  const int walk_grid = std::max(1, std::min((chunk + tile - 1) / tile, P->nsm * per_sm));
+  const size_t slot_floats = (size_t)walk_grid * k.nslots * tile * A;
+  const size_t slot_ints = (size_t)walk_grid * k.nslots * tile;
+  const size_t stage_floats = R > 1 ? (size_t)(R - 1) * chunk * A : 0;
+  auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
+  int rc;
+  if ((rc = P->grow(P->work, al(slot_floats * 4) + al(slot_ints * 4) + 2 * al(stage_floats * 4) + 256, stream)))
+    return rc;
+  char *base = (char *)P->work.p;
+  k.scrV = (float *)base;
+  base += al(slot_floats * 4);
+  k.scrW = (int *)base;
+  base += al(slot_ints * 4);
+  float *sa = R > 1 ? (float *)base : nullptr;
+  base += al(stage_floats * 4);
+  float *sb = R > 1 ? (float *)base : nullptr;
+  for (int c0 = 0; c0 < C; c0 += chunk) {
+    const int cc = std::min(chunk, C - c0);
+    int lr = launch_walk_post(k, A, R > 1 ? 3 : 0, tc, sa, sb, c0, cc, walk_grid, stream);
+    if (lr != 0) return fail(SUBBY_ERR_CUDA, std::string("walk launch failed: ") + cudaGetErrorString((cudaError_t)lr));
+    g_launches += 1;
+    if (R == 1) continue;
+    const long long items = (long long)(cc + post_tile() - 1) / post_tile() * (R - 1);
+    const int grid = (int)std::max<long long>(1, std::min<long long>(items, (long long)P->nsm * 8));
+    lr = launch_grad_cx(k, A, sa, sb, P->d_gq, d_g, c0, cc, d_gt, grid, stream);
+    if (lr != 0) return fail(SUBBY_ERR_CUDA, std::string("gradient launch failed: ") + cudaGetErrorString((cudaError_t)lr));
+    g_launches += 1;
+  }
+  return mark_use(P, stream);
+}
+
 // Columns per chunk of the host-pointer pipeline: whole waves of the
 // one-CTA-per-SM kernels (nsm x 256 columns), about eight chunks for large C,
 // a single chunk below two waves (nothing to overlap).
@@ -1738,6 +1808,25 @@ int subby_plan_grad(subby_plan *P, const int32_t *aln, int C, const float *g, fl
     d_aln = a;
     d_g = gg;
     d_ll = ll;
+  }
+  if (P->irrev) {
+    // complex-system plans: distance gradient only (dldS: the gradient with
+    // respect to exchangeabilities does not apply; zeros)
+    double *d_gt = nullptr;
+    CU(pool_alloc((void **)&d_gt, sizeof(double) * R, P->pool, stream));
+    CU(cudaMemsetAsync(d_gt, 0, sizeof(double) * R, stream));
+    rc = run_cx_grad(P, d_aln, C, logL ? d_ll : nullptr, d_g, d_gt, stream);
+    cudaError_t e = cudaSuccess;
+    if (rc == 0) e = cudaMemcpyAsync(dldt, d_gt, sizeof(double) * R, cudaMemcpyDeviceToHost, stream);
+    if (rc == 0 && e == cudaSuccess && logL && !dev)
+      e = cudaMemcpyAsync(logL, d_ll, (size_t)C * 4, cudaMemcpyDeviceToHost, stream);
+    cudaFreeAsync(d_gt, stream);
+    cudaError_t e2 = cudaStreamSynchronize(stream);
+    if (rc) return rc;
+    if (e != cudaSuccess || e2 != cudaSuccess) return cuda_fail(e != cudaSuccess ? e : e2, "gradient readback");
+    dldt[0] = 0.0;
+    for (int i = 0; i < A * A; ++i) dldS[i] = 0.0;
+    return SUBBY_OK;
   }
   // gradient partials live in a separate small allocation per call
   Launch L;

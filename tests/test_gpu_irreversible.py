@@ -173,3 +173,28 @@ def test_reversible_model_as_irreversible_gives_the_same_counts():
     assert_loglike(b['logLike'], a['logLike'])
     assert_cols(b['counts'], a['counts'], COUNTS_RTOL, "counts")
     assert_cols(b['rootProb'], a['rootProb'], ROOTPROB_RTOL, "rootProb")
+
+
+@pytest.mark.parametrize("A,leaves,C", [(4, 10, 200), (20, 6, 40), (64, 5, 30)])
+def test_distance_gradient_vs_oracle(A, leaves, C):
+    """d(sum g logL)/dt for irreversible models (subby/jax/vjp.py:62-133:
+    D V and V^-1 U projections, real part): walk raw staging + the
+    gradient kernel vs the oracle; through LogLikeCustomGrad with autograd."""
+    rng = np.random.default_rng(90 + A)
+    m = models.random_irreversible(A, rng)
+    tree = synth.random_tree(leaves, 0.2, rng)
+    aln = synth.simulated_alignment(tree, m, C, 0.1, rng)
+    ot = oracle.Tree(tree.parentIndex, tree.distanceToParent)
+    g = rng.uniform(0.5, 1.5, C)
+    ref = oracle.loglike_distance_grad(aln, ot, m._asdict(), g=g)
+    plan = sg.Plan(tree, m)
+    ll, dldt, dldS = plan.grad(aln, g=g.astype(np.float32))
+    plan.close()
+    assert_loglike(ll, oracle.LogLike(aln, ot, m._asdict()))
+    scale = max(np.abs(ref).max(), 1e-3)
+    assert np.abs(dldt - ref).max() / scale <= 1e-4, (dldt, ref)
+    assert dldt[0] == 0.0 and not np.any(dldS)
+    d = torch.as_tensor(tree.distanceToParent.copy(), dtype=torch.float64).requires_grad_(True)
+    out = sg.LogLikeCustomGrad(aln, sg.Tree(tree.parentIndex, d), m)
+    (out * torch.as_tensor(g)).sum().backward()
+    assert np.abs(d.grad.numpy() - ref).max() / scale <= 1e-4

@@ -100,8 +100,9 @@ int subby_plan_create(const int32_t *parent_index, const double *distances,
  * Re V diag(e^{mu t}) V^-1 and the complex J(t) are formed in FP64 on the
  * host (subby/oracle/oracle.py:474-534).  LogLike, RootProb, posteriors,
  * Counts and per-branch counts (complex accumulation and back-transform,
- * oracle.py:537-740) then run on this plan; the F81 fast path and the
- * gradient return errors (the reference's F81 path is reversible-only).
+ * oracle.py:537-740) and the distance gradient (subby_plan_grad; dldS
+ * is zeros) then run on this plan; the F81 fast path returns an error (the
+ * reference's F81 path is reversible-only).
  * Counts are implemented for A = 4, 8, 16, 20, 32, 64.
  */
 int subby_plan_create_irrev(const int32_t *parent_index, const double *distances, const double *eigenvalues,

@@ -115,8 +115,9 @@ int subby_plan_create_irrev(const int32_t *parent_index, const double *distances
  * M_n; the root prior is node 0's pi.  LogLike, RootProb and posteriors run
  * the usual kernels on the per-node M(t); Counts and per-branch counts run
  * the complex accumulation once per group of branches sharing a system
- * (each branch projected and back-transformed in its own eigenbasis).  The
- * F81 fast path and the gradient return errors.
+ * (each branch projected and back-transformed in its own eigenbasis); the
+ * distance gradient (subby_plan_grad) uses each node's dM/dt.  The F81
+ * fast path returns an error.
  */
 int subby_plan_create_rows(const int32_t *parent_index, const double *distances, const double *eigenvalues,
                            const double *eigenvectors, const double *pi, int R, int A, subby_plan **out);

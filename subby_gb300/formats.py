@@ -64,9 +64,13 @@ def lookup_table(alphabet, lowercase=True):
     return lut
 
 
-def _as_bytes(sequences):
+def _as_bytes(sequences, names=None):
     C = len(sequences[0])
-    buf = np.frombuffer("".join(sequences).encode("latin-1"), dtype=np.uint8)
+    try:
+        buf = np.frombuffer("".join(sequences).encode("latin-1"), dtype=np.uint8)
+    except UnicodeEncodeError as e:
+        # a character outside one byte is in no alphabet: report it as such
+        _unknown(e.object[e.start], e.start // C, e.start % C, names)
     return buf.reshape(len(sequences), C)
 
 
@@ -130,7 +134,7 @@ def _encode(sequences, alphabet, names, empty_msg, unequal_msg, zero_msg):
         for s in sequences:
             seen.update(s.upper())
         alphabet = detect_alphabet(seen - _GAP_CHARS)
-    return tokenize(_as_bytes(sequences), alphabet, names=names), alphabet
+    return tokenize(_as_bytes(sequences, names), alphabet, names=names), alphabet
 
 
 # ------------------------------------------------------------------- Newick
@@ -334,7 +338,7 @@ def parse_maf(text, alphabet=None):
         for sp in species:
             rows[sp].append(have.get(sp, "-" * width))
     seqs = ["".join(rows[sp]) for sp in species]
-    aln = tokenize(_as_bytes(seqs), alphabet, names=species) if seqs and len(seqs[0]) else \
+    aln = tokenize(_as_bytes(seqs, species), alphabet, names=species) if seqs and len(seqs[0]) else \
         np.zeros((len(species), 0), np.int32)
     return {"alignment": aln, "leaf_names": species, "alphabet": alphabet}
 

@@ -48,3 +48,42 @@ def test_root_prior_identity():
     q = oracle.RootProb(aln, tree, mg)
     np.testing.assert_allclose(ll0, llg + np.log(batch._ratio_to_root0(q, mg['pi'], pi0)), atol=1e-12)
     np.testing.assert_allclose(oracle.LogLike_per_column(aln, tree, [mg] * 30), llg, atol=1e-12)
+
+
+def test_column_groups_by_model():
+    a = models.hky85_diag(2.0, [0.25] * 4)
+    b = models.hky85_diag(3.0, [0.1, 0.2, 0.3, 0.4])
+    aln = np.zeros((5, 6), dtype=np.int32)
+    ms, groups = batch._groups(aln, [a, b, a, a, b, a])
+    assert [idx for _, idx in groups] == [[0, 2, 3, 5], [1, 4]]
+    with pytest.raises(ValueError):
+        batch._groups(aln, [a, b])
+    with pytest.raises(NotImplementedError):
+        batch._groups(aln[:, :2], [models.scale_model(a, np.array([1.0, 2.0])), a])
+
+
+def test_take_and_put_numpy():
+    x = np.arange(20, dtype=np.float32).reshape(4, 5)
+    sub = batch._take(x, [1, 3])
+    np.testing.assert_array_equal(sub, x[:, [1, 3]])
+    out = np.zeros((4, 5), np.float32)
+    batch._put(out, [1, 3], sub)
+    np.testing.assert_array_equal(out[:, [1, 3]], sub)
+
+
+def test_request_models():
+    from subby_gb300 import io
+    m, alpha = io._parse_model({"name": "jukes-cantor", "alphabetSize": 4, "alphabet": list("ACGT")})
+    assert alpha == list("ACGT") and np.allclose(m.pi, 0.25)
+    m, _ = io._parse_model({"name": "HKY_85", "kappa": 2, "pi": [0.1, 0.2, 0.3, 0.4]})
+    assert type(m).__name__ == "DiagModel"
+    Q = np.array([[-1.0, 0.5, 0.5], [0.5, -1.0, 0.5], [0.5, 0.5, -1.0]])
+    m, _ = io._parse_model({"subRate": Q.tolist(), "rootProb": [1 / 3] * 3})
+    assert type(m).__name__ == "DiagModel"            # detailed balance holds
+    m, _ = io._parse_model({"subRate": Q.tolist(), "rootProb": [1 / 3] * 3, "reversible": False})
+    assert type(m).__name__ == "IrrevDiagModel"
+    with pytest.raises(ValueError):
+        io._parse_model({"name": "gtr"})
+    with pytest.raises(ValueError):
+        io._parse_alignment(["AC", "GT"], None)
+    assert io._parse_alignment([["A", "-"], ["G", "T"]], list("ACGT")).tolist() == [[0, 5], [2, 3]]

@@ -156,6 +156,11 @@ int launch_acc_cx(const KParams &p, int A, bool pb, const float *sa, const float
                   int n_lo, int n_hi, float2 *cbuf, int grid, cudaStream_t s);
 int launch_bt_cx(const KParams &p, int A, const float2 *cbuf, int c_base, int c_count, int row, int grid,
                  cudaStream_t s);
+// reversible large-alphabet gradient (k_grad.cu): X_n += sum_c g_c D~_nc (x) U~_nc
+// from the walk's eigen staging, X (R x A x A) FP64
+int xgram_items(int R, int c_count);
+int launch_xgram(int A, const float *sa, const float *sb, const float *g, int c_base, int c_count, int R, double *X,
+                 int grid, cudaStream_t s);
 // distance gradient from the raw staging: grad_t[n] += sum_c g_c (D s)^T G_n U
 int launch_grad_cx(const KParams &p, int A, const float *sa, const float *sb, const float *gq, const float *g,
                    int c_base, int c_count, double *grad_t, int grid, cudaStream_t s);

@@ -238,7 +238,7 @@ struct subby_plan {
   std::vector<int4> prog;
   int prog_steps = 0, prog_slots = 0;
   int4 *d_prog = nullptr;
-  std::vector<double> V, mu, pi;
+  std::vector<double> V, mu, pi, t;   // FP64 model and branch lengths (host)
   float f81_mu = 0.f;
   int f81_model = 0;   // M(t) has the F81 / JC closed form (checked on the host)
   // irreversible model: M(t) from the complex eigensystem (host FP64), and
@@ -459,6 +459,7 @@ int plan_create(const int32_t *parent, const double *dist, const double *evals, 
   }
 
   // ---- FP64 host tables
+  P->t.assign(dist, dist + R);
   P->V.assign(evecs, evecs + (size_t)A * A);
   P->mu.assign(evals, evals + A);
   P->pi.assign(pi, pi + A);
@@ -1396,6 +1397,56 @@ int run_cx(subby_plan *P, const int32_t *d_aln, int C, float *d_logL, float *d_c
   return mark_use(P, stream);
 }
 
+// Gradient of reversible large-alphabet plans: the walk's eigen staging
+// (mode 1, unmasked; LogLike from its inside pass) and k_xgram's per-branch
+// X_n = sum_c g_c D~_nc (x) U~_nc accumulated into d_X (R x A x A, FP64).
+int run_big_grad(subby_plan *P, const int32_t *d_aln, int C, float *d_logL, const float *d_g, double *d_X,
+                 cudaStream_t stream) {
+  const int A = P->A, R = P->R;
+  KParams k = walk_params(P, d_aln, C, kModeCounts | (d_logL ? kModeLogLike : 0), SUBBY_MASK_NONE, nullptr,
+                          d_logL, nullptr, nullptr);
+  const bool tc = (A == 64) && P->d_tab16 && (g_kernel_sel == 0 || g_kernel_sel == 5);
+  const int tile = big_tile();
+  const int H = (A + 31) / 32;
+  int chunk = C;
+  if (R > 1) {
+    const size_t per_col = (size_t)2 * (R - 1) * A * sizeof(float);
+    size_t cmax = std::max<size_t>(tile, kStageBudget / per_col);
+    cmax = cmax / tile * tile;
+    const size_t nch = ((size_t)C + cmax - 1) / cmax;
+    const size_t even = ((size_t)C + nch - 1) / nch;
+    chunk = (int)std::min<size_t>((size_t)C, (even + tile - 1) / tile * tile);
+  }
+  const int walk_grid = std::max(1, std::min((chunk + tile - 1) / tile, P->nsm * (H == 2 ? 1 : 2)));
+  const size_t slot_floats = (size_t)walk_grid * k.nslots * tile * A;
+  const size_t slot_ints = (size_t)walk_grid * k.nslots * tile;
+  const size_t stage_floats = R > 1 ? (size_t)(R - 1) * chunk * A : 0;
+  auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
+  int rc;
+  if ((rc = P->grow(P->work, al(slot_floats * 4) + al(slot_ints * 4) + 2 * al(stage_floats * 4) + 256, stream)))
+    return rc;
+  char *base = (char *)P->work.p;
+  k.scrV = (float *)base;
+  base += al(slot_floats * 4);
+  k.scrW = (int *)base;
+  base += al(slot_ints * 4);
+  float *sa = (float *)base;
+  base += al(stage_floats * 4);
+  float *sb = (float *)base;
+  for (int c0 = 0; c0 < C; c0 += chunk) {
+    const int cc = std::min(chunk, C - c0);
+    int lr = launch_walk(k, A, R > 1 ? 1 : 0, tc, sa, sb, c0, cc, walk_grid, stream);
+    if (lr != 0) return fail(SUBBY_ERR_CUDA, std::string("walk launch failed: ") + cudaGetErrorString((cudaError_t)lr));
+    g_launches += 1;
+    if (R == 1) continue;
+    const int grid = std::max(1, std::min(xgram_items(R, cc), P->nsm * 4));
+    lr = launch_xgram(A, sa, sb, d_g, c0, cc, R, d_X, grid, stream);
+    if (lr != 0) return fail(SUBBY_ERR_CUDA, std::string("gradient launch failed: ") + cudaGetErrorString((cudaError_t)lr));
+    g_launches += 1;
+  }
+  return mark_use(P, stream);
+}
+
 // Distance gradient of complex-system plans (irreversible or per-branch
 // models; subby/jax/vjp.py:62-133): the walk stages D_n s_n and U_n (no
 // mask), k_grad_cx adds sum_c g_c (D_n s_n)^T (dM_n/dt) U_n into grad_t[n].
@@ -1826,6 +1877,56 @@ int subby_plan_grad(subby_plan *P, const int32_t *aln, int C, const float *g, fl
     if (e != cudaSuccess || e2 != cudaSuccess) return cuda_fail(e != cudaSuccess ? e : e2, "gradient readback");
     dldt[0] = 0.0;
     for (int i = 0; i < A * A; ++i) dldS[i] = 0.0;
+    return SUBBY_OK;
+  }
+  if (big_supported(A) && g_kernel_sel == 0) {
+    // walk + per-branch X_n (k_grad.cu); the gradients follow on the host in FP64
+    double *d_X = nullptr;
+    const size_t xb = sizeof(double) * (size_t)R * A * A;
+    CU(pool_alloc((void **)&d_X, xb, P->pool, stream));
+    CU(cudaMemsetAsync(d_X, 0, xb, stream));
+    rc = run_big_grad(P, d_aln, C, logL ? d_ll : nullptr, d_g, d_X, stream);
+    std::vector<double> X((size_t)R * A * A);
+    cudaError_t e = cudaSuccess;
+    if (rc == 0) e = cudaMemcpyAsync(X.data(), d_X, xb, cudaMemcpyDeviceToHost, stream);
+    if (rc == 0 && e == cudaSuccess && logL && !dev)
+      e = cudaMemcpyAsync(logL, d_ll, (size_t)C * 4, cudaMemcpyDeviceToHost, stream);
+    cudaFreeAsync(d_X, stream);
+    cudaError_t e2 = cudaStreamSynchronize(stream);
+    if (rc) return rc;
+    if (e != cudaSuccess || e2 != cudaSuccess) return cuda_fail(e != cudaSuccess ? e : e2, "gradient readback");
+    // d/dt_n = sum_k mu_k e^{mu_k t_n} X_n[k][k];  Cg = sum_n J_n o X_n
+    // (J with the 1e-8 degeneracy rule, subby/oracle/oracle.py:931-959)
+    std::vector<double> Cg((size_t)A * A, 0.0), E(A);
+    dldt[0] = 0.0;
+    for (int n = 1; n < R; ++n) {
+      const double tn = P->t[n];
+      const double *Xn = X.data() + (size_t)n * A * A;
+      for (int k2 = 0; k2 < A; ++k2) E[k2] = std::exp(P->mu[k2] * tn);
+      double gd = 0.0;
+      for (int k2 = 0; k2 < A; ++k2) gd += P->mu[k2] * E[k2] * Xn[k2 * A + k2];
+      dldt[n] = gd;
+      for (int k2 = 0; k2 < A; ++k2)
+        for (int l = 0; l < A; ++l) {
+          const double d = P->mu[k2] - P->mu[l];
+          const double J = std::fabs(d) < 1e-8 ? tn * E[k2] : (E[k2] - E[l]) / d;
+          Cg[k2 * A + l] += J * Xn[k2 * A + l];
+        }
+    }
+    const std::vector<double> &V = P->V;
+    std::vector<double> T((size_t)A * A, 0.0);
+    for (int k2 = 0; k2 < A; ++k2)
+      for (int j = 0; j < A; ++j) {
+        double sm = 0.0;
+        for (int l = 0; l < A; ++l) sm += Cg[k2 * A + l] * V[j * A + l];
+        T[k2 * A + j] = sm;
+      }
+    for (int i = 0; i < A; ++i)
+      for (int j = 0; j < A; ++j) {
+        double sm = 0.0;
+        for (int k2 = 0; k2 < A; ++k2) sm += V[i * A + k2] * T[k2 * A + j];
+        dldS[i * A + j] = sm;
+      }
     return SUBBY_OK;
   }
   // gradient partials live in a separate small allocation per call

@@ -38,19 +38,33 @@ __global__ void __launch_bounds__(kXThreads) k_xgram(const float *__restrict__ s
     float acc[16];
 #pragma unroll
     for (int q = 0; q < 16; ++q) acc[q] = 0.f;
+    auto add = [&](float4 d, const float4 u, float w) {
+      d.x *= w, d.y *= w, d.z *= w, d.w *= w;
+      const float dv[4] = {d.x, d.y, d.z, d.w}, uv[4] = {u.x, u.y, u.z, u.w};
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) acc[4 * i + j] = fmaf(dv[i], uv[j], acc[4 * i + j]);
+    };
+    auto ld = [&](const float *base, int c, int blk) {
+      return __ldg(reinterpret_cast<const float4 *>(base + ((size_t)(n - 1) * c_count + c) * A) + blk);
+    };
     if (busy) {
-      for (int c = c0 + grp; c < c1; c += GROUPS) {
-        const size_t row = ((size_t)(n - 1) * c_count + c) * A;
-        float4 d = __ldg(reinterpret_cast<const float4 *>(sa + row) + kb);
-        const float4 u = __ldg(reinterpret_cast<const float4 *>(sb + row) + lb);
-        const float w = g ? __ldg(g + c_base + c) : 1.f;
-        d.x *= w, d.y *= w, d.z *= w, d.w *= w;
-        const float dv[4] = {d.x, d.y, d.z, d.w}, uv[4] = {u.x, u.y, u.z, u.w};
+      int c = c0 + grp;
+      // four columns' loads in flight before their FMAs (the pass is load-latency-bound)
+      for (; c + 3 * GROUPS < c1; c += 4 * GROUPS) {
+        float4 d[4], u[4];
+        float w[4];
 #pragma unroll
-        for (int i = 0; i < 4; ++i)
+        for (int q = 0; q < 4; ++q) {
+          d[q] = ld(sa, c + q * GROUPS, kb);
+          u[q] = ld(sb, c + q * GROUPS, lb);
+          w[q] = g ? __ldg(g + c_base + c + q * GROUPS) : 1.f;
+        }
 #pragma unroll
-          for (int j = 0; j < 4; ++j) acc[4 * i + j] = fmaf(dv[i], uv[j], acc[4 * i + j]);
+        for (int q = 0; q < 4; ++q) add(d[q], u[q], w[q]);
       }
+      for (; c < c1; c += GROUPS) add(ld(sa, c, kb), ld(sb, c, lb), g ? __ldg(g + c_base + c) : 1.f);
     }
     __syncthreads();  // the previous item's reads of s_part are done
     if (busy)

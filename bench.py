@@ -158,7 +158,9 @@ def cpu_oracle_throughput(aln, tree, model, target_s=12.0, pool=None, cores=None
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=None,
+                    help="timed steps (default 200 for this implementation, whose steps take ~3 ms, so that "
+                         "the clock sampler sees the timed region; 10 for --impl reference)")
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--columns", type=int, default=1 << 20)
@@ -173,6 +175,8 @@ def main():
     if args.warmup < 3:
         args.warmup = 3
 
+    if args.steps is None:
+        args.steps = 10 if args.impl == "reference" else (200 if args.workload == "plain_large" else 20)
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))

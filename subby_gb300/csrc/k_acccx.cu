@@ -220,7 +220,7 @@ __global__ void __launch_bounds__(kCxThreads) k_acc_cx(const KParams P, const fl
 // V T in FP64 with V, Vinv, T in shared memory (224 KB at A = 64); output
 // row `row` of counts.
 template <int A>
-__global__ void __launch_bounds__(kCxThreads) k_bt_cx(const KParams P, const float2 *__restrict__ cbuf, int c_base,
+__global__ void __launch_bounds__(1024) k_bt_cx(const KParams P, const float2 *__restrict__ cbuf, int c_base,
                                                       int c_count, int row) {
   extern __shared__ __align__(16) double2 s_bt[];
   double2 *sV = s_bt;           // A x A
@@ -298,7 +298,7 @@ int bt_launch(const KParams &p, const float2 *cbuf, int c_base, int c_count, int
   const size_t smem = (size_t)3 * A * A * sizeof(double2) + (size_t)A * A * sizeof(float2);
   cudaError_t e = cudaFuncSetAttribute(k_bt_cx<A>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return (int)e;
-  k_bt_cx<A><<<grid, kCxThreads, smem, s>>>(p, cbuf, c_base, c_count, row);
+  k_bt_cx<A><<<grid, 1024, smem, s>>>(p, cbuf, c_base, c_count, row);  // 32 warps: FP64 latency
   return (int)cudaGetLastError();
 }
 

@@ -9,7 +9,7 @@ from .models import (hky85_diag, jukes_cantor_model, f81_model, diagonalize_rate
                      diagonalize_irreversible, gamma_rate_categories, scale_model)
 from .api import (LogLike, Counts, BranchCounts, RootProb, MixturePosterior, LogLikeCustomGrad, InsideOutside, Plan,
                   get_plan, clear_plan_cache)
-from . import _lib, formats, io
+from . import _lib, formats, io, maf_batch
 
 __all__ = ["BranchCounts", "Tree", "DiagModel", "IrrevDiagModel", "RateModel", "irrev_model_from_rate_matrix",
            "diagonalize_irreversible", "gamma_rate_categories", "scale_model", "MixturePosterior", "hky85_diag", "jukes_cantor_model", "f81_model",

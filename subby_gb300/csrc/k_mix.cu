@@ -31,8 +31,9 @@ __global__ void k_mixture(const float *__restrict__ logL, const double *__restri
 
 extern "C" int subby_mixture_posterior(const float *logL, const double *log_weights, int K, int C, float *out,
                                        int flags, void *stream_) {
-  if (!logL || !log_weights || !out || K <= 0 || C < 0) return SUBBY_ERR_ARG;
-  if (C == 0) return SUBBY_OK;
+  if (!log_weights || K <= 0 || C < 0) return SUBBY_ERR_ARG;
+  if (C == 0) return SUBBY_OK;  // empty device buffers may be null
+  if (!logL || !out) return SUBBY_ERR_ARG;
   cudaStream_t s = (cudaStream_t)stream_;
   const int block = 256;
   int dev = 0, nsm = 1;

@@ -50,9 +50,10 @@ __global__ void k_tokenize(const uint8_t *__restrict__ in, long long n, const in
 
 extern "C" int subby_tokenize(const uint8_t *chars, int64_t n, const int32_t *lut, int32_t *out,
                               int64_t *first_bad, void *stream_) {
-  if (!chars || !lut || !out || !first_bad || n < 0) return SUBBY_ERR_ARG;
+  if (!lut || !first_bad || n < 0) return SUBBY_ERR_ARG;
+  if (n == 0) return SUBBY_OK;  // empty device buffers may be null
+  if (!chars || !out) return SUBBY_ERR_ARG;
   if ((reinterpret_cast<uintptr_t>(chars) & 15) || (reinterpret_cast<uintptr_t>(out) & 15)) return SUBBY_ERR_ARG;
-  if (n == 0) return SUBBY_OK;
   cudaStream_t s = (cudaStream_t)stream_;
   int dev = 0, nsm = 1;
   cudaGetDevice(&dev);

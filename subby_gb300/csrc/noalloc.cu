@@ -61,16 +61,17 @@ extern "C" int subby_counts_noalloc(const int32_t *d_aln, const int32_t *parent,
                                     float *d_counts, float *d_logL, void *stream_) {
   using namespace subby;
   const int A = 4;
-  if (!d_aln || !parent || !dist || !evals || !evecs || !pi || !d_counts)
-    return nfail(SUBBY_ERR_ARG, "null argument");
+  if (!parent || !dist || !evals || !evecs || !pi) return nfail(SUBBY_ERR_ARG, "null argument");
   if (C < 0) return nfail(SUBBY_ERR_ARG, "negative column count");
   if (counts_kind != SUBBY_COUNTS_EIGEN && counts_kind != SUBBY_COUNTS_F81)
     return nfail(SUBBY_ERR_ARG, "bad counts_kind");
-  if (mask_mode < 0 || mask_mode > 2 || (mask_mode == SUBBY_MASK_GIVEN && !d_mask))
-    return nfail(SUBBY_ERR_ARG, "bad mask_mode or missing mask");
+  if (mask_mode < 0 || mask_mode > 2) return nfail(SUBBY_ERR_ARG, "bad mask_mode");
   if (R < 1 || R > kNoAllocMaxNodes)
     return nfail(SUBBY_ERR_UNSUPPORTED, "tree larger than the no-allocation limit of 1023 nodes");
+  // zero columns: nothing to compute (empty device buffers may be null)
   if (C == 0) return SUBBY_OK;
+  if (!d_aln || !d_counts) return nfail(SUBBY_ERR_ARG, "null alignment or counts");
+  if (mask_mode == SUBBY_MASK_GIVEN && !d_mask) return nfail(SUBBY_ERR_ARG, "missing mask");
 
   // ---- tree validation and children (fixed-size arrays, no heap)
   int left[kNoAllocMaxNodes], right[kNoAllocMaxNodes], cnt[kNoAllocMaxNodes];

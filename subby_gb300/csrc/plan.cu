@@ -1607,13 +1607,15 @@ int subby_plan_run(subby_plan *P, const int32_t *aln, int C, float *logL, float 
                    void *stream_) {
   g_last_error.clear();
   g_launches = 0;
-  if (!P || !aln) return fail(SUBBY_ERR_ARG, "null plan or alignment");
+  if (!P) return fail(SUBBY_ERR_ARG, "null plan");
   if (C < 0) return fail(SUBBY_ERR_ARG, "negative column count");
   if (mask_mode < 0 || mask_mode > 2) return fail(SUBBY_ERR_ARG, "bad mask_mode");
-  if (mask_mode == SUBBY_MASK_GIVEN && !mask) return fail(SUBBY_ERR_ARG, "mask required");
   if (counts_kind != SUBBY_COUNTS_EIGEN && counts_kind != SUBBY_COUNTS_F81)
     return fail(SUBBY_ERR_ARG, "bad counts_kind");
+  // zero columns: nothing to compute (an empty device buffer may be null)
   if (C == 0) return SUBBY_OK;
+  if (!aln) return fail(SUBBY_ERR_ARG, "null alignment");
+  if (mask_mode == SUBBY_MASK_GIVEN && !mask) return fail(SUBBY_ERR_ARG, "mask required");
   std::lock_guard<std::mutex> g(P->lock);
   cudaStream_t stream = (cudaStream_t)stream_;
   int dev = 0;
@@ -1730,13 +1732,14 @@ int subby_plan_branch_counts(subby_plan *P, const int32_t *aln, int C, float *br
                              int mask_mode, const uint8_t *mask, int flags, void *stream_) {
   g_last_error.clear();
   g_launches = 0;
-  if (!P || !aln || !branchCounts) return fail(SUBBY_ERR_ARG, "null argument");
+  if (!P) return fail(SUBBY_ERR_ARG, "null plan");
   if (C < 0) return fail(SUBBY_ERR_ARG, "negative column count");
   if (mask_mode < 0 || mask_mode > 2) return fail(SUBBY_ERR_ARG, "bad mask_mode");
-  if (mask_mode == SUBBY_MASK_GIVEN && !mask) return fail(SUBBY_ERR_ARG, "mask required");
   if (counts_kind != SUBBY_COUNTS_EIGEN && counts_kind != SUBBY_COUNTS_F81)
     return fail(SUBBY_ERR_ARG, "bad counts_kind");
   if (C == 0) return SUBBY_OK;
+  if (!aln || !branchCounts) return fail(SUBBY_ERR_ARG, "null argument");
+  if (mask_mode == SUBBY_MASK_GIVEN && !mask) return fail(SUBBY_ERR_ARG, "mask required");
   std::lock_guard<std::mutex> g(P->lock);
   cudaStream_t stream = (cudaStream_t)stream_;
   int dev = 0;
@@ -1785,14 +1788,15 @@ int subby_plan_posteriors(subby_plan *P, const int32_t *aln, int C, int node, fl
                           int flags, void *stream_) {
   g_last_error.clear();
   g_launches = 0;
-  if (!P || !aln) return fail(SUBBY_ERR_ARG, "null plan or alignment");
-  if (!nodePost && !branchPost) return fail(SUBBY_ERR_ARG, "no output requested");
+  if (!P) return fail(SUBBY_ERR_ARG, "null plan");
   if (C < 0) return fail(SUBBY_ERR_ARG, "negative column count");
   if (node < -1 || node >= P->R) return fail(SUBBY_ERR_ARG, "node index out of range");
-  if (node == 0 && branchPost) return fail(SUBBY_ERR_ARG, "node 0 (the root) has no branch");
   if (!post_supported(P->A))
     return fail(SUBBY_ERR_UNSUPPORTED, "posteriors are implemented for A = 4, 8, 16, 20, 32, 64");
   if (C == 0) return SUBBY_OK;
+  if (!aln) return fail(SUBBY_ERR_ARG, "null alignment");
+  if (!nodePost && !branchPost) return fail(SUBBY_ERR_ARG, "no output requested");
+  if (node == 0 && branchPost) return fail(SUBBY_ERR_ARG, "node 0 (the root) has no branch");
   std::lock_guard<std::mutex> g(P->lock);
   cudaStream_t stream = (cudaStream_t)stream_;
   int dev = 0;
@@ -1832,8 +1836,14 @@ int subby_plan_grad(subby_plan *P, const int32_t *aln, int C, const float *g, fl
                     double *dldt, double *dldS, int flags, void *stream_) {
   g_last_error.clear();
   g_launches = 0;
-  if (!P || !aln || !dldt || !dldS) return fail(SUBBY_ERR_ARG, "null argument");
-  if (C <= 0) return fail(SUBBY_ERR_ARG, "C must be positive");
+  if (!P || !dldt || !dldS) return fail(SUBBY_ERR_ARG, "null argument");
+  if (C < 0) return fail(SUBBY_ERR_ARG, "negative column count");
+  if (C == 0) {  // the empty sum: zero gradients
+    std::fill(dldt, dldt + P->R, 0.0);
+    std::fill(dldS, dldS + (size_t)P->A * P->A, 0.0);
+    return SUBBY_OK;
+  }
+  if (!aln) return fail(SUBBY_ERR_ARG, "null alignment");
   std::lock_guard<std::mutex> lk(P->lock);
   cudaStream_t stream = (cudaStream_t)stream_;
   const int A = P->A, R = P->R;

@@ -287,3 +287,35 @@ def test_tensor_core_walk_repeatable_small_tree():
     for _ in range(30):
         np.testing.assert_array_equal(plan.run(aln, loglike=True, counts=True)['counts'], ref)
     plan.close()
+
+
+@pytest.mark.parametrize("A", [4, 20])
+def test_zero_columns(A):
+    """C = 0 gives empty outputs of the reference's shapes (the reference
+    oracle returns them too) through every entry point, on host arrays and on
+    CUDA tensors (whose data pointer is null when empty); the gradient of the
+    empty sum is zero."""
+    rng = np.random.default_rng(4)
+    m = models.hky85_diag(2.0, [0.3, 0.2, 0.25, 0.25]) if A == 4 else models.random_reversible(A, rng)[0]
+    tree = synth.random_tree(6, 0.1, rng)
+    R = len(tree.parentIndex)
+    otree = oracle.Tree(tree.parentIndex, tree.distanceToParent)
+    md = _model_dict(m)
+    empty = np.zeros((R, 0), np.int32)
+    assert oracle.Counts(empty, otree, md).shape == (A, A, 0)
+    plan = sg.Plan(tree, m)
+    for aln in (empty, torch.zeros((R, 0), dtype=torch.int32, device="cuda")):
+        r = plan.run(aln, loglike=True, counts=True, rootprob=True)
+        assert tuple(r['logLike'].shape) == (0,)
+        assert tuple(r['counts'].shape) == (A, A, 0)
+        assert tuple(r['rootProb'].shape) == (A, 0)
+        r = plan.run(aln, loglike=False, counts=True, branch_mask=np.zeros((R, 0), bool))
+        assert tuple(r['counts'].shape) == (A, A, 0)
+        assert tuple(plan.branch_counts(aln).shape) == (R, A, A, 0)
+        post = plan.posteriors(aln, want_node=True, want_branch=True)
+        assert tuple(post['node'].shape) == (R, A, 0) and tuple(post['branch'].shape) == (R, A, A, 0)
+        assert tuple(sg.MixturePosterior(aln, tree, [m, m], np.log([0.25, 0.75])).shape) == (2, 0)
+    torch.cuda.synchronize()
+    ll, dldt, dldS = plan.grad(empty)
+    assert ll.shape == (0,) and dldt.shape == (R,) and not dldt.any() and not dldS.any()
+    plan.close()

@@ -4,7 +4,10 @@ Same names, arguments, return values and errors as subby/formats.py
 (``detect_alphabet`` :37-60, ``parse_newick`` :150-225, ``parse_fasta``
 :228-315, ``parse_stockholm`` :318-410, ``parse_maf`` :413-507,
 ``parse_strings`` :510-564, ``parse_dict`` :567-625,
-``combine_tree_alignment`` :1101-1169).  Differences are in how, not what:
+``combine_tree_alignment`` :1101-1169; the k-mer, codon and paired-column
+transforms ``sliding_windows``, ``all_column_ktuples``, ``kmer_tokenize``,
+``genetic_code``, ``codon_to_sense``, ``split_paired_columns``,
+``merge_paired_columns`` :628-1098).  Differences are in how, not what:
 
 * characters are tokenised through a 256-entry lookup table over the raw
   bytes (numpy on the host; ``tokenize(..., device=...)`` runs the CUDA
@@ -381,3 +384,193 @@ def combine_tree_alignment(tree_result, alignment_result):
                           tree=Tree(parentIndex=tree_result["parentIndex"],
                                     distanceToParent=tree_result["distanceToParent"]),
                           alphabet=alphabet, leaf_names=leaves)
+
+
+# ---------------------------------------------------------------------------
+# k-mer, codon and paired-column transforms (subby/formats.py:628-1098):
+# derived alphabets for the large-A paths (A^k k-mers, 61 sense codons,
+# A^2 column pairs), same names, token conventions and errors.
+# ---------------------------------------------------------------------------
+
+class KmerIndex:
+    """Column tuples <-> positions of a k-mer alignment (subby/formats.py:628-656)."""
+
+    def __init__(self, column_tuples):
+        self.tuples = np.asarray(column_tuples, dtype=np.int64)
+        self._pos = {tuple(int(x) for x in t): i for i, t in enumerate(self.tuples)}
+
+    def tuple_to_idx(self, t):
+        """Position of a column tuple in the k-mer alignment, -1 if absent."""
+        return self._pos.get(tuple(int(x) for x in t), -1)
+
+    def idx_to_tuple(self, idx):
+        return tuple(self.tuples[idx])
+
+    def __len__(self):
+        return len(self.tuples)
+
+    def __repr__(self):
+        return f"KmerIndex({len(self)} tuples, k={self.tuples.shape[1] if len(self) > 0 else 0})"
+
+
+def sliding_windows(C, k, stride=None, offset=0, edge="truncate"):
+    """(M, k) int64 column indices of windows of k columns starting at
+    offset, offset + stride, ... (stride defaults to k).  edge='truncate'
+    keeps whole windows only; edge='pad' keeps the ragged last windows with
+    -1 past the end (subby/formats.py:659-693)."""
+    step = k if stride is None else stride
+    if edge == "truncate":
+        starts = np.arange(offset, C - k + 1, step)
+    elif edge == "pad":
+        starts = np.arange(offset, C, step)
+    else:
+        raise ValueError(f"Unknown edge mode: {edge!r}")
+    cols = (starts[:, None] + np.arange(k)[None, :]).astype(np.int64)
+    if edge == "pad":
+        cols[cols >= C] = -1
+    return cols.reshape(-1, k)
+
+
+def all_column_ktuples(C, k, ordered=True):
+    """Every k-tuple of distinct columns: permutations (ordered) or
+    combinations, in itertools order, as (T, k) int64 (subby/formats.py:696-720)."""
+    from itertools import combinations, permutations
+    gen = permutations(range(C), k) if ordered else combinations(range(C), k)
+    return np.array(list(gen), dtype=np.int64).reshape(-1, k)
+
+
+def _kmer_labels(alphabet, k):
+    if alphabet is None:
+        return None
+    from itertools import product
+    return ["".join(p) for p in product(alphabet, repeat=k)]
+
+
+def kmer_tokenize(alignment, A, k_or_tuples, gap_mode="any", alphabet=None):
+    """k-mer tokens of an A-state alignment (subby/formats.py:723-842).
+
+    ``k_or_tuples``: an int k (consecutive non-overlapping windows; C must be
+    a multiple of k) or a (T, k) array of column tuples (-1 = a position
+    outside the alignment, read as unobserved).  Output tokens: the base-A
+    number of k observed states (first column most significant), A^k when
+    any position is unobserved, A^k + 1 when a position is a gap (token < 0
+    or > A) — with gap_mode='all' only all-gap k-mers are gaps and partly
+    gapped ones get the illegal token A^k + 2.  Returns {'alignment' (R, T)
+    int32, 'A_kmer': A^k, 'index': KmerIndex, 'alphabet' (labels, when an
+    alphabet is given)}."""
+    aln = np.asarray(alignment, dtype=np.int32)
+    R, C = aln.shape
+    if isinstance(k_or_tuples, (int, np.integer)):
+        k = int(k_or_tuples)
+        if C % k != 0:
+            raise ValueError(f"Number of columns ({C}) not divisible by k ({k})")
+        tuples = sliding_windows(C, k)
+    else:
+        tuples = np.asarray(k_or_tuples, dtype=np.int64)
+        if tuples.ndim != 2:
+            raise ValueError(f"column_tuples must be 2D (T, k), got shape {tuples.shape}")
+        k = tuples.shape[1]
+    A_k = A ** k
+    out = {"alignment": np.zeros((R, 0), dtype=np.int32), "A_kmer": A_k, "index": KmerIndex(tuples)}
+    if len(tuples):
+        outside = tuples < 0
+        b = aln[:, np.where(outside, 0, tuples)]                  # (R, T, k)
+        b = np.where(outside[None], A, b)
+        obs = (b >= 0) & (b < A)
+        gap = (b < 0) | (b > A)
+        weights = np.int64(A) ** np.arange(k - 1, -1, -1, dtype=np.int64)
+        code = (np.where(obs, b, 0).astype(np.int64) * weights).sum(axis=2)
+        tok = np.where(obs.all(axis=2), code, A_k)
+        any_gap, all_gap = gap.any(axis=2), gap.all(axis=2)
+        if gap_mode == "any":
+            tok = np.where(any_gap, A_k + 1, tok)
+        elif gap_mode == "all":
+            tok = np.where(all_gap, A_k + 1, np.where(any_gap, A_k + 2, tok))
+        else:
+            raise ValueError(f"Unknown gap_mode: {gap_mode!r}")
+        out["alignment"] = tok.astype(np.int32)
+    labels = _kmer_labels(alphabet, k)
+    if labels is not None:
+        out["alphabet"] = labels
+    return out
+
+
+# The standard genetic code, third / second / first base varying fastest in
+# T, C, A, G order (the textbook table read row by row); '*' = stop.
+_CODE_TCAG = "FFLLSSSSYY**CC*WLLLLPPPPHHQQRRRRIIIMTTTTNNKKSSRRVVVVAAAADDEEGGGG"
+
+
+def genetic_code():
+    """The standard genetic code over the 64 codons in ACGT lexicographic
+    order (AAA, AAC, ..., TTT): codons, amino_acids, sense_mask, the 61
+    sense_indices, codon_to_sense (stop -> -1), sense_codons,
+    sense_amino_acids (subby/formats.py:877-919)."""
+    from itertools import product
+    tcag = "TCAG"
+    codons = ["".join(p) for p in product("ACGT", repeat=3)]
+    aa = [_CODE_TCAG[16 * tcag.index(c[0]) + 4 * tcag.index(c[1]) + tcag.index(c[2])] for c in codons]
+    sense = np.array([a != "*" for a in aa], dtype=bool)
+    idx = np.flatnonzero(sense).astype(np.int64)
+    to_sense = np.full(64, -1, dtype=np.int64)
+    to_sense[idx] = np.arange(len(idx), dtype=np.int64)
+    return {"codons": codons, "amino_acids": aa, "sense_mask": sense, "sense_indices": idx,
+            "codon_to_sense": to_sense, "sense_codons": [codons[i] for i in idx],
+            "sense_amino_acids": [aa[i] for i in idx]}
+
+
+def codon_to_sense(alignment, A=64):
+    """64-codon tokens -> 61 sense-codon tokens: sense codons renumbered,
+    stop codons and gaps (A + 1 or negative) -> 62, unobserved (A) and
+    anything else -> 61 (subby/formats.py:922-965)."""
+    aln = np.asarray(alignment, dtype=np.int32)
+    table = genetic_code()["codon_to_sense"].copy()
+    table[table < 0] = 62
+    res = np.full_like(aln, 61)
+    codon = (aln >= 0) & (aln < 64)
+    res[codon] = table[aln[codon]]
+    res[aln == A] = 61
+    res[(aln == A + 1) | (aln < 0)] = 62
+    return {"alignment": res, "A_sense": 61, "alphabet": genetic_code()["sense_codons"]}
+
+
+def split_paired_columns(alignment, paired_columns, A=20):
+    """Split an alignment into an A^2-state alignment of column pairs and an
+    A-state alignment of the columns in no pair (subby/formats.py:972-1039);
+    pairs and singles are k-mer tokens with gap_mode='any'."""
+    aln = np.asarray(alignment, dtype=np.int32)
+    N, C = aln.shape
+    in_pair = {int(c) for pc in paired_columns for c in pc}
+    singles = [c for c in range(C) if c not in in_pair]
+    if len(paired_columns):
+        pt = kmer_tokenize(aln, A, np.array(paired_columns, dtype=np.int64), gap_mode="any")
+        p_aln, p_idx = pt["alignment"], pt["index"]
+    else:
+        p_aln, p_idx = np.zeros((N, 0), dtype=np.int32), KmerIndex(np.zeros((0, 2), dtype=np.int64))
+    if singles:
+        st = kmer_tokenize(aln, A, np.array(singles, dtype=np.int64).reshape(-1, 1), gap_mode="any")
+        s_aln, s_idx = st["alignment"], st["index"]
+    else:
+        s_aln, s_idx = np.zeros((N, 0), dtype=np.int32), KmerIndex(np.zeros((0, 1), dtype=np.int64))
+    return {"paired_alignment": p_aln, "singles_alignment": s_aln, "paired_columns": list(paired_columns),
+            "single_columns": singles, "A_paired": A * A, "A_singles": A, "paired_index": p_idx,
+            "singles_index": s_idx}
+
+
+def merge_paired_columns(paired_posterior, singles_posterior, split_info):
+    """(A, C) per-column posteriors from (A^2, P) pair posteriors (marginals
+    over the partner column) and (A, S) single-column posteriors, in the
+    original column order (subby/formats.py:1042-1098)."""
+    pp = np.asarray(paired_posterior, dtype=np.float64)
+    sp = np.asarray(singles_posterior, dtype=np.float64)
+    pairs = split_info["paired_columns"]
+    singles = split_info["single_columns"]
+    A = split_info["A_singles"]
+    cols = [c for pc in pairs for c in pc] + list(singles)
+    out = np.zeros((A, max(cols) + 1 if cols else 0), dtype=np.float64)
+    for p, (ci, cj) in enumerate(pairs):
+        joint = pp[:A * A, p].reshape(A, A)
+        out[:, ci] = joint.sum(axis=1)
+        out[:, cj] = joint.sum(axis=0)
+    for s, c in enumerate(singles):
+        out[:, c] = sp[:, s]
+    return out

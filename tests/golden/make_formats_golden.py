@@ -4,7 +4,9 @@
 
 Runs the reference's own parsers (``subby.formats``: parse_newick,
 parse_fasta, parse_stockholm, parse_maf, parse_strings, parse_dict,
-combine_tree_alignment, detect_alphabet) and JSON request runner
+combine_tree_alignment, detect_alphabet; sliding_windows,
+all_column_ktuples, kmer_tokenize, codon_to_sense, split_paired_columns,
+merge_paired_columns) and JSON request runner
 (``subby.io.run``, FP64 oracle) on small synthetic inputs written here,
 and stores inputs, outputs and error messages as JSON.
 """
@@ -38,6 +40,60 @@ STRINGS = [["ACGT", "AC-T", "acgt"], ["ACDE", "FGHI"]]
 DICTS = [{"human": "ACGTT", "mouse": "AC.TT", "rat": "ACGTA"}]
 BAD = [("fasta", ">a\nACGX\n>b\nACGT\n", ["A", "C", "G", "T"]), ("fasta", ">a\nACG\n>b\nACGT\n", None),
        ("strings", ["ACGJ", "ACGT"], ["A", "C", "G", "T"]), ("newick", "((A,B);", None), ("newick", "", None)]
+
+
+def _err(fn, *a, **k):
+    try:
+        fn(*a, **k)
+    except Exception as e:  # noqa: BLE001
+        return f"{type(e).__name__}: {e}"
+    return None
+
+
+def _transforms(F):
+    """k-mer, codon and paired-column transforms (subby/formats.py:628-1098)."""
+    rng = np.random.default_rng(77)
+    t = {"sliding": [], "ktuples": [], "kmer": [], "codon": [], "paired": []}
+    for C, k, stride, offset, edge in [(10, 3, None, 0, "truncate"), (10, 3, None, 0, "pad"), (10, 4, 2, 1, "pad"),
+                                       (5, 6, None, 0, "truncate"), (7, 2, 3, 0, "truncate"), (6, 2, 1, 2, "pad")]:
+        t["sliding"].append({"args": [C, k, stride, offset, edge],
+                             "out": F.sliding_windows(C, k, stride, offset, edge).tolist()})
+    t["sliding_error"] = _err(F.sliding_windows, 10, 3, edge="wrap")
+    for C, k, ordered in [(4, 2, True), (5, 3, False), (1, 2, True), (3, 1, False)]:
+        t["ktuples"].append({"args": [C, k, ordered], "out": F.all_column_ktuples(C, k, ordered).tolist()})
+    a4 = rng.integers(-1, 6, size=(5, 12))
+    cases = [(a4, 4, 2, "any", None), (a4, 4, 3, "all", ["A", "C", "G", "T"]),
+             (a4, 4, F.sliding_windows(12, 5, 3, 0, "pad"), "any", None),
+             (a4, 4, F.sliding_windows(12, 5, 3, 0, "pad"), "all", None),
+             (a4, 4, [[0, 11], [3, 3], [7, 1]], "all", list("ACGT")), (a4, 4, np.zeros((0, 2)), "any", list("AC")),
+             (rng.integers(-1, 22, size=(4, 6)), 20, [[0, 1, 2], [5, 4, 3]], "any", None)]
+    for aln, A, kt, mode, alpha in cases:
+        r = F.kmer_tokenize(aln, A, kt, gap_mode=mode, alphabet=alpha)
+        t["kmer"].append({"alignment": np.asarray(aln).tolist(), "A": A,
+                          "k_or_tuples": kt if isinstance(kt, int) else np.asarray(kt).tolist(),
+                          "k": int(r["index"].tuples.shape[1]),
+                          "gap_mode": mode, "alphabet": alpha, "out": r["alignment"].tolist(), "A_kmer": r["A_kmer"],
+                          "tuples": r["index"].tuples.tolist(), "repr": repr(r["index"]),
+                          "labels": r.get("alphabet")})
+    t["kmer_errors"] = [_err(F.kmer_tokenize, a4, 4, 5), _err(F.kmer_tokenize, a4, 4, [0, 1, 2]),
+                        _err(F.kmer_tokenize, a4, 4, 2, gap_mode="some")]
+    codon = rng.integers(-2, 68, size=(3, 40))
+    t["codon"] = {"alignment": codon.tolist(), "out": F.codon_to_sense(codon)["alignment"].tolist(),
+                  "out_A63": F.codon_to_sense(codon, A=63)["alignment"].tolist(),
+                  "alphabet": F.codon_to_sense(codon)["alphabet"]}
+    a20 = rng.integers(-1, 22, size=(4, 8))
+    for pairs in ([(0, 3), (5, 2)], [], [(0, 1), (2, 3), (4, 5), (6, 7)], [(7, 0)]):
+        sp = F.split_paired_columns(a20, pairs, A=20)
+        P, S = len(pairs), len(sp["single_columns"])
+        pp = np.round(rng.random((400, P)), 3)
+        ss = np.round(rng.random((20, S)), 3)
+        t["paired"].append({"alignment": a20.tolist(), "pairs": [list(p) for p in pairs],
+                            "paired_alignment": sp["paired_alignment"].tolist(),
+                            "singles_alignment": sp["singles_alignment"].tolist(),
+                            "single_columns": sp["single_columns"], "A_paired": sp["A_paired"],
+                            "paired_post": pp.tolist(), "singles_post": ss.tolist(),
+                            "merged": F.merge_paired_columns(pp, ss, sp).tolist()})
+    return t
 
 
 def main():
@@ -101,6 +157,7 @@ def main():
                  "alignment": rng.integers(0, 6, size=(5, 7)).tolist()})
     for r in reqs:
         out["requests"].append({"request": r, "result": IO.run(r)})
+    out["transforms"] = _transforms(F)
     with open(os.path.join(HERE, "formats", "formats.json"), "w") as f:
         json.dump(out, f, indent=1)
     print("wrote formats/formats.json")

@@ -74,3 +74,61 @@ def test_request_parsing():
         assert compute == case["request"].get("compute", ["logLike", "counts", "rootProb"])
     m, _ = io._parse_model(G["requests"][2]["request"]["model"])
     assert type(m).__name__ == "IrrevDiagModel"   # random rate matrix: detailed balance fails
+
+
+T = G["transforms"]
+
+
+def test_sliding_windows_and_ktuples():
+    for c in T["sliding"]:
+        got = formats.sliding_windows(*c["args"])
+        assert got.dtype == np.int64 and got.shape[1] == c["args"][1] and got.tolist() == c["out"]
+    with pytest.raises(ValueError) as ei:
+        formats.sliding_windows(10, 3, edge="wrap")
+    assert f"ValueError: {ei.value}" == T["sliding_error"]
+    for c in T["ktuples"]:
+        got = formats.all_column_ktuples(*c["args"])
+        assert got.dtype == np.int64 and got.shape[1] == c["args"][1] and got.tolist() == c["out"]
+
+
+def test_kmer_tokenize():
+    for c in T["kmer"]:
+        kt = c["k_or_tuples"]
+        kt = kt if isinstance(kt, int) else np.array(kt, dtype=np.int64).reshape(-1, c["k"])
+        r = formats.kmer_tokenize(np.array(c["alignment"]), c["A"], kt,
+                                  gap_mode=c["gap_mode"], alphabet=c["alphabet"])
+        assert r["alignment"].dtype == np.int32 and r["alignment"].tolist() == c["out"]
+        assert r["A_kmer"] == c["A_kmer"] and r["index"].tuples.tolist() == c["tuples"]
+        assert repr(r["index"]) == c["repr"] and r.get("alphabet") == c["labels"]
+        for i, t in enumerate(c["tuples"]):
+            assert r["index"].tuple_to_idx(t) == i and list(r["index"].idx_to_tuple(i)) == t
+        assert r["index"].tuple_to_idx((99, 98)) == -1
+    a = np.array(T["kmer"][0]["alignment"])
+    for args, kw, exp in zip(([a, 4, 5], [a, 4, [0, 1, 2]], [a, 4, 2]), ({}, {}, {"gap_mode": "some"}),
+                             T["kmer_errors"]):
+        with pytest.raises(ValueError) as ei:
+            formats.kmer_tokenize(*args, **kw)
+        assert f"ValueError: {ei.value}" == exp
+
+
+def test_codon_to_sense_and_genetic_code():
+    c = T["codon"]
+    aln = np.array(c["alignment"])
+    r = formats.codon_to_sense(aln)
+    assert r["alignment"].tolist() == c["out"] and r["A_sense"] == 61 and r["alphabet"] == c["alphabet"]
+    assert formats.codon_to_sense(aln, A=63)["alignment"].tolist() == c["out_A63"]
+    gc = formats.genetic_code()
+    assert len(gc["sense_codons"]) == 61 and [gc["codons"][i] for i in (48, 50, 56)] == ["TAA", "TAG", "TGA"]
+    assert gc["amino_acids"][gc["codons"].index("ATG")] == "M" and gc["sense_codons"] == c["alphabet"]
+
+
+def test_split_and_merge_paired_columns():
+    for c in T["paired"]:
+        pairs = [tuple(p) for p in c["pairs"]]
+        sp = formats.split_paired_columns(np.array(c["alignment"]), pairs, A=20)
+        assert sp["paired_alignment"].tolist() == c["paired_alignment"]
+        assert sp["singles_alignment"].tolist() == c["singles_alignment"]
+        assert sp["single_columns"] == c["single_columns"] and sp["A_paired"] == c["A_paired"]
+        merged = formats.merge_paired_columns(np.array(c["paired_post"]).reshape(400, -1),
+                                              np.array(c["singles_post"]).reshape(20, -1), sp)
+        np.testing.assert_allclose(merged, np.array(c["merged"]).reshape(20, -1), rtol=1e-14, atol=0)

@@ -76,6 +76,25 @@ def test_request_parsing():
     assert type(m).__name__ == "IrrevDiagModel"   # random rate matrix: detailed balance fails
 
 
+
+def test_command_line_validate(tmp_path):
+    """``python -m subby_gb300 --validate``: exit 0 and "Valid." for a good
+    request, exit 1 and "Invalid: <reason>" for a bad one (subby/__main__.py)."""
+    import subprocess
+    import sys
+    good = tmp_path / "good.json"
+    good.write_text(json.dumps(G["requests"][0]["request"]))
+    bad = tmp_path / "bad.json"
+    bad.write_text(json.dumps(dict(G["requests"][0]["request"], model={"name": "wag"})))
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    r = subprocess.run([sys.executable, "-m", "subby_gb300", str(good), "--validate"], capture_output=True,
+                       text=True, cwd=root)
+    assert r.returncode == 0 and r.stderr.strip() == "Valid."
+    r = subprocess.run([sys.executable, "-m", "subby_gb300", "--validate"], input=bad.read_text(),
+                       capture_output=True, text=True, cwd=root)
+    assert r.returncode == 1 and r.stderr.strip() == "Invalid: Unknown model name: wag"
+
+
 T = G["transforms"]
 
 

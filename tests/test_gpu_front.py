@@ -68,6 +68,25 @@ def test_requests_match_reference_io(case):
         assert_cols(np.array(got["rootProb"]), np.array(ref["rootProb"]), ROOTPROB_RTOL, "rootProb")
 
 
+def test_command_line_runs_a_request(tmp_path):
+    """``python -m subby_gb300 request.json -o out.json`` (subby/__main__.py)
+    writes the reference io.run result, within the usual tolerances."""
+    import subprocess
+    import sys
+    case = G["requests"][0]
+    req = tmp_path / "req.json"
+    req.write_text(json.dumps(case["request"]))
+    out = tmp_path / "out.json"
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    subprocess.run([sys.executable, "-m", "subby_gb300", str(req), "-o", str(out), "--indent", "1"], check=True,
+                   cwd=root)
+    got, ref = json.loads(out.read_text()), case["result"]
+    assert set(got) == set(ref)
+    assert_loglike(np.array(got["logLike"]), np.array(ref["logLike"]))
+    assert_cols(np.array(got["counts"]), np.array(ref["counts"]), COUNTS_RTOL, "counts")
+    assert_cols(np.array(got["rootProb"]), np.array(ref["rootProb"]), ROOTPROB_RTOL, "rootProb")
+
+
 def test_maf_batch_pipeline(tmp_path):
     """The command line of the MAF batch pipeline on the GPU: manifest,
     per-block files and diagnostics as the reference script wrote them;

@@ -26,6 +26,7 @@ import numpy as np
 
 from . import _lib, batch
 from .models import ensure_diag
+from .padding import strip_dummy_leaves
 from .types import IrrevDiagModel, Tree
 
 _PLAN_CACHE_SIZE = 32
@@ -474,6 +475,16 @@ def _grid(alignment, tree, grid, fn, out_shape):
     return out
 
 
+def _unpad(alignment, tree, model, k):
+    """subby.jax's padded trees (dummy leaves under the root) for LogLike
+    and RootProb: the trailing dummy leaves are dropped (each contributes a
+    factor 1), so the kernels see the binary tree."""
+    if k == 'grid':
+        return alignment, tree
+    m0 = model[0] if k == 'list' else model
+    return strip_dummy_leaves(alignment, tree, lambda: int(np.asarray(ensure_diag(m0).pi).shape[-1]))
+
+
 def _slice_mask(branch_mask, idx):
     if idx is None or branch_mask is None or isinstance(branch_mask, str):
         return branch_mask
@@ -485,6 +496,7 @@ def LogLike(alignment, tree: Tree, model, maxChunkSize: int = 128):
     batched model gives (*H, C); a list of C models one model per column."""
     del maxChunkSize  # columns are tiled on the device
     k = batch.kind(model)
+    alignment, tree = _unpad(alignment, tree, model, k)
     if k == 'grid':
         return _grid(alignment, tree, model, lambda p, a, idx: p.run(a, loglike=True)['logLike'],
                      (int(alignment.shape[1]),))
@@ -542,6 +554,7 @@ def RootProb(alignment, tree: Tree, model, maxChunkSize: int = 128):
     """(A, C) posterior root distribution; subby/jax/__init__.py:543."""
     del maxChunkSize
     k = batch.kind(model)
+    alignment, tree = _unpad(alignment, tree, model, k)
     if k == 'grid':
         A = len(ensure_diag(model[0][0]).pi)
         return _grid(alignment, tree, model, lambda p, a, idx: p.run(a, loglike=False, rootprob=True)['rootProb'],

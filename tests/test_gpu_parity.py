@@ -319,3 +319,30 @@ def test_zero_columns(A):
     ll, dldt, dldS = plan.grad(empty)
     assert ll.shape == (0,) and dldt.shape == (R,) and not dldt.any() and not dldS.any()
     plan.close()
+
+
+def test_padded_tree_and_alignment_are_neutral():
+    """subby.jax's padding workflow (pad_tree_and_alignment, then LogLike /
+    RootProb / MixturePosterior on the padded inputs, then unpad_columns):
+    the real columns equal the unpadded results and the gap columns have
+    logLike 0, as in the reference's padding tests."""
+    rng = np.random.default_rng(12)
+    m = models.hky85_diag(2.0, [0.3, 0.2, 0.25, 0.25])
+    m2 = models.hky85_diag(4.0, [0.25, 0.25, 0.25, 0.25])
+    tree = synth.random_tree(40, 0.1, rng)
+    aln = synth.simulated_alignment(tree, m, 300, 0.1, rng)
+    ptree, paln, R, C = sg.pad_tree_and_alignment(tree, aln)
+    assert len(ptree.parentIndex) > R and paln.shape[1] > C
+    ll = sg.LogLike(paln, ptree, m)
+    assert_loglike(sg.unpad_columns(ll, C), sg.LogLike(aln, tree, m))
+    assert np.abs(ll[C:]).max() <= 1e-5
+    assert_cols(sg.unpad_columns(sg.RootProb(paln, ptree, m), C), sg.RootProb(aln, tree, m), ROOTPROB_RTOL,
+                "RootProb")
+    lw = np.log([0.3, 0.7])
+    assert_cols(sg.unpad_columns(sg.MixturePosterior(paln, ptree, [m, m2], lw), C),
+                sg.MixturePosterior(aln, tree, [m, m2], lw), 1e-5, "MixturePosterior")
+    dev = sg.LogLike(torch.as_tensor(paln).cuda(), ptree, m)
+    torch.cuda.synchronize()
+    np.testing.assert_array_equal(dev.cpu().numpy(), ll)
+    with pytest.raises(_lib.TreeError):          # Counts keeps the reference's binary-tree rule
+        sg.Counts(paln, ptree, m)

@@ -1,0 +1,69 @@
+"""Generate tests/golden/models.npz from the REFERENCE model constructors.
+
+    python tests/golden/make_models_golden.py [--reference /root/reference]
+
+Runs subby/oracle/oracle.py's hky85_diag, jukes_cantor_model, f81_model,
+diagonalize_rate_matrix, diagonalize_irreversible, check_detailed_balance
+and model_from_rate_matrix on seeded inputs and stores their outputs
+(eigenvalues, eigenvectors, eigenvectors_inv, pi) and the inputs.
+"""
+from __future__ import annotations
+
+import argparse
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--reference", default="/root/reference")
+    args = ap.parse_args()
+    sys.path.insert(0, args.reference)
+    from subby.oracle import oracle as ro   # noqa: E402  (reference)
+    rng = np.random.default_rng(404)
+    out = {}
+
+    def put(name, m, **inputs):
+        for k in ("eigenvalues", "eigenvectors", "eigenvectors_inv", "pi"):
+            if k in m:
+                out[f"{name}/{k}"] = np.asarray(m[k])
+        for k, v in inputs.items():
+            out[f"{name}/in_{k}"] = np.asarray(v)
+
+    for i, (kappa, pi) in enumerate([(2.0, [0.25] * 4), (4.0, [0.295, 0.205, 0.205, 0.295]),
+                                     (0.7, rng.dirichlet(np.ones(4)))]):
+        put(f"hky{i}", ro.hky85_diag(kappa, np.asarray(pi)), kappa=kappa, pi=pi)
+    for A in (2, 4, 20, 64):
+        put(f"jc{A}", ro.jukes_cantor_model(A), A=A)
+    for A in (4, 20):
+        pi = rng.dirichlet(np.ones(A))
+        put(f"f81_{A}", ro.f81_model(pi), pi=pi)
+    for A in (4, 20):
+        pi = rng.dirichlet(2 * np.ones(A))
+        S = rng.lognormal(size=(A, A))
+        S = S + S.T
+        Q = S * pi[None, :]
+        np.fill_diagonal(Q, 0.0)
+        np.fill_diagonal(Q, -Q.sum(1))
+        put(f"rev{A}", ro.diagonalize_rate_matrix(Q, pi), Q=Q, pi=pi)
+        put(f"auto_rev{A}", ro.model_from_rate_matrix(Q, pi), Q=Q, pi=pi)
+        N = rng.uniform(0.1, 1.0, size=(A, A))
+        np.fill_diagonal(N, 0.0)
+        np.fill_diagonal(N, -N.sum(1))
+        w, v = np.linalg.eig(N.T)
+        st = np.real(v[:, np.argmin(np.abs(w))])
+        st = st / st.sum()
+        put(f"irrev{A}", ro.diagonalize_irreversible(N, st), Q=N, pi=st)
+        put(f"auto_irrev{A}", ro.model_from_rate_matrix(N, st), Q=N, pi=st)
+        out[f"balance/rev{A}"] = np.asarray(ro.check_detailed_balance(Q, pi))
+        out[f"balance/irrev{A}"] = np.asarray(ro.check_detailed_balance(N, st))
+    np.savez_compressed(os.path.join(HERE, "models.npz"), **out)
+    print(f"wrote models.npz ({len(out)} arrays)")
+
+
+if __name__ == "__main__":
+    main()

@@ -1,4 +1,4 @@
-"""Generate tests/golden/models.npz from the REFERENCE model constructors.
+"""Generate tests/golden/models/constructors.npz from the REFERENCE model constructors.
 
     python tests/golden/make_models_golden.py [--reference /root/reference]
 
@@ -61,8 +61,9 @@ def main():
         put(f"auto_irrev{A}", ro.model_from_rate_matrix(N, st), Q=N, pi=st)
         out[f"balance/rev{A}"] = np.asarray(ro.check_detailed_balance(Q, pi))
         out[f"balance/irrev{A}"] = np.asarray(ro.check_detailed_balance(N, st))
-    np.savez_compressed(os.path.join(HERE, "models.npz"), **out)
-    print(f"wrote models.npz ({len(out)} arrays)")
+    os.makedirs(os.path.join(HERE, "models"), exist_ok=True)
+    np.savez_compressed(os.path.join(HERE, "models", "constructors.npz"), **out)
+    print(f"wrote models/constructors.npz ({len(out)} arrays)")
 
 
 if __name__ == "__main__":

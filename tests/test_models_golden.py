@@ -11,7 +11,7 @@ import pytest
 from subby_gb300 import models
 from subby_gb300.types import DiagModel, IrrevDiagModel
 
-Z = np.load(__file__.replace("test_models_golden.py", "golden/models.npz"))
+Z = np.load(__file__.replace("test_models_golden.py", "golden/models/constructors.npz"))
 T = (0.05, 0.3, 2.0)
 
 

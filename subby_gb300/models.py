@@ -292,3 +292,37 @@ def model_from_rate_matrix(subRate, pi, reversible=None, tol: float = 1e-10):
     if reversible is None:
         reversible = check_detailed_balance(subRate, pi, tol)
     return diagonalize_rate_matrix(subRate, pi) if reversible else diagonalize_irreversible(subRate, pi)
+
+
+def gy94_rate_matrix(omega: float, kappa: float, pi=None) -> np.ndarray:
+    """Goldman-Yang 1994 rate matrix over the 61 sense codons (ACGT
+    lexicographic order, stops removed): Q_ij = pi_j kappa^[transition]
+    omega^[non-synonymous] for codons one nucleotide apart, 0 otherwise;
+    rows sum to 0, scaled so that -sum_i pi_i Q_ii = 1
+    (subby/oracle/oracle.py:388-471, subby/jax/models.py:189-232)."""
+    from .formats import genetic_code
+    gc = genetic_code()
+    sense = [gc["codons"][i] for i in gc["sense_indices"]]
+    aa = np.array(gc["sense_amino_acids"])
+    A = len(sense)
+    p = np.full(A, 1.0 / A) if pi is None else np.asarray(pi, dtype=np.float64)
+    nuc = np.array([[c[k] for k in range(3)] for c in sense])            # (61, 3) letters
+    differs = nuc[:, None, :] != nuc[None, :, :]                        # (61, 61, 3)
+    one = differs.sum(axis=2) == 1
+    pos = np.argmax(differs, axis=2)
+    a = np.take_along_axis(nuc[:, None, :].repeat(A, 1), pos[..., None], 2)[..., 0]
+    b = np.take_along_axis(nuc[None, :, :].repeat(A, 0), pos[..., None], 2)[..., 0]
+    purine = np.isin(a, ["A", "G"]) == np.isin(b, ["A", "G"])          # A<->G or C<->T
+    Q = np.where(one, p[None, :], 0.0)
+    Q = Q * np.where(one & purine, kappa, 1.0) * np.where(one & (aa[:, None] != aa[None, :]), omega, 1.0)
+    np.fill_diagonal(Q, 0.0)
+    np.fill_diagonal(Q, -Q.sum(axis=1))
+    return Q / -np.sum(p * np.diag(Q))
+
+
+def gy94_model(omega: float, kappa: float, pi=None) -> DiagModel:
+    """The GY94 codon model (61 states) as a DiagModel (reversible: pi_i Q_ij
+    = pi_j Q_ji).  The kernels take A up to 64 in sizes 2..8, 16, 20, 32, 64:
+    61 states run through ``subby_gb300.embed.EmbeddedPlan``."""
+    p = np.full(61, 1.0 / 61) if pi is None else np.asarray(pi, dtype=np.float64)
+    return diagonalize_rate_matrix(gy94_rate_matrix(omega, kappa, p), p)

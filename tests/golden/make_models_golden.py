@@ -3,8 +3,8 @@
     python tests/golden/make_models_golden.py [--reference /root/reference]
 
 Runs subby/oracle/oracle.py's hky85_diag, jukes_cantor_model, f81_model,
-diagonalize_rate_matrix, diagonalize_irreversible, check_detailed_balance
-and model_from_rate_matrix on seeded inputs and stores their outputs
+diagonalize_rate_matrix, diagonalize_irreversible, check_detailed_balance,
+model_from_rate_matrix and gy94_model on seeded inputs and stores their outputs
 (eigenvalues, eigenvectors, eigenvectors_inv, pi) and the inputs.
 """
 from __future__ import annotations
@@ -62,6 +62,9 @@ def main():
         out[f"balance/rev{A}"] = np.asarray(ro.check_detailed_balance(Q, pi))
         out[f"balance/irrev{A}"] = np.asarray(ro.check_detailed_balance(N, st))
     os.makedirs(os.path.join(HERE, "models"), exist_ok=True)
+    for i, (omega, kappa, pi) in enumerate([(0.3, 2.0, None), (1.7, 0.5, rng.dirichlet(np.ones(61)))]):
+        put(f"gy94_{i}", ro.gy94_model(omega, kappa, pi), omega=omega, kappa=kappa,
+            pi=np.full(61, 1.0 / 61) if pi is None else pi)
     np.savez_compressed(os.path.join(HERE, "models", "constructors.npz"), **out)
     print(f"wrote models/constructors.npz ({len(out)} arrays)")
 

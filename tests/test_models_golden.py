@@ -74,3 +74,14 @@ def test_f81_and_rate_matrices(A):
     for kind in ("rev", "irrev"):
         q = _ref(f"{kind}{A}")
         assert models.check_detailed_balance(q["in_Q"], q["in_pi"]) == bool(Z[f"balance/{kind}{A}"])
+
+
+@pytest.mark.parametrize("i", [0, 1])
+def test_gy94(i):
+    r = _ref(f"gy94_{i}")
+    pi = r["in_pi"]
+    m = models.gy94_model(float(r["in_omega"]), float(r["in_kappa"]), None if i == 0 else pi)
+    _check_reversible(m, r)
+    Q = models.gy94_rate_matrix(float(r["in_omega"]), float(r["in_kappa"]), pi)
+    np.testing.assert_allclose(pi[:, None] * Q, (pi[:, None] * Q).T, atol=1e-15)   # detailed balance
+    assert np.count_nonzero(Q[0]) == 1 + 8            # AAA: 9 one-nucleotide neighbours, TAA a stop

@@ -28,8 +28,11 @@ exact in FP64 (tests/test_embed_host.py runs it through the oracle), but on a
 GB300 a 61-state random reversible model (pi ~ Dirichlet(1), uniformly
 random tokens on every node) embedded in the A = 64 tensor-core path gave
 LogLike within 1e-5 and Counts with a column-wise error of 1.13e-4, above the
-1e-4 bar; whether the embedding or that input's FP32 conditioning causes it
-is not yet separated.
+1e-4 bar.  In an FP32 restatement on the CPU the embedded and the direct
+61-state computations agree to summation order and both carry ~1e-4 error
+against FP64 on that input class (as does a plain 64-state model with
+random tokens), so the deviation is the input's FP32 conditioning; the
+posterior and irreversible paths of the embedding have not run on a GPU.
 """
 from __future__ import annotations
 

@@ -76,3 +76,62 @@ def test_embedded_plan_equals_the_model_itself(A, irrev):
     assert r2['counts'] is out['counts'] and np.allclose(out['counts'], r2['counts'])
     with pytest.raises(NotImplementedError):
         p.run(aln, counts=True, f81=True)
+
+
+def _counts_fp32(aln, tree, md):
+    """The eigenbasis Counts algorithm (unmasked) with every array in FP32,
+    the arithmetic of the FP32 kernels; back-transform in FP64."""
+    f = np.float32
+    mu, pi = np.asarray(md['eigenvalues'], np.float64), np.asarray(md['pi'], np.float64)
+    M = oracle.compute_sub_matrices(md, tree.distanceToParent).astype(f)
+    J = oracle.compute_J(mu, tree.distanceToParent).astype(f)
+    R, C = aln.shape
+    A = len(pi)
+    L = oracle.token_to_likelihood(aln, A).astype(f)
+    par = tree.parentIndex
+    sib = oracle.children_of(par)[2]
+    U, lnU = L.copy(), np.zeros((R, C), f)
+    for n in range(R - 1, 0, -1):
+        p = par[n]
+        U[p] *= U[n] @ M[n].T
+        mx = np.maximum(U[p].max(-1), f(1e-30))
+        U[p] /= mx[:, None]
+        lnU[p] += lnU[n] + np.log(mx)
+    lnL = lnU[0] + np.log(U[0] @ pi.astype(f))
+    D, lnD = np.zeros((R, C, A), f), np.zeros((R, C), f)
+    for n in range(1, R):
+        p, s = par[n], sib[n]
+        pv = np.broadcast_to(pi.astype(f), (C, A)) if p == 0 else D[p] @ M[p]
+        raw = (U[s] @ M[s].T) * pv * L[p]
+        mx = np.maximum(raw.max(-1), f(1e-30))
+        D[n] = raw / mx[:, None]
+        lnD[n] = lnU[s] + (lnD[p] if p else 0) + np.log(mx)
+    sp, V = np.sqrt(pi).astype(f), np.asarray(md['eigenvectors']).astype(f)
+    Ut, Dt = (U * sp) @ V, (D / sp) @ V
+    Cm = np.zeros((A, A, C), f)
+    for n in range(1, R):
+        Cm += np.einsum('ck,kl,cl,c->klc', Dt[n], J[n], Ut[n], np.exp(lnD[n] + lnU[n] - lnL))
+    return oracle.back_transform(Cm.astype(np.float64), md)
+
+
+def test_embedding_changes_nothing_in_fp32_arithmetic():
+    """In FP32 arithmetic the embedded model's real-state counts equal the
+    A-state model's up to summation order (the extra states meet the real
+    ones only through exact zeros of the block-diagonal eigenvectors), so the
+    GPU error of an embedded model is that of the A-state input itself.  The
+    same input class is FP32-hard without embedding too: a random 61-state
+    model (pi ~ Dirichlet(1)) with uniformly random tokens carries ~1e-4
+    column-wise FP32 error against FP64 either way."""
+    rng = np.random.default_rng(561)
+    m = models.random_reversible(61, rng)[0]
+    tree = synth.random_tree(5, 0.15, rng)
+    t = oracle.Tree(tree.parentIndex, tree.distanceToParent)
+    aln = rng.integers(-1, 64, size=(len(tree.parentIndex), 12)).astype(np.int32)
+    direct = _counts_fp32(aln, t, m._asdict())
+    emb = _counts_fp32(embed.embed_tokens(aln, 61, 64), t, embed.embed_model(m, 64)._asdict())[:61, :61]
+    np.testing.assert_allclose(emb, direct, rtol=1e-5, atol=1e-9)
+    ref = oracle.Counts(aln, t, m._asdict(), branch_mask=None)
+    scale = np.maximum(np.abs(ref).max(axis=(0, 1)), 1e-3)
+    e_direct = (np.abs(direct - ref).max(axis=(0, 1)) / scale).max()
+    e_emb = (np.abs(emb - ref).max(axis=(0, 1)) / scale).max()
+    assert e_emb <= 1.01 * e_direct + 1e-7

@@ -10,13 +10,14 @@ from .models import (hky85_diag, jukes_cantor_model, f81_model, diagonalize_rate
 from .api import (LogLike, Counts, BranchCounts, RootProb, MixturePosterior, LogLikeCustomGrad, InsideOutside, Plan,
                   get_plan, clear_plan_cache)
 from .padding import GEOM_BINS, pad_to_geom_bin, pad_alignment, pad_tree, pad_tree_and_alignment, unpad_columns
+from .ctmc import ExpectedCounts
 from . import _lib, formats, io, maf_batch
 
 __all__ = ["BranchCounts", "Tree", "DiagModel", "IrrevDiagModel", "RateModel", "irrev_model_from_rate_matrix",
            "diagonalize_irreversible", "gamma_rate_categories", "scale_model", "gy94_model", "MixturePosterior", "hky85_diag", "jukes_cantor_model", "f81_model",
            "diagonalize_rate_matrix", "reversible_rate_matrix", "random_reversible", "LogLike",
            "Counts", "RootProb", "LogLikeCustomGrad", "InsideOutside", "Plan", "get_plan", "clear_plan_cache",
-           "GEOM_BINS", "pad_to_geom_bin", "pad_alignment", "pad_tree", "pad_tree_and_alignment", "unpad_columns"]
+           "ExpectedCounts", "GEOM_BINS", "pad_to_geom_bin", "pad_alignment", "pad_tree", "pad_tree_and_alignment", "unpad_columns"]
 
 __version__ = "0.1.0"
 

@@ -5,7 +5,8 @@
 Runs subby/oracle/oracle.py's hky85_diag, jukes_cantor_model, f81_model,
 diagonalize_rate_matrix, diagonalize_irreversible, check_detailed_balance,
 model_from_rate_matrix and gy94_model on seeded inputs and stores their outputs
-(eigenvalues, eigenvectors, eigenvectors_inv, pi) and the inputs.
+(eigenvalues, eigenvectors, eigenvectors_inv, pi) and the inputs; and
+ExpectedCounts on a few models (models/expected_counts.npz).
 """
 from __future__ import annotations
 
@@ -58,6 +59,8 @@ def main():
         st = np.real(v[:, np.argmin(np.abs(w))])
         st = st / st.sum()
         put(f"irrev{A}", ro.diagonalize_irreversible(N, st), Q=N, pi=st)
+        if A == 4:
+            irrev4 = ro.diagonalize_irreversible(N, st)
         put(f"auto_irrev{A}", ro.model_from_rate_matrix(N, st), Q=N, pi=st)
         out[f"balance/rev{A}"] = np.asarray(ro.check_detailed_balance(Q, pi))
         out[f"balance/irrev{A}"] = np.asarray(ro.check_detailed_balance(N, st))
@@ -67,6 +70,30 @@ def main():
             pi=np.full(61, 1.0 / 61) if pi is None else pi)
     np.savez_compressed(os.path.join(HERE, "models", "constructors.npz"), **out)
     print(f"wrote models/constructors.npz ({len(out)} arrays)")
+
+    # ExpectedCounts (single-branch CTMC integrals), oracle.py:1909-2105
+    ec = {}
+    pi6 = rng.dirichlet(np.ones(6))
+    S6 = rng.lognormal(size=(6, 6))
+    Q6 = (S6 + S6.T) * pi6[None, :]
+    np.fill_diagonal(Q6, 0.0)
+    np.fill_diagonal(Q6, -Q6.sum(1))
+    N5 = rng.uniform(0.1, 1.0, size=(5, 5))
+    np.fill_diagonal(N5, 0.0)
+    np.fill_diagonal(N5, -N5.sum(1))
+    cases = [("hky", ro.hky85_diag(2.0, np.array([0.1, 0.2, 0.3, 0.4])), 0.3),
+             ("jc", ro.jukes_cantor_model(4), 1.0),
+             ("rev6", ro.diagonalize_rate_matrix(Q6, pi6), 0.7),
+             ("irrev4", irrev4, 0.5),
+             ("irrev5", ro.diagonalize_irreversible(N5, np.full(5, 0.2)), 0.2)]
+    for name, m, t in cases:
+        for k in ("eigenvalues", "eigenvectors", "eigenvectors_inv", "pi"):
+            if k in m:
+                ec[f"{name}/{k}"] = np.asarray(m[k])
+        ec[f"{name}/t"] = np.asarray(t)
+        ec[f"{name}/expected"] = ro.ExpectedCounts(m, t)
+    np.savez_compressed(os.path.join(HERE, "models", "expected_counts.npz"), **ec)
+    print(f"wrote models/expected_counts.npz ({len(ec)} arrays)")
 
 
 if __name__ == "__main__":

@@ -73,3 +73,16 @@ def ExpectedCounts(model, t: float) -> np.ndarray:
         return _one(m, t)
     _, ms = unbatch(m)
     return np.stack([_one(x, t) for x in ms]).reshape(tuple(H) + (len(np.asarray(ms[0].pi)),) * 4)
+
+
+def expected_counts_eigen(eigenvalues, eigenvectors, pi, t) -> np.ndarray:
+    """ExpectedCounts of a reversible eigensystem (subby/jax/ctmc.py:21-91)."""
+    del pi
+    return _reversible(np.asarray(eigenvalues, np.float64), np.asarray(eigenvectors, np.float64), float(t))
+
+
+def expected_counts_eigen_irrev(eigenvalues, eigenvectors, eigenvectors_inv, pi, t) -> np.ndarray:
+    """ExpectedCounts of an irreversible eigensystem (subby/jax/ctmc.py:94-158)."""
+    del pi
+    return _irreversible(np.asarray(eigenvalues, np.complex128), np.asarray(eigenvectors, np.complex128),
+                         np.asarray(eigenvectors_inv, np.complex128), float(t))

@@ -326,3 +326,67 @@ def gy94_model(omega: float, kappa: float, pi=None) -> DiagModel:
     61 states run through ``subby_gb300.embed.EmbeddedPlan``."""
     p = np.full(61, 1.0 / 61) if pi is None else np.asarray(pi, dtype=np.float64)
     return diagonalize_rate_matrix(gy94_rate_matrix(omega, kappa, p), p)
+
+
+def diagonalize_rate_matrix_auto(subRate, rootProb, reversible=None, tol: float = 1e-10):
+    """subby.jax's name for ``model_from_rate_matrix``
+    (subby/jax/diagonalize.py:89-111)."""
+    return model_from_rate_matrix(subRate, rootProb, reversible=reversible, tol=tol)
+
+
+# Host FP64 model preparation, as subby.jax exposes it (the plans compute the
+# same tables internally; these are for callers that want them).
+
+def compute_J(eigenvalues, distances) -> np.ndarray:
+    """(*H, R, A, A) J_kl(t_n) = (e^{mu_k t} - e^{mu_l t}) / (mu_k - mu_l), and
+    t e^{mu_k t} when |mu_k - mu_l| < 1e-8 (subby/jax/eigensub.py:7-50;
+    complex eigenvalues as compute_J_complex, :234-262)."""
+    mu = np.asarray(eigenvalues)
+    mu = mu.astype(np.complex128 if np.iscomplexobj(mu) else np.float64)
+    t = np.asarray(distances, dtype=np.float64)
+    E = np.exp(mu[..., None, :] * t[:, None])                                  # (*H, R, A)
+    diff = mu[..., :, None] - mu[..., None, :]                                 # (*H, A, A)
+    deg = (np.abs(diff) < 1e-8)[..., None, :, :]
+    dd = (E[..., :, None] - E[..., None, :]) / np.where(deg, 1.0, diff[..., None, :, :])
+    return np.where(deg, t[:, None, None] * E[..., :, None], dd)
+
+
+compute_J_complex = compute_J
+
+
+def compute_J_per_row(eigenvalues, distances) -> np.ndarray:
+    """(R, A, A) J with each branch's own eigenvalues (eigenvalues (R, A))
+    (subby/jax/eigensub.py:440-506)."""
+    mu = np.asarray(eigenvalues)
+    t = np.asarray(distances, dtype=np.float64)
+    return np.stack([compute_J(mu[n], t[n:n + 1])[0] for n in range(len(t))])
+
+
+compute_J_per_row_complex = compute_J_per_row
+
+
+def compute_sub_matrices(model, distances) -> np.ndarray:
+    """(*H, R, A, A) M_ij(t) = sqrt(pi_j / pi_i) sum_k V_ik e^{mu_k t} V_jk
+    (subby/jax/diagonalize.py:141-172); irreversible models as
+    compute_sub_matrices_irrev."""
+    m = ensure_diag(model)
+    if isinstance(m, IrrevDiagModel):
+        return compute_sub_matrices_irrev(m, distances)
+    V = np.asarray(m.eigenvectors, dtype=np.float64)
+    mu = np.asarray(m.eigenvalues, dtype=np.float64)
+    sp = np.sqrt(np.asarray(m.pi, dtype=np.float64))
+    t = np.asarray(distances, dtype=np.float64)
+    E = np.exp(mu[..., None, :] * t[:, None])                                  # (*H, R, A)
+    S = np.einsum('...ik,...rk,...jk->...rij', V, E, V)
+    return S / sp[..., None, :, None] * sp[..., None, None, :]
+
+
+def compute_sub_matrices_irrev(model, distances) -> np.ndarray:
+    """(*H, R, A, A) M(t) = Re(V e^{mu t} V^-1) (subby/jax/diagonalize.py:114-138)."""
+    m = ensure_diag(model)
+    V = np.asarray(m.eigenvectors, dtype=np.complex128)
+    Vi = np.asarray(m.eigenvectors_inv, dtype=np.complex128)
+    mu = np.asarray(m.eigenvalues, dtype=np.complex128)
+    t = np.asarray(distances, dtype=np.float64)
+    E = np.exp(mu[..., None, :] * t[:, None])
+    return np.einsum('...ik,...rk,...kj->...rij', V, E, Vi).real

@@ -17,7 +17,7 @@ They mirror subby's own NamedTuples so that code written against
 """
 from __future__ import annotations
 
-from typing import NamedTuple
+from typing import NamedTuple, Union
 
 import numpy as np
 
@@ -43,3 +43,7 @@ class IrrevDiagModel(NamedTuple):
 class RateModel(NamedTuple):
     subRate: np.ndarray
     rootProb: np.ndarray
+
+
+AnyDiagModel = Union[DiagModel, IrrevDiagModel]
+AnyModel = Union[DiagModel, IrrevDiagModel, RateModel]

@@ -57,3 +57,14 @@ def test_identities_irreversible_and_batches():
     assert E.shape == (2, 4, 4, 4, 4)
     for k, r in enumerate((0.5, 2.0)):
         np.testing.assert_allclose(E[k], ctmc.ExpectedCounts(models.scale_model(base, r), 0.3), rtol=1e-12)
+
+
+def test_eigensystem_entry_points():
+    rng = np.random.default_rng(2)
+    m = models.random_reversible(5, rng)[0]
+    np.testing.assert_array_equal(sg.expected_counts_eigen(m.eigenvalues, m.eigenvectors, m.pi, 0.3),
+                                  sg.ExpectedCounts(m, 0.3))
+    mi = models.random_irreversible(4, rng)
+    np.testing.assert_array_equal(
+        sg.expected_counts_eigen_irrev(mi.eigenvalues, mi.eigenvectors, mi.eigenvectors_inv, mi.pi, 0.3),
+        sg.ExpectedCounts(mi, 0.3))

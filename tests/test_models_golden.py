@@ -85,3 +85,35 @@ def test_gy94(i):
     Q = models.gy94_rate_matrix(float(r["in_omega"]), float(r["in_kappa"]), pi)
     np.testing.assert_allclose(pi[:, None] * Q, (pi[:, None] * Q).T, atol=1e-15)   # detailed balance
     assert np.count_nonzero(Q[0]) == 1 + 8            # AAA: 9 one-nucleotide neighbours, TAA a stop
+
+
+def test_model_preparation_helpers_match_the_oracle():
+    """compute_J / compute_sub_matrices (host FP64, subby.jax's names) vs the
+    oracle's restatement of the reference (pinned by the golden fixtures),
+    single and *H-batched, reversible and irreversible."""
+    import oracle
+    rng = np.random.default_rng(9)
+    m = models.random_reversible(6, rng)[0]
+    t = rng.uniform(0.0, 1.0, 7)
+    t[0] = 0.0
+    np.testing.assert_allclose(models.compute_J(m.eigenvalues, t), oracle.compute_J(m.eigenvalues, t), rtol=1e-13)
+    np.testing.assert_allclose(models.compute_sub_matrices(m, t), oracle.compute_sub_matrices(m._asdict(), t),
+                               rtol=1e-12, atol=1e-15)
+    mi = models.random_irreversible(5, rng)
+    np.testing.assert_allclose(models.compute_J_complex(mi.eigenvalues, t),
+                               oracle.compute_J_complex(mi.eigenvalues, t), rtol=1e-13)
+    np.testing.assert_allclose(models.compute_sub_matrices(mi, t),
+                               oracle.compute_sub_matrices_irrev(mi._asdict(), t), rtol=1e-12, atol=1e-14)
+    b = models.scale_model(m, np.array([0.5, 2.0]))
+    Jb, Mb = models.compute_J(b.eigenvalues, t), models.compute_sub_matrices(b, t)
+    assert Jb.shape == (2, 7, 6, 6) and Mb.shape == (2, 7, 6, 6)
+    for k, r in enumerate((0.5, 2.0)):
+        mk = models.scale_model(m, r)
+        np.testing.assert_allclose(Jb[k], models.compute_J(mk.eigenvalues, t), rtol=1e-14)
+        np.testing.assert_allclose(Mb[k], models.compute_sub_matrices(mk, t), rtol=1e-13, atol=1e-16)
+    rows = np.stack([m.eigenvalues, 2 * m.eigenvalues, m.eigenvalues])
+    Jr = models.compute_J_per_row(rows, t[:3])
+    for n in range(3):
+        np.testing.assert_allclose(Jr[n], models.compute_J(rows[n], t[n:n + 1])[0], rtol=1e-15)
+    assert models.diagonalize_rate_matrix_auto(models.reversible_rate_matrix(rng.normal(size=15), m.pi), m.pi) \
+        ._fields == ("eigenvalues", "eigenvectors", "pi")

@@ -1,7 +1,10 @@
 """subby_gb300 — GB300-native (sm_103a) backend for subby's eigensubstitution
 hot path: Felsenstein inside pass, outside pass, eigenbasis J(t) count
 accumulation (general and F81/JC fast path), per-column LogLike, Counts and
-root posteriors.  Drop-in for the single-model entry points of ``subby.jax``.
+root posteriors, per-branch counts, node and branch posteriors, distance
+gradients, irreversible and batched models.  Drop-in for ``subby.jax``'s
+entry points (same names, arguments and output layouts), with subby's
+front-end (``formats``, ``io``, the command line, ``maf_batch``) on top.
 """
 from .types import Tree, DiagModel, IrrevDiagModel, RateModel, AnyDiagModel, AnyModel
 from .models import (hky85_diag, jukes_cantor_model, f81_model, diagonalize_rate_matrix,

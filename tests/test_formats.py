@@ -151,3 +151,23 @@ def test_split_and_merge_paired_columns():
         merged = formats.merge_paired_columns(np.array(c["paired_post"]).reshape(400, -1),
                                               np.array(c["singles_post"]).reshape(20, -1), sp)
         np.testing.assert_allclose(merged, np.array(c["merged"]).reshape(20, -1), rtol=1e-14, atol=0)
+
+
+def test_request_field_parsing():
+    """The request fields as the reference's tests/test_cli.py checks them:
+    integer and character alignments, '-' -> A + 1, the missing-alphabet and
+    model-spec errors."""
+    acgt = ["A", "C", "G", "T"]
+    a = io._parse_alignment([[0, 1], [2, 3]], None)
+    assert a.dtype == np.int32 and a.shape == (2, 2)
+    assert io._parse_alignment(["AC", "GT"], acgt).tolist() == [[0, 1], [2, 3]]
+    assert io._parse_alignment(["A-", "GT"], acgt)[0, 1] == 5
+    assert io._parse_alignment([["A", "C"], ["G", "T"]], acgt).tolist() == [[0, 1], [2, 3]]
+    with pytest.raises(ValueError, match="Alphabet required"):
+        io._parse_alignment(["AC", "GT"], None)
+    with pytest.raises(ValueError, match="Unknown model"):
+        io._parse_model({"name": "bogus", "alphabetSize": 4})
+    with pytest.raises(ValueError, match="must have"):
+        io._parse_model({"alphabet": ["A", "C"]})
+    m, alpha = io._parse_model({"name": "hky85", "kappa": 2.0, "pi": [0.3, 0.2, 0.2, 0.3]})
+    assert alpha is None and np.allclose(m.pi, [0.3, 0.2, 0.2, 0.3])

@@ -1,19 +1,23 @@
-"""Drop-in replacement for the single-model entry points of ``subby.jax``.
+"""Drop-in replacement for the entry points of ``subby.jax``.
 
-``LogLike``, ``Counts``, ``RootProb`` and ``LogLikeCustomGrad`` take the same
-arguments as subby/jax/__init__.py:207, :338, :543 and :294 and return the
-same shapes (column last).  They run on the GPU through the C ABI of
+``LogLike``, ``Counts``, ``BranchCounts``, ``RootProb``, ``MixturePosterior``,
+``LogLikeCustomGrad`` and ``InsideOutside`` take the same arguments as
+subby/jax/__init__.py:207, :338, :450, :543, :653, :294 and :681 and return
+the same shapes (column last).  They run on the GPU through the C ABI of
 ``libsubby_gb300.so``; there is no CPU fallback.
 
 Inputs may be numpy arrays (results come back as numpy float32, copies in
 and out are part of the call) or CUDA ``torch`` tensors (results stay on the
 device as torch tensors, work is enqueued on the current torch stream).
 
-Irreversible models (``IrrevDiagModel``, complex eigensystem) are accepted
-by every entry point except the F81 fast path (reversible-only in the
-reference too) and the gradient.  Not supported (raise
-``NotImplementedError``): per-column model lists and model grids
-(subby/jax/__init__.py:53-205) and ``*H`` batch dimensions.
+Models: ``DiagModel``, ``RateModel`` (diagonalised on the host),
+``IrrevDiagModel`` (complex eigensystem; every entry point but the F81 fast
+path, which is reversible-only in the reference too), ``*H`` batches,
+per-column model lists and per-branch model grids
+(subby/jax/__init__.py:53-205; ``subby_gb300/batch.py``).  Not supported
+(``NotImplementedError``): InsideOutside over model grids (as in the
+reference) and over per-column lists whose pi differ, per-branch
+irreversible models.
 """
 from __future__ import annotations
 

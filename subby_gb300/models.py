@@ -20,6 +20,12 @@ subby/oracle/oracle.py:265-301: numpy ``eig`` and ``inv`` in complex128) and
 Rate heterogeneity: ``gamma_rate_categories`` (Yang 1994 quantile medians,
 subby/jax/models.py:126-158) and ``scale_model`` (subby/jax/models.py:
 160-186; a (K,) multiplier adds a leading batch dimension).
+
+Codons: ``gy94_model`` / ``gy94_rate_matrix`` (subby/jax/models.py:189-232).
+Reversibility: ``check_detailed_balance``, ``model_from_rate_matrix`` /
+``diagonalize_rate_matrix_auto``.  Model preparation under subby.jax's
+names: ``compute_J`` (and the complex / per-row variants) and
+``compute_sub_matrices`` (and the irreversible variant).
 """
 from __future__ import annotations
 

@@ -169,6 +169,18 @@ int subby_mixture_posterior(const float *logL, const double *log_weights, int K,
  */
 int subby_tokenize(const uint8_t *chars, int64_t n, const int32_t *lut, int32_t *out, int64_t *first_bad,
                    void *stream);
+/*
+ * Gather token rows into a contiguous (R, C) int32 device array on
+ * `stream`: dst[r*C + c] = src[map(r)*pitch + c] with map(r) = rowmap[r]
+ * (a device array of R row indices) or r when rowmap is NULL.  src may be
+ * pinned host memory (the SMs read it over the host link) or device memory;
+ * pitch >= C is its row length in elements; R <= 65535.  The serving loop
+ * uploads each job's alignment with it from a window of a larger host
+ * buffer.  No reference counterpart (the reference builds its inputs on the
+ * host).
+ */
+int subby_gather_rows(const int32_t *src, int64_t pitch, const int32_t *rowmap, int R, int C,
+                      int32_t *dst, void *stream);
 /* Wait for the plan's enqueued work and report SUBBY_ERR_TIMEOUT if a
  * bounded device wait (tensor-core kernels) gave up since the last check
  * (device-pointer runs return before their kernels finish, so they report
@@ -240,10 +252,15 @@ int subby_rootprob(const int32_t *alignment, const int32_t *parent_index,
  * Limits: A = 4, R <= 1023 nodes, and the tree program must fit the A = 4
  * kernel's on-chip budget; larger inputs return SUBBY_ERR_UNSUPPORTED.
  * The first call on a device resolves the array's device address with that
- * device current; make that first call before any stream capture.  Each call
- * rewrites every table it uses, so nothing needs clearing between calls, but
- * calls that overlap on the GPU share the array and race.  Work is enqueued
- * on `stream`.  No counterpart in the reference.
+ * device current and loads the kernels; make that first call before any
+ * stream capture.  A call with C = 0 validates its arguments and does only
+ * this set-up: it is the warm-up step.  The tables are uploaded from a host
+ * staging buffer that the next call rewrites, so a call on a stream that is
+ * capturing returns SUBBY_ERR_UNSUPPORTED.  Each call rewrites every table it
+ * uses, so nothing needs clearing between calls, but calls that overlap on
+ * the GPU share the array and race.  A rejection's reason is a fixed string
+ * returned by subby_last_error().  Work is enqueued on `stream`.  No
+ * counterpart in the reference.
  */
 int subby_counts_noalloc(const int32_t *alignment, const int32_t *parent_index,
                          const double *distances, const double *eigenvalues,
@@ -262,6 +279,16 @@ int subby_counts_noalloc(const int32_t *alignment, const int32_t *parent_index,
  * CUDA-core back-transform, 6 (A = 64) CUDA-core walk with the tensor-core
  * back-transform.  No reference counterpart. */
 int subby_debug_set_kernel(int which);
+
+/* Test hook of the bounded-wait failure path: with polls > 0, every
+ * tensor-core tree walk (A = 64) launched afterwards first waits on an
+ * mbarrier that nothing arms, while no copy or MMA is in flight, gives up
+ * after `polls` polls, frees its tensor memory and skips its work, so that
+ * subby_plan_status (device pointers) or the call itself (host pointers)
+ * reports SUBBY_ERR_TIMEOUT and the outputs are left unwritten.  0 (the
+ * default) turns it off; polls must be 0..4096.  No reference
+ * counterpart. */
+int subby_debug_fail_waits(int polls);
 
 /* Number of kernel launches the most recent subby_plan_run /
  * subby_plan_grad on this thread enqueued (for launch accounting). */

@@ -680,27 +680,37 @@ def reversible_rate_matrix(log_exch, pi):
     return Q
 
 
-def loglike_fd_grad(alignment, tree, log_exch, pi, h=1e-4, wrt="distances"):
-    """Central finite differences (FP64) of sum_c logL_c, for adjoint checks."""
-    def total(dist, le):
-        model = diagonalize_rate_matrix(reversible_rate_matrix(le, pi), pi)
-        return float(np.sum(LogLike(alignment, Tree(tree.parentIndex, dist), model)))
+def _fd_total(args):
+    """sum_c logL_c of the reversible model (log_exch, pi) on (parent, dist)."""
+    alignment, parent, dist, le, pi = args
+    model = diagonalize_rate_matrix(reversible_rate_matrix(le, pi), pi)
+    return float(np.sum(LogLike(alignment, Tree(parent, dist), model)))
+
+
+def loglike_fd_grad(alignment, tree, log_exch, pi, h=1e-4, wrt="distances", idx=None, pool=None):
+    """Central finite differences (FP64) of sum_c logL_c, for adjoint checks.
+
+    ``idx``: the components to difference (default all; the others stay 0);
+    ``pool``: a multiprocessing pool (spawn context) that evaluates the
+    perturbed likelihoods in parallel.
+    """
     dist = np.array(tree.distanceToParent, dtype=np.float64)
     le = np.array(log_exch, dtype=np.float64)
-    if wrt == "distances":
-        g = np.zeros(len(dist))
-        for n in range(1, len(dist)):
-            dp, dm = dist.copy(), dist.copy()
-            dp[n] += h
-            dm[n] -= h
-            g[n] = (total(dp, le) - total(dm, le)) / (2 * h)
-        return g
-    g = np.zeros(len(le))
-    for i in range(len(le)):
-        lp, lm = le.copy(), le.copy()
-        lp[i] += h
-        lm[i] -= h
-        g[i] = (total(dist, lp) - total(dist, lm)) / (2 * h)
+    parent = np.asarray(tree.parentIndex)
+    base = dist if wrt == "distances" else le
+    if idx is None:
+        idx = range(1, len(dist)) if wrt == "distances" else range(len(le))
+    idx = list(idx)
+    work = []
+    for i in idx:
+        for sgn in (1.0, -1.0):
+            x = base.copy()
+            x[i] += sgn * h
+            work.append((alignment, parent, x, le, pi) if wrt == "distances" else (alignment, parent, dist, x, pi))
+    vals = pool.map(_fd_total, work) if pool is not None else list(map(_fd_total, work))
+    g = np.zeros(len(base))
+    for j, i in enumerate(idx):
+        g[i] = (vals[2 * j] - vals[2 * j + 1]) / (2 * h)
     return g
 
 

@@ -23,7 +23,8 @@ EXPORTS = (
     "subby_plan_destroy", "subby_plan_device_bytes", "subby_plan_trim", "subby_plan_branch_counts",
     "subby_plan_posteriors", "subby_plan_status", "subby_plan_run", "subby_plan_grad",
     "subby_loglike", "subby_counts", "subby_rootprob", "subby_last_launch_count",
-    "subby_debug_set_kernel", "subby_counts_noalloc", "subby_mixture_posterior", "subby_tokenize",
+    "subby_debug_set_kernel", "subby_debug_fail_waits", "subby_counts_noalloc", "subby_mixture_posterior",
+    "subby_tokenize", "subby_gather_rows",
 )
 
 _lock = threading.Lock()
@@ -55,6 +56,8 @@ def _declare(lib):
     lib.subby_last_launch_count.restype = ct.c_int
     lib.subby_debug_set_kernel.restype = ct.c_int
     lib.subby_debug_set_kernel.argtypes = [ct.c_int]
+    lib.subby_debug_fail_waits.restype = ct.c_int
+    lib.subby_debug_fail_waits.argtypes = [ct.c_int]
     lib.subby_plan_create.restype = ct.c_int
     lib.subby_plan_create.argtypes = [_p, _p, _p, _p, _p, ct.c_int, ct.c_int, ct.POINTER(ct.c_void_p)]
     lib.subby_plan_create_rows.restype = ct.c_int
@@ -73,6 +76,8 @@ def _declare(lib):
     lib.subby_plan_branch_counts.argtypes = [_p, _p, ct.c_int, _p, ct.c_int, ct.c_int, _p, ct.c_int, _p]
     lib.subby_tokenize.restype = ct.c_int
     lib.subby_tokenize.argtypes = [_p, ct.c_int64, _p, _p, _p, _p]
+    lib.subby_gather_rows.restype = ct.c_int
+    lib.subby_gather_rows.argtypes = [_p, ct.c_int64, _p, ct.c_int, ct.c_int, _p, _p]
     lib.subby_mixture_posterior.restype = ct.c_int
     lib.subby_mixture_posterior.argtypes = [_p, _p, ct.c_int, ct.c_int, _p, ct.c_int, _p]
     lib.subby_plan_posteriors.restype = ct.c_int

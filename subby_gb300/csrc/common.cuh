@@ -96,6 +96,8 @@ struct KParams {
   // (4096 elements each), then [Vd^T 1|2|3 | Vu^T 1|2|3] at R*24576
   const uint16_t *tab16;
   int *err;               // device status: bounded waits that gave up (tensor-core walk)
+  int dbg_wait_polls;     // test hook: > 0 makes the tensor-core walk's prologue wait
+                          // on an unarmed mbarrier for that many polls and give up
   // the model is F81 / JC: M_n = e_n I + (1 - e_n) 1 pi^T, so the walk's
   // products take the closed form (tables EF) instead of A x A products
   int f81_model;
@@ -147,6 +149,12 @@ int launch_acc(const KParams &p, int A, bool f81, bool tc, const float *sa, cons
                int c_count, int grid, cudaStream_t s);
 int launch_tree4(const KParams &p, bool f81, int mask_mode, int grid, int block, size_t smem,
                  cudaStream_t s);
+// Load the counts variants of the A = 4 kernel into the current context
+// (cudaFuncGetAttributes), so that a later launch needs no module loading.
+int preload_tree4();
+// Record a fixed failure reason for subby_last_error without allocating
+// (plan.cu); nullptr or "" clears it.
+void set_static_error(const char *why);
 // irreversible counts (k_acccx.cu): complex accumulation + back-transform
 // over the walk's raw staging; pb: per-branch counts
 bool cx_supported(int A);

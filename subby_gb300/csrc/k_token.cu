@@ -64,3 +64,45 @@ extern "C" int subby_tokenize(const uint8_t *chars, int64_t n, const int32_t *lu
   subby::k_tokenize<<<grid, block, 0, s>>>(chars, n, lut, out, reinterpret_cast<unsigned long long *>(first_bad));
   return cudaGetLastError() == cudaSuccess ? SUBBY_OK : SUBBY_ERR_CUDA;
 }
+
+// Token rows of a job's alignment gathered from where the caller holds them
+// (pinned host memory, read by the SMs over the host link, or device memory)
+// into a contiguous (R, C) device array: dst[r][c] = src[map(r) * pitch + c],
+// map(r) = rowmap[r] (device array) or r.  A serving loop hands each job's
+// alignment over as a window of a larger host buffer this way, without a
+// host-side copy into a staging buffer.  Rows whose source and destination
+// are 16-byte aligned (and C a multiple of 4) move as 16-byte vectors.
+namespace subby {
+namespace {
+
+__global__ void k_gather_rows(const int32_t *__restrict__ src, long long pitch, const int32_t *__restrict__ rowmap,
+                              int C, int32_t *__restrict__ dst) {
+  const int r = blockIdx.y;
+  const long long sr = rowmap ? (long long)rowmap[r] : (long long)r;
+  const int32_t *s = src + sr * pitch;
+  int32_t *d = dst + (long long)r * C;
+  const bool vec = ((reinterpret_cast<uintptr_t>(s) | reinterpret_cast<uintptr_t>(d)) & 15) == 0 && (C & 3) == 0;
+  if (vec) {
+    const int nv = C >> 2;
+    for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < nv; v += gridDim.x * blockDim.x)
+      reinterpret_cast<int4 *>(d)[v] = reinterpret_cast<const int4 *>(s)[v];
+  } else {
+    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < C; c += gridDim.x * blockDim.x) d[c] = s[c];
+  }
+}
+
+}  // namespace
+}  // namespace subby
+
+extern "C" int subby_gather_rows(const int32_t *src, int64_t pitch, const int32_t *rowmap, int R, int C,
+                                 int32_t *dst, void *stream_) {
+  if (R < 0 || C < 0 || pitch < C) return SUBBY_ERR_ARG;
+  if (R == 0 || C == 0) return SUBBY_OK;
+  if (!src || !dst) return SUBBY_ERR_ARG;
+  if (R > 65535) return SUBBY_ERR_UNSUPPORTED;
+  const int block = 256;
+  const int per_thread = 4;  // 16-byte vectors per thread per row
+  const int gx = std::max(1, std::min(1024, (C / 4 + block * per_thread - 1) / (block * per_thread)));
+  subby::k_gather_rows<<<dim3(gx, R), block, 0, (cudaStream_t)stream_>>>(src, pitch, rowmap, C, dst);
+  return cudaGetLastError() == cudaSuccess ? SUBBY_OK : SUBBY_ERR_CUDA;
+}

@@ -636,6 +636,18 @@ int launch_tree4(const KParams &p, bool f81, int mask_mode, int grid, int block,
                                 : t4launch_m<kOutSum>(p, f81, mask_mode, grid, block, smem, s);
 }
 
+int preload_tree4() {
+  cudaFuncAttributes a;
+  const void *fns[] = {(const void *)k_tree4<false, kMaskAuto, kOutSum>, (const void *)k_tree4<false, kMaskGiven, kOutSum>,
+                       (const void *)k_tree4<false, kMaskNone, kOutSum>, (const void *)k_tree4<true, kMaskAuto, kOutSum>,
+                       (const void *)k_tree4<true, kMaskGiven, kOutSum>, (const void *)k_tree4<true, kMaskNone, kOutSum>};
+  for (const void *f : fns) {
+    const cudaError_t e = cudaFuncGetAttributes(&a, f);
+    if (e != cudaSuccess) return (int)e;
+  }
+  return 0;
+}
+
 int launch_tree4_post(const KParams &p, int grid, int block, size_t smem, cudaStream_t s) {
   return t4launch<false, kMaskNone, kOutPost>(p, grid, block, smem, s);
 }

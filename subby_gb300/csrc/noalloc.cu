@@ -16,13 +16,21 @@
 //    anything larger returns SUBBY_ERR_UNSUPPORTED with a message.
 //  * Alignment, mask and outputs are device pointers supplied by the caller.
 //  * The first call on a device resolves the device address of the array
-//    (cudaGetSymbolAddress, with that device current); make that first call
-//    before any stream capture.
+//    (cudaGetSymbolAddress, with that device current) and loads the kernel
+//    variants (cudaFuncGetAttributes), so that no later call needs lazy
+//    module loading; make that first call before any stream capture.  A
+//    call with C = 0 does only this set-up (after validating its arguments)
+//    and is the warm-up step.
+//  * The tables are uploaded from one host staging buffer that the next call
+//    rewrites, so a call on a stream that is being captured returns
+//    SUBBY_ERR_UNSUPPORTED instead of recording a copy of that buffer.
 //  * Every call rewrites the whole table region it uses, so nothing carries
 //    over between calls and nothing needs clearing; calls that overlap on
 //    the GPU (for example on two streams) share the array and race.
 //  * No cudaMalloc, cudaFree or other allocating routine is called, on the
 //    device or on the host: host-side staging uses a fixed static buffer.
+//  * A rejection's reason is a fixed string that subby_last_error returns
+//    (no message is formatted, which could allocate).
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -44,11 +52,25 @@ float g_stage[kNoAllocFloats];            // host staging of the tables
 float *g_dev_tables[kMaxDevices] = {nullptr};
 std::mutex g_noalloc_lock;
 
-// Status-code-only failure (no message string: building one could allocate).
-// The reason of each rejection is stated at the return site.
+// Failure with a fixed reason string for subby_last_error (no formatting,
+// no allocation).
 int nfail(int code, const char *why) {
-  (void)why;
+  subby::set_static_error(why);
   return code;
+}
+
+// Once per device, with it current: the device address of the table array
+// and the kernel variants loaded.  Called with g_noalloc_lock held.
+int noalloc_setup(int dev, float **dtab) {
+  if (!g_dev_tables[dev]) {
+    float *ptr = nullptr;
+    const cudaError_t ce = cudaGetSymbolAddress((void **)&ptr, g_noalloc_tables);
+    if (ce != cudaSuccess || !ptr) return nfail(SUBBY_ERR_CUDA, "cudaGetSymbolAddress failed");
+    if (subby::preload_tree4() != 0) return nfail(SUBBY_ERR_CUDA, "loading the A=4 kernels failed");
+    g_dev_tables[dev] = ptr;
+  }
+  *dtab = g_dev_tables[dev];
+  return SUBBY_OK;
 }
 
 int align4(int n) { return (n + 3) & ~3; }
@@ -61,6 +83,7 @@ extern "C" int subby_counts_noalloc(const int32_t *d_aln, const int32_t *parent,
                                     float *d_counts, float *d_logL, void *stream_) {
   using namespace subby;
   const int A = 4;
+  set_static_error("");
   if (!parent || !dist || !evals || !evecs || !pi) return nfail(SUBBY_ERR_ARG, "null argument");
   if (C < 0) return nfail(SUBBY_ERR_ARG, "negative column count");
   if (counts_kind != SUBBY_COUNTS_EIGEN && counts_kind != SUBBY_COUNTS_F81)
@@ -68,8 +91,24 @@ extern "C" int subby_counts_noalloc(const int32_t *d_aln, const int32_t *parent,
   if (mask_mode < 0 || mask_mode > 2) return nfail(SUBBY_ERR_ARG, "bad mask_mode");
   if (R < 1 || R > kNoAllocMaxNodes)
     return nfail(SUBBY_ERR_UNSUPPORTED, "tree larger than the no-allocation limit of 1023 nodes");
-  // zero columns: nothing to compute (empty device buffers may be null)
-  if (C == 0) return SUBBY_OK;
+  cudaStream_t stream = (cudaStream_t)stream_;
+  int dev = 0;
+  cudaError_t ce = cudaGetDevice(&dev);
+  if (ce != cudaSuccess || dev < 0 || dev >= kMaxDevices) return nfail(SUBBY_ERR_CUDA, "cudaGetDevice failed");
+  // zero columns: only the per-device set-up (empty device buffers may be null)
+  if (C == 0) {
+    std::lock_guard<std::mutex> guard(g_noalloc_lock);
+    float *dtab = nullptr;
+    return noalloc_setup(dev, &dtab);
+  }
+  {
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    ce = cudaStreamIsCapturing(stream, &cs);
+    if (ce != cudaSuccess) return nfail(SUBBY_ERR_CUDA, "cudaStreamIsCapturing failed");
+    if (cs != cudaStreamCaptureStatusNone)
+      return nfail(SUBBY_ERR_UNSUPPORTED, "the stream is capturing: the table upload reads a host buffer that "
+                                          "later calls rewrite");
+  }
   if (!d_aln || !d_counts) return nfail(SUBBY_ERR_ARG, "null alignment or counts");
   if (mask_mode == SUBBY_MASK_GIVEN && !d_mask) return nfail(SUBBY_ERR_ARG, "missing mask");
 
@@ -136,17 +175,11 @@ extern "C" int subby_counts_noalloc(const int32_t *d_aln, const int32_t *parent,
     if (order[i] == 0 || kind[order[i]] >= 0) ++nsteps;
 
   std::lock_guard<std::mutex> guard(g_noalloc_lock);
-  int dev = 0;
-  cudaError_t ce = cudaGetDevice(&dev);
-  if (ce != cudaSuccess || dev < 0 || dev >= kMaxDevices) return nfail(SUBBY_ERR_CUDA, "cudaGetDevice failed");
-  if (!g_dev_tables[dev]) {
-    // one-time set-up on this device (with it current): device address of the array
-    float *ptr = nullptr;
-    ce = cudaGetSymbolAddress((void **)&ptr, g_noalloc_tables);
-    if (ce != cudaSuccess || !ptr) return nfail(SUBBY_ERR_CUDA, "cudaGetSymbolAddress failed");
-    g_dev_tables[dev] = ptr;
+  float *dtab = nullptr;
+  {
+    const int rc = noalloc_setup(dev, &dtab);
+    if (rc != SUBBY_OK) return rc;
   }
-  float *dtab = g_dev_tables[dev];
 
   // ---- table layout inside the array (floats)
   TableOffsets o{};
@@ -294,7 +327,6 @@ extern "C" int subby_counts_noalloc(const int32_t *d_aln, const int32_t *parent,
   sofs += nslots * threads;
   if (sofs < (maxsm / 2 + 4096) / 4) sofs = (maxsm / 2 + 4096) / 4;
 
-  cudaStream_t stream = (cudaStream_t)stream_;
   ce = cudaMemcpyAsync(dtab, T, (size_t)cur * sizeof(float), cudaMemcpyHostToDevice, stream);
   if (ce != cudaSuccess) return nfail(SUBBY_ERR_CUDA, "table upload failed");
 

@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <complex>
 #include <cstdlib>
@@ -23,6 +24,9 @@ using namespace subby;
 namespace {
 
 thread_local std::string g_last_error;
+// A fixed reason string set by entry points that must not allocate (a
+// std::string assignment could); it takes precedence over g_last_error.
+thread_local const char *g_static_error = nullptr;
 thread_local int g_launches = 0;
 // Test hook (subby_debug_set_kernel): 0 automatic, 1 thread-per-column
 // kernel (k_small) for A <= 8 / warp-per-column kernel (k_warp) above, 2
@@ -30,10 +34,19 @@ thread_local int g_launches = 0;
 // cores) for large A, 3 tree program with global-memory slots, 4 generic
 // tree program with tensor-memory slots (bypassing the A = 4 specialisation).
 int g_kernel_sel = 0;
+// Test hook (subby_debug_fail_waits): > 0 makes every tensor-core walk give
+// up a prologue wait after that many polls.
+std::atomic<int> g_dbg_wait_polls{0};
 
 int fail(int code, const std::string &msg) {
+  g_static_error = nullptr;
   g_last_error = msg;
   return code;
+}
+
+void clear_error() {
+  g_static_error = nullptr;
+  g_last_error.clear();
 }
 
 int cuda_fail(cudaError_t e, const char *where) {
@@ -304,6 +317,10 @@ int validate_tree(const int32_t *parent, int R, std::vector<int> &left, std::vec
 
 }  // namespace
 
+namespace subby {
+void set_static_error(const char *why) { g_static_error = why; }
+}  // namespace subby
+
 extern "C" {
 
 const char *subby_version(void) { return "subby_gb300 0.1 (sm_103a)"; }
@@ -321,7 +338,7 @@ const char *subby_strerror(int s) {
   }
 }
 
-const char *subby_last_error(void) { return g_last_error.c_str(); }
+const char *subby_last_error(void) { return g_static_error ? g_static_error : g_last_error.c_str(); }
 
 int subby_debug_set_kernel(int which) {
   if (which < 0 || which > 6) return fail(SUBBY_ERR_ARG, "kernel selector must be 0..6");
@@ -329,6 +346,12 @@ int subby_debug_set_kernel(int which) {
   return SUBBY_OK;
 }
 int subby_last_launch_count(void) { return g_launches; }
+
+int subby_debug_fail_waits(int polls) {
+  if (polls < 0 || polls > 4096) return fail(SUBBY_ERR_ARG, "polls must be 0..4096");
+  g_dbg_wait_polls.store(polls);
+  return SUBBY_OK;
+}
 
 }  // extern "C"
 
@@ -344,7 +367,7 @@ struct IrrevInput {
 
 int plan_create(const int32_t *parent, const double *dist, const double *evals, const double *evecs,
                 const double *pi, int R, int A, subby_plan **out, const IrrevInput *ir) {
-  g_last_error.clear();
+  clear_error();
   if (!out || !parent || !dist || !evals || !evecs || !pi) return fail(SUBBY_ERR_ARG, "null argument");
   *out = nullptr;
   if (!small_supported(A) && !warp_supported(A))
@@ -779,7 +802,7 @@ int subby_plan_create(const int32_t *parent, const double *dist, const double *e
 int subby_plan_create_irrev(const int32_t *parent, const double *dist, const double *eigenvalues,
                             const double *eigenvectors, const double *eigenvectors_inv, const double *pi, int R,
                             int A, subby_plan **out) {
-  g_last_error.clear();
+  clear_error();
   if (!eigenvalues || !eigenvectors || !eigenvectors_inv) return fail(SUBBY_ERR_ARG, "null argument");
   if (!(A >= 2 && A <= 64)) return fail(SUBBY_ERR_UNSUPPORTED, "alphabet size out of range");
   for (int i = 0; i < 2 * A; ++i)
@@ -798,7 +821,7 @@ int subby_plan_create_irrev(const int32_t *parent, const double *dist, const dou
 
 int subby_plan_create_rows(const int32_t *parent, const double *dist, const double *eigenvalues,
                            const double *eigenvectors, const double *pi, int R, int A, subby_plan **out) {
-  g_last_error.clear();
+  clear_error();
   if (!parent || !dist || !eigenvalues || !eigenvectors || !pi || !out) return fail(SUBBY_ERR_ARG, "null argument");
   if (!(A >= 2 && A <= 64) || R < 1) return fail(SUBBY_ERR_UNSUPPORTED, "alphabet size out of range");
   // node n's reversible system as V = diag(pi)^-1/2 W, V^-1 = W^T diag(pi)^1/2
@@ -1137,6 +1160,7 @@ KParams walk_params(const subby_plan *P, const int32_t *d_aln, int C, int mode, 
   k.nslots = std::max(P->prog_slots, 1);
   k.tab16 = P->d_tab16;
   k.err = P->d_err;
+  k.dbg_wait_polls = g_dbg_wait_polls.load();
   return k;
 }
 
@@ -1605,7 +1629,7 @@ extern "C" {
 int subby_plan_run(subby_plan *P, const int32_t *aln, int C, float *logL, float *counts,
                    float *rootProb, int counts_kind, int mask_mode, const uint8_t *mask, int flags,
                    void *stream_) {
-  g_last_error.clear();
+  clear_error();
   g_launches = 0;
   if (!P) return fail(SUBBY_ERR_ARG, "null plan");
   if (C < 0) return fail(SUBBY_ERR_ARG, "negative column count");
@@ -1721,6 +1745,7 @@ int subby_plan_run(subby_plan *P, const int32_t *aln, int C, float *logL, float 
     if (dev_err) {
       cudaMemsetAsync(P->d_err, 0, sizeof(int), stream);
       cudaStreamSynchronize(stream);
+      if (dev != P->device) cudaSetDevice(dev);
       return fail(SUBBY_ERR_TIMEOUT, "a bounded device wait gave up (tensor-core walk)");
     }
   }
@@ -1730,7 +1755,7 @@ int subby_plan_run(subby_plan *P, const int32_t *aln, int C, float *logL, float 
 
 int subby_plan_branch_counts(subby_plan *P, const int32_t *aln, int C, float *branchCounts, int counts_kind,
                              int mask_mode, const uint8_t *mask, int flags, void *stream_) {
-  g_last_error.clear();
+  clear_error();
   g_launches = 0;
   if (!P) return fail(SUBBY_ERR_ARG, "null plan");
   if (C < 0) return fail(SUBBY_ERR_ARG, "negative column count");
@@ -1786,7 +1811,7 @@ int subby_plan_branch_counts(subby_plan *P, const int32_t *aln, int C, float *br
 
 int subby_plan_posteriors(subby_plan *P, const int32_t *aln, int C, int node, float *nodePost, float *branchPost,
                           int flags, void *stream_) {
-  g_last_error.clear();
+  clear_error();
   g_launches = 0;
   if (!P) return fail(SUBBY_ERR_ARG, "null plan");
   if (C < 0) return fail(SUBBY_ERR_ARG, "negative column count");
@@ -1834,7 +1859,7 @@ int subby_plan_posteriors(subby_plan *P, const int32_t *aln, int C, int node, fl
 
 int subby_plan_grad(subby_plan *P, const int32_t *aln, int C, const float *g, float *logL,
                     double *dldt, double *dldS, int flags, void *stream_) {
-  g_last_error.clear();
+  clear_error();
   g_launches = 0;
   if (!P || !dldt || !dldS) return fail(SUBBY_ERR_ARG, "null argument");
   if (C < 0) return fail(SUBBY_ERR_ARG, "negative column count");
@@ -2006,6 +2031,7 @@ static int one_shot(const int32_t *aln, const int32_t *parent, const double *dis
   std::string keep = g_last_error;
   subby_plan_destroy(P);
   g_last_error = keep;
+  g_static_error = nullptr;
   return rc;
 }
 

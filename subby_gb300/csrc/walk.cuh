@@ -68,8 +68,8 @@ constexpr uint32_t kIdesc128 = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(
                                ((uint32_t)(128 >> 4) << 24);
 constexpr int kWaitLimit = 1 << 24;  // bounded mbarrier waits
 
-__device__ __forceinline__ bool mbar_wait(uint32_t mb, uint32_t phase) {
-  for (int it = 0; it < kWaitLimit; ++it) {
+__device__ __forceinline__ bool mbar_wait(uint32_t mb, uint32_t phase, int limit = kWaitLimit) {
+  for (int it = 0; it < limit; ++it) {
     uint32_t done;
     asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
                  : "=r"(done)
@@ -176,11 +176,15 @@ struct Walk {
       }
     }
   }
-  // wait for the MMAs of this round trip
+  // wait for the MMAs of this round trip.  Lane 0 of warp 0 arrives here
+  // after issuing them while the other lanes poll already; the __syncwarp
+  // reconverges the warp before the warp-collective (.sync.aligned)
+  // tensor-memory loads that follow.
   __device__ __forceinline__ void mma_wait() {
     TcState &T = tcs;
     if (!mbar_wait(T.mbM, T.nM & 1)) *T.err = 1;
     T.nM += 1;
+    __syncwarp();
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   }
   // this thread's 32 FP32 accumulator columns [col, col + 32) of its lane
@@ -407,6 +411,7 @@ __global__ void __launch_bounds__(128 * Geo<A>::H, 1) k_walk(const KParams P, fl
   __shared__ __align__(8) uint64_t s_mbar[2];
   __shared__ uint32_t s_taddr;
   __shared__ int s_err;
+  __shared__ int s_skip;
   extern __shared__ __align__(1024) unsigned char s_dyn[];  // TC: operand tiles (layout at TcState)
   if constexpr (TC) {
     if ((threadIdx.x >> 5) == 0) {
@@ -434,7 +439,11 @@ __global__ void __launch_bounds__(128 * Geo<A>::H, 1) k_walk(const KParams P, fl
       s_tc.nB = 0;
       s_tc.nM = 0;
       s_tc.err = &s_err;
-      if (MODE == 1) {
+      // Test hook of the failure path: wait on the MMA mbarrier, which
+      // nothing has armed yet (no copy or MMA is in flight), for a few
+      // polls; the wait gives up and the CTA skips its work.
+      s_skip = P.dbg_wait_polls > 0 && !mbar_wait(s_tc.mbM, 0, P.dbg_wait_polls);
+      if (MODE == 1 && !s_skip) {
         // Vd (stacked behind the per-node matrix slots) and Vu, once per CTA
         const uint16_t *Vg = P.tab16 + (size_t)P.R * 24576;
         asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(s_tc.mbB), "r"(6 * 8192)
@@ -453,6 +462,17 @@ __global__ void __launch_bounds__(128 * Geo<A>::H, 1) k_walk(const KParams P, fl
     }
     __syncthreads();
     wk.tcs = s_tc;
+    if (s_skip) {
+      // the test hook's wait gave up (nothing in flight): free the tensor
+      // memory, record the failure in the status word, leave the outputs
+      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+      __syncthreads();
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      if ((threadIdx.x >> 5) == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(s_tc.tmem), "r"(256) : "memory");
+      if (threadIdx.x == 0 && P.err) atomicAdd(P.err, 1);
+      return;
+    }
   }
   wk.warp = threadIdx.x >> 5;
   const int lane = threadIdx.x & 31;

@@ -11,8 +11,21 @@ tokens and tree with the F81 model and reported beside it.
 Output: one JSON line (rank 0).  ``value`` is device throughput with inputs
 resident in HBM; ``e2e`` is the same metric through the public API with host
 (pinned) buffers, copies included; ``roofline`` is the Counts kernel against
-the measured HBM copy bandwidth; ``cpu_baseline`` is the FP64 oracle port on
-the host cores on a bounded sample.
+the measured HBM copy bandwidth, with ``fp32_issue`` (its issue-slot and
+FP32 FLOP fractions) beside it; ``cpu_baseline`` is the FP64 oracle port on
+the host cores on a bounded sample.  On one GPU the line also carries the
+other workloads of the metric, each with its own clock record:
+
+* ``precision64``: A=64 random reversible model with near-degenerate
+  eigenvalue pairs, R=127, C=65536 — Counts + LogLike on the split-BF16
+  tensor-core walk and on the plain FP32 CUDA-core walk, their ratio, errors
+  against the FP64 oracle and each arm's fraction of its own peak;
+* ``grad20``: A=20, R=399, C=10^5 — LogLike + adjoint gradient columns/s
+  through host buffers;
+* ``serving``: 10000 jobs (Poisson 200/s, uneven R, C, A) through the
+  continuous-batching server, each job's alignment uploaded from pinned host
+  memory and its results read back inside its latency — p50 / p99 latency,
+  queue and service percentiles.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
@@ -47,6 +60,51 @@ def _peaks():
             d = json.load(f)
         return float(d["hbm_gbs"]), float(d["bf16_tflops"]), "measured"
     return 6800.0, 1900.0, "fallback"
+
+
+def _fp32_peak_tflops():
+    """Nominal FP32 CUDA-core peak: SMs x 128 FP32 lanes x 2 FLOP x max SM
+    clock (no FP32 peak is measured on this machine)."""
+    import torch
+    nsm = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
+    mhz = 2070.0
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            mhz = float(json.load(f).get("sm_max_mhz", mhz))
+    return nsm * 128 * 2 * mhz * 1e6 / 1e12, nsm, mhz
+
+
+def _profile_entry(kernel):
+    p = os.path.join(ROOT, "profiles", "traffic.json")
+    if not os.path.exists(p):
+        return {}
+    with open(p) as f:
+        return json.load(f).get(kernel, {})
+
+
+def fp32_issue_block(cols_per_s, R, A, clocks):
+    """Issue-slot and FP32 fractions of the A=4 Counts kernel beside its HBM
+    roofline: the kernel is issue-bound, so these are the fractions that
+    move.  Warp instructions per column come from the committed ncu summary
+    (profiles/traffic.json); FP32 FLOP per column is the algorithmic count
+    11 A^2 (R-1) + 4 A^3 (inside / outside products, projections,
+    accumulation, back-transform)."""
+    peak, nsm, mhz = _fp32_peak_tflops()
+    flop_col = 11 * A * A * (R - 1) + 4 * A ** 3
+    out = {"flop_per_column": flop_col, "achieved_tflops": flop_col * cols_per_s / 1e12,
+           "fp32_peak_tflops": peak, "fp32_frac": flop_col * cols_per_s / 1e12 / peak,
+           "fp32_peak_kind": f"nominal: {nsm} SMs x 128 lanes x 2 FLOP x {mhz:.0f} MHz"}
+    e = _profile_entry("counts_eigen_a4")
+    ipc = e.get("thread_instructions_per_column")
+    if ipc:
+        clk = (clocks or {}).get("sm_mhz") or mhz
+        slots = nsm * 4 * clk * 1e6          # warp-instruction issue slots per second
+        out["issue_frac"] = (ipc / 32.0) * cols_per_s / slots
+        out["thread_instructions_per_column"] = ipc
+        out["issue_source"] = ("ncu smsp__inst_executed.sum of the same kernel (profiles/traffic.json) x "
+                               "columns/s / (SMs x 4 schedulers x median SM clock of the timed region)")
+    return out
 
 
 def _traffic_per_column(kernel):
@@ -169,6 +227,8 @@ def main():
                                            "posteriors", "irreversible", "gamma4"],
                     default="plain_large",
                     help="plain_large is the headline line; the others print their own line")
+    ap.add_argument("--headline-only", action="store_true",
+                    help="plain_large: skip the precision64 / grad20 / serving blocks")
     ap.add_argument("--jobs", type=int, default=10000, help="serving: number of jobs")
     ap.add_argument("--rate", type=float, default=200.0, help="serving: Poisson arrival rate (jobs/s)")
     args = ap.parse_args()
@@ -296,6 +356,16 @@ def main():
             torch.distributed.destroy_process_group()
         return 0
 
+    blocks = {}
+    if world == 1 and not args.headline_only:
+        del d_aln, d_aln_f, out, out_f, h_aln, h_out, hbuf
+        plan.close()
+        plan_f81.close()
+        torch.cuda.empty_cache()
+        blocks["precision64"] = precision64_block(args)
+        blocks["grad20"] = grad20_block(args)
+        blocks["serving"] = serving_block(args)
+
     hbm, _, peak_kind = _peaks()
     b_col = 4 * R + 4 * A * A           # int32 tokens in, FP32 counts out
     achieved = b_col * C / (ms / 1000) / 1e9
@@ -323,11 +393,13 @@ def main():
                      "frac": achieved / hbm, "peak_kind": peak_kind,
                      "traffic": None if tr is None else tr * C,
                      "algorithmic_bytes_per_column": b_col},
+        "fp32_issue": fp32_issue_block(C / (ms / 1000), R, A, clocks),
         "cpu_baseline": cpu,
         "clocks": clocks,
         "gpu_launches": launches_per_step * args.steps,
         "max_colwise_err_vs_oracle_64cols": err,
     }
+    line.update(blocks)
     print(json.dumps(line))
     if dist_on:
         torch.distributed.destroy_process_group()
@@ -348,60 +420,98 @@ def _time_fn(fn, steps, warmup):
     return e0.elapsed_time(e1) / steps
 
 
-def precision64_bench(args):
+def precision64_block(args):
     """A=64 random reversible model with near-degenerate eigenvalue pairs,
-    R=127, C=65536: Counts columns/s and error vs the FP64 oracle."""
+    R=127, C=65536 (inputs resident, CUDA events): Counts + LogLike on the
+    split-BF16 tensor-core walk and on the plain FP32 CUDA-core walk, errors
+    against the FP64 oracle on 64 seeded columns, each arm's fraction of its
+    own peak."""
     import torch
     import oracle
     import subby_gb300 as sg
     from subby_gb300 import synth, _lib
     from tests._tol import colwise_err, loglike_err
-    C = args.columns if args.columns != (1 << 20) else 65536
+    C = 65536
     w = synth.precision64(seed=3, C=C)
+    R = len(w['tree'].parentIndex)
+    A = 64
     plan = sg.Plan(w['tree'], w['model'])
     d_aln = torch.as_tensor(w['alignment']).cuda()
-    sub = w['alignment'][:, :32]
+    idx = np.sort(np.random.default_rng(64).choice(C, 64, replace=False))
+    sub = np.ascontiguousarray(w['alignment'][:, idx])
     md = w['model']._asdict()
     t = oracle.Tree(w['tree'].parentIndex, w['tree'].distanceToParent)
     ref_c = oracle.Counts(sub, t, md, branch_mask=None)
     ref_l = oracle.LogLike(sub, t, md)
-    res = {}
     lib = _lib.load()
-    # 0: tensor-core walk (split-BF16) ; 2: plain FP32 CUDA-core walk
+    _, bf16, peak_kind = _peaks()
+    fp32_peak, _, _ = _fp32_peak_tflops()
+    # FLOP per column (FMA = 2): tensor-core-eligible products of the walk,
+    # 8 A^2 per branch (inside M, outside M^T, Vd and Vu projections), and
+    # the back-transform 4 A^3; the whole step adds the J-weighted
+    # accumulation, 3 A^2 per branch, on CUDA cores
+    tc_flop = 8 * A * A * (R - 1) + 4 * A ** 3
+    all_flop = 11 * A * A * (R - 1) + 4 * A ** 3
+    ii = torch.as_tensor(idx).cuda()
+    res = {}
+    steps = max(3, args.steps)
     for name, sel in (("split_bf16_tensor_core", 0), ("fp32_cuda_core", 2)):
         lib.subby_debug_set_kernel(sel)
-        out = {'counts': torch.empty((64, 64, C), dtype=torch.float32, device="cuda"),
-               'logLike': torch.empty(C, dtype=torch.float32, device="cuda")}
-        ms = _time_fn(lambda: plan.run(d_aln, loglike=True, counts=True, branch_mask=None, out=out),
-                      args.steps, args.warmup)
-        launches = _lib.last_launch_count()
-        res[name] = {"value": C / (ms / 1e3), "ms_per_step": ms, "gpu_launches": launches * args.steps,
-                     "err_vs_oracle": {"loglike_rel": loglike_err(out['logLike'][:32].cpu().numpy(), ref_l),
-                                       "counts_colwise": colwise_err(out['counts'][:, :, :32].cpu().numpy(), ref_c),
-                                       "columns": 32}}
-        # LogLike alone (inside pass only)
-        ll = {'logLike': out['logLike']}
-        ms_ll = _time_fn(lambda: plan.run(d_aln, loglike=True, out=ll), args.steps, args.warmup)
-        res[name]["loglike_only_columns_per_s"] = C / (ms_ll / 1e3)
-    lib.subby_debug_set_kernel(0)
+        try:
+            out = {'counts': torch.empty((A, A, C), dtype=torch.float32, device="cuda"),
+                   'logLike': torch.empty(C, dtype=torch.float32, device="cuda")}
+            with ClockSampler(torch.cuda.current_device()) as clk:
+                ms = _time_fn(lambda: plan.run(d_aln, loglike=True, counts=True, branch_mask=None, out=out),
+                              steps, args.warmup)
+            launches = _lib.last_launch_count()
+            ll = {'logLike': out['logLike']}
+            ms_ll = _time_fn(lambda: plan.run(d_aln, loglike=True, out=ll), steps, args.warmup)
+            plan.status()
+            r = {"columns_per_s": C / (ms / 1e3), "ms_per_step": ms, "gpu_launches_per_step": launches,
+                 "loglike_only_columns_per_s": C / (ms_ll / 1e3),
+                 "err_vs_oracle": {"loglike_rel": loglike_err(out['logLike'][ii].cpu().numpy(), ref_l),
+                                   "counts_colwise": colwise_err(out['counts'][:, :, ii].cpu().numpy(), ref_c),
+                                   "columns": len(idx), "branch_mask": None},
+                 "clocks": clk.summary()}
+        finally:
+            lib.subby_debug_set_kernel(0)
+        if sel == 0:
+            ach = tc_flop * r["columns_per_s"] / 1e12
+            r["peak"] = {"unit": "TFLOP/s", "flop_per_column": tc_flop, "achieved": ach, "peak": bf16,
+                         "peak_kind": f"{peak_kind} bf16 burst", "frac": ach / bf16,
+                         "frac_of_split_bf16_ceiling": 6 * ach / bf16,
+                         "note": "useful tensor-core-eligible FLOP over the whole Counts step; split-BF16 "
+                                 "issues 6 BF16 MMAs per product, so its ceiling is 1/6 of the BF16 peak"}
+        else:
+            ach = all_flop * r["columns_per_s"] / 1e12
+            r["peak"] = {"unit": "TFLOP/s", "flop_per_column": all_flop, "achieved": ach, "peak": fp32_peak,
+                         "peak_kind": "nominal FP32 CUDA-core peak", "frac": ach / fp32_peak}
+        res[name] = r
+        del out, ll
+    plan.close()
     tc, fp = res["split_bf16_tensor_core"], res["fp32_cuda_core"]
-    # tensor-core roofline of the step: the tree walk's matrix products,
-    # 8 A^2 FLOP per branch (inside M, outside M^T, Vd and Vu products)
-    R = len(w['tree'].parentIndex)
-    flop_col = 8 * 64 * 64 * (R - 1)
-    _, bf16, peak_kind = _peaks()
-    achieved = flop_col * tc["value"] / 1e12
-    print(json.dumps({"metric": "Counts columns/s (A=64 reversible, R=127, C=65536)", "value": tc["value"],
-                      "unit": UNIT, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
-                      "dtype": "fp32 (split-bf16 tensor-core products)", "forced_near_degenerate_pairs": w['forced_pairs'],
-                      "tensor_core_vs_fp32_speedup": tc["value"] / fp["value"],
-                      "loglike_tensor_core_vs_fp32_speedup": tc["loglike_only_columns_per_s"] / fp["loglike_only_columns_per_s"],
-                      "roofline": {"bound": "tensor", "achieved": achieved, "peak": bf16, "unit": "TFLOP/s",
-                                   "frac": achieved / bf16, "peak_kind": peak_kind, "traffic": None,
-                                   "flop_per_column": flop_col,
-                                   "note": "useful walk FLOP over the whole Counts step; split-BF16 issues 6 "
-                                           "MMAs per product"},
-                      "variants": res}))
+    return {"workload": "precision64: A=64 random reversible (exchangeabilities LogNormal(0,1), "
+                        "pi ~ Dir(1^64), ~5% of eigenvalue pairs within 1e-7), R=127 (64 leaves), "
+                        "C=65536 simulated columns, Counts (unmasked) + LogLike",
+            "unit": UNIT, "steps": steps, "warmup": args.warmup,
+            "forced_near_degenerate_pairs": w['forced_pairs'],
+            "tensor_core_vs_fp32_speedup": tc["columns_per_s"] / fp["columns_per_s"],
+            "loglike_tensor_core_vs_fp32_speedup": tc["loglike_only_columns_per_s"] / fp["loglike_only_columns_per_s"],
+            "precision": {"propagation": "split-BF16 (3 terms, 6 products, FP32 accumulation in TMEM) on the "
+                                         "tensor-core arm; FP32 on the CUDA-core arm",
+                          "J(t)": "FP64 for near-degenerate pairs (|dmu| t < 1e-3), FP32 expm1 form otherwise",
+                          "back_transform": "FP32 (tensor-core arm: split-BF16 products) — the reference "
+                                            "keeps FP64; the measured Counts error above is its effect"},
+            "variants": res}
+
+
+def precision64_bench(args):
+    """Prints the precision64 block as its own line."""
+    b = precision64_block(args)
+    b.update({"metric": "Counts columns/s (A=64 reversible, R=127, C=65536)",
+              "value": b["variants"]["split_bf16_tensor_core"]["columns_per_s"], "higher_is_better": True,
+              "dtype": "fp32 (split-bf16 tensor-core products)"})
+    print(json.dumps(b))
     return 0
 
 
@@ -489,45 +599,63 @@ def widened_bench(args):
     return 0
 
 
-def grad20_bench(args):
+def grad20_block(args):
     """A=20 reversible model, R=399, C=100000: forward + adjoint gradient
-    (d sum logL / d branch lengths and / d log-exchangeabilities)."""
+    (d sum logL / d branch lengths and / d log-exchangeabilities) through
+    host buffers (each step uploads the alignment and reads the gradients)."""
     import torch
     import subby_gb300 as sg
     from subby_gb300 import synth, autograd
-    C = args.columns if args.columns != (1 << 20) else 100000
+    C = 100000
     w = synth.grad20(seed=4, C=C)
     plan = sg.Plan(w['tree'], w['model'])
     aln = w['alignment']
-    t0 = time.perf_counter()
     for _ in range(args.warmup):
         plan.grad(aln)
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        _, dldt, G = plan.grad(aln)
-    ms = (time.perf_counter() - t0) * 1e3 / args.steps
+    steps = max(3, args.steps)
+    with ClockSampler(torch.cuda.current_device()) as clk:
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            _, dldt, G = plan.grad(aln)
+        ms = (time.perf_counter() - t0) * 1e3 / steps
     dle = autograd.exchangeability_grad(G, w['log_exch'], w['pi'])
-    print(json.dumps({"metric": "LogLike + adjoint gradient columns/s (A=20, R=399, C=100000, host buffers)",
-                      "value": C / (ms / 1e3), "unit": UNIT, "ms_per_step": ms, "steps": args.steps,
-                      "higher_is_better": True, "dtype": "fp32",
-                      "grad_norms": {"d_dt": float(np.linalg.norm(dldt)), "d_dlogs": float(np.linalg.norm(dle))}}))
+    dev_bytes = plan.device_bytes()
+    plan.close()
+    return {"workload": "grad20: A=20 reversible (exchangeabilities LogNormal(0,0.5), pi ~ Dir(2^20)), R=399 "
+                        "(200 leaves), C=100000 simulated columns, 15% gaps",
+            "value": C / (ms / 1e3), "unit": UNIT, "ms_per_step": ms, "steps": steps,
+            "what": "LogLike + d/d(branch lengths) + d/dS~ per step, host buffers (1.6e8 B in), synchronous",
+            "h2d_bytes_per_step": aln.nbytes, "plan_device_bytes": dev_bytes,
+            "grad_norms": {"d_dt": float(np.linalg.norm(dldt)), "d_dlogs": float(np.linalg.norm(dle))},
+            "clocks": clk.summary()}
+
+
+def grad20_bench(args):
+    b = grad20_block(args)
+    b["metric"] = "LogLike + adjoint gradient columns/s (A=20, R=399, C=100000, host buffers)"
+    b["higher_is_better"] = True
+    print(json.dumps(b))
     return 0
 
 
-def serving_bench(args):
+def serving_block(args):
     """Poisson job stream (uneven R, C, A) through the continuous-batching
-    loop; per-job latency from arrival to results in host memory."""
+    server.  Each job's alignment is a window of a pinned host buffer that
+    the server uploads on the job's stream (the SMs gather it over the host
+    link), and its results are copied back to pinned host memory: per-job
+    latency runs from arrival to results in host memory and includes both."""
     # keep freed plan memory cached in the library pool between jobs
     os.environ.setdefault("SUBBY_POOL_KEEP_MB", str(32 << 10))
     import torch
-    import subby_gb300 as sg
     from subby_gb300 import synth, serve, models
     desc = synth.serving_jobs(n_jobs=args.jobs, rate=args.rate, seed=5)
     # warm-up stream (other seed, not timed): loads every kernel once and
     # grows the slot arenas and host/device pools to their working sizes
     wdesc = synth.serving_jobs(n_jobs=max(100, 50 * args.warmup), rate=args.rate, seed=6)
-    # token pools drawn once on the device, per alphabet: leaf states uniform
-    # with 5% gaps (A+1); each job reads a window of its alphabet's pool
+    # token pools in pinned host memory, one per alphabet: rows of leaf
+    # states uniform with 5% gaps (A+1) and a last row of A (unobserved) for
+    # the internal nodes; a job reads its leaves' rows and that row over a
+    # window of columns
     POOL_C = max(d['C'] for d in desc + wdesc)
     max_leaves = max(d['leaves'] for d in desc + wdesc)
     g = torch.Generator(device="cuda")
@@ -535,8 +663,11 @@ def serving_bench(args):
     pools = {}
     for A_ in sorted({d['A'] for d in desc + wdesc}):
         v = torch.randint(0, 20 * A_, (max_leaves + 1, POOL_C), dtype=torch.int32, device="cuda", generator=g)
-        pools[A_] = torch.where(v < 19 * A_, v % A_, A_ + 1).contiguous()
-        pools[A_][max_leaves].fill_(A_)
+        v = torch.where(v < 19 * A_, v % A_, A_ + 1)
+        v[max_leaves].fill_(A_)
+        h = torch.empty((max_leaves + 1, POOL_C), dtype=torch.int32, pin_memory=True)
+        h.copy_(v)
+        pools[A_] = h
         del v
     torch.cuda.synchronize()
 
@@ -554,17 +685,13 @@ def serving_bench(args):
             tree = synth.random_tree(d['leaves'], 0.1, rng)
             R, C = len(tree.parentIndex), d['C']
             leaf = synth.leaf_mask(tree)
-            # pool row of every tree row: leaves take distinct random rows,
-            # internal rows the pool's constant row of A (unobserved)
-            rowmap = np.full(R, max_leaves, dtype=np.int64)
-            rowmap[leaf] = np.arange(int(leaf.sum()))
-            rowmap = torch.from_numpy(rowmap).cuda()
+            # pool row of every tree row: leaves take distinct rows, internal
+            # rows the pool's row of A (unobserved)
+            rowmap = np.full(R, max_leaves, dtype=np.int32)
+            rowmap[leaf] = np.arange(int(leaf.sum()), dtype=np.int32)
             off = int(np.random.default_rng(d['seed']).integers(0, POOL_C - C + 1))
-
-            def make(stream, device, out, C=C, A=A, rowmap=rowmap, off=off):
-                # the job's tokens in one gather, with no allocation and no host wait
-                torch.index_select(pools[A][:, off:off + C], 0, rowmap, out=out)
-            out.append(serve.Job(id=d['id'], alignment=make, shape=(R, C), tree=tree, model=model,
+            aln = serve.HostRows(base=pools[A], col0=off, rowmap=torch.from_numpy(rowmap).cuda(), R=R, C=C)
+            out.append(serve.Job(id=d['id'], alignment=aln, tree=tree, model=model,
                                  f81=(d['kind'] == 'f81'), want=("counts",), arrival=d['arrival']))
         return out
 
@@ -575,7 +702,8 @@ def serving_bench(args):
     srv.run(warm, realtime=False, on_done=lambda j: j.release())
     srv.completed = []
     srv.host_s = {k: 0.0 for k in srv.host_s}
-    done = srv.run(jobs, realtime=True, on_done=lambda j: j.release())
+    with ClockSampler(torch.cuda.current_device()) as clk:
+        done = srv.run(jobs, realtime=True, on_done=lambda j: j.release())
     st = serve.latency_stats(done)
     kind_of = {d['id']: f"A={d['A']} {d['kind']}" for d in desc}
     by_kind = {}
@@ -586,17 +714,32 @@ def serving_bench(args):
             by_kind[k] = {"jobs": s2['jobs'], "p50_ms": s2['p50_ms'], "p99_ms": s2['p99_ms'],
                           "queue_p99_ms": s2['queue_p99_ms'], "service_p99_ms": s2['service_p99_ms'],
                           "columns": s2['columns']}
+    failed = sum(1 for j in done if j.error)
+    h2d = sum(j.alignment.nbytes for j in done)
+    d2h = sum(4 * j.RC[1] * len(j.model.pi) ** 2 for j in done)
     srv.close()
-    print(json.dumps({"metric": "serving latency (Poisson arrivals, uneven R/C/A)", "value": st['p99_ms'],
-                      "unit": "ms (p99)", "higher_is_better": False, "p50_ms": st['p50_ms'],
-                      "p99_ms": st['p99_ms'], "max_ms": st['max_ms'], "jobs": st['jobs'],
-                      "queue_p50_ms": st['queue_p50_ms'], "queue_p99_ms": st['queue_p99_ms'],
-                      "service_p50_ms": st['service_p50_ms'], "service_p99_ms": st['service_p99_ms'],
-                      "columns_per_s": st['columns_per_s'], "span_s": st['span_s'], "rate_jobs_per_s": args.rate,
-                      "by_kind": by_kind,
-                      "host_s": {k: round(v, 3) for k, v in srv.host_s.items()},
-                      "data": "synthetic: per-job random tree and model; leaf tokens uniform with 5% gaps, "
-                              "windows of a device-resident pool; internal rows unobserved"}))
+    return {"workload": f"{st['jobs']} jobs, Poisson arrivals at {args.rate:g}/s; leaves log-uniform 8..512, "
+                        "C log-uniform 100..2e5, A in {4 HKY85, 16 random reversible, 64 F81 or random "
+                        "reversible}; Counts (mask auto) per job",
+            "value": st['p99_ms'], "unit": "ms (p99)", "higher_is_better": False,
+            "p50_ms": st['p50_ms'], "p99_ms": st['p99_ms'], "max_ms": st['max_ms'], "jobs": st['jobs'],
+            "failed_jobs": failed,
+            "queue_p50_ms": st['queue_p50_ms'], "queue_p99_ms": st['queue_p99_ms'],
+            "service_p50_ms": st['service_p50_ms'], "service_p99_ms": st['service_p99_ms'],
+            "columns_per_s": st['columns_per_s'], "span_s": st['span_s'], "rate_jobs_per_s": args.rate,
+            "h2d_bytes": h2d, "d2h_bytes": d2h, "by_kind": by_kind,
+            "host_s": {k: round(v, 3) for k, v in srv.host_s.items()},
+            "latency": "arrival -> counts in pinned host memory; includes the upload of the job's alignment "
+                       "from pinned host memory and the result copy",
+            "data": "synthetic: per-job random tree and model; leaf tokens uniform with 5% gaps from a pinned "
+                    "host pool, internal rows unobserved",
+            "clocks": clk.summary()}
+
+
+def serving_bench(args):
+    b = serving_block(args)
+    b["metric"] = "serving latency (Poisson arrivals, uneven R/C/A)"
+    print(json.dumps(b))
     return 0
 
 

@@ -33,6 +33,7 @@ checks this).
 from __future__ import annotations
 
 import collections
+import ctypes as ct
 import hashlib
 import threading
 import time
@@ -40,16 +41,40 @@ from dataclasses import dataclass, field
 
 import numpy as np
 
+from . import _lib
 from .api import Plan
 from .models import ensure_diag
 from . import batch
 
 
 @dataclass
+class HostRows:
+    """A job's alignment held as rows of a larger pinned host buffer: row r
+    of the job is row ``rowmap[r]`` of ``base`` (``rowmap`` a CUDA int32
+    tensor of R entries, or None for row r), columns [col0, col0 + C).  The
+    server uploads it with one gather kernel (subby_gather_rows) on the
+    job's stream, the SMs reading the host rows over the host link."""
+    base: object          # pinned CPU torch int32 tensor (rows, pitch)
+    col0: int
+    rowmap: object        # CUDA int32 tensor (R,) or None
+    R: int
+    C: int
+
+    @property
+    def shape(self):
+        return (self.R, self.C)
+
+    @property
+    def nbytes(self):
+        return 4 * self.R * self.C
+
+
+@dataclass
 class Job:
     id: int
-    alignment: object              # (R, C) int32: host array, CUDA tensor, or a
-    #                                callable(stream, device, out) that fills
+    alignment: object              # (R, C) int32: host array, CUDA tensor,
+    #                                HostRows (rows of a pinned host buffer), or
+    #                                a callable(stream, device, out) that fills
     #                                the (R, C) int32 CUDA tensor ``out``
     tree: object
     model: object
@@ -259,7 +284,16 @@ class Server:
         t_tok = time.perf_counter()
         pinned_in = None
         with torch.cuda.stream(stream):
-            if callable(job.alignment):
+            if isinstance(job.alignment, HostRows):
+                hr = job.alignment
+                pitch = int(hr.base.stride(0))
+                src = hr.base.data_ptr() + 4 * int(hr.col0)
+                rm = hr.rowmap.data_ptr() if hr.rowmap is not None else None
+                _lib.check(_lib.load().subby_gather_rows(
+                    ct.c_void_p(src), pitch, None if rm is None else ct.c_void_p(rm), R, C,
+                    ct.c_void_p(v["aln"].data_ptr()), ct.c_void_p(stream.cuda_stream)), "subby_gather_rows")
+                d_aln = v["aln"]
+            elif callable(job.alignment):
                 job.alignment(stream, self.device, v["aln"])
                 d_aln = v["aln"]
             elif isinstance(job.alignment, torch.Tensor) and job.alignment.is_cuda:

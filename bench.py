@@ -231,6 +231,9 @@ def main():
                     help="plain_large: skip the precision64 / grad20 / serving blocks")
     ap.add_argument("--jobs", type=int, default=10000, help="serving: number of jobs")
     ap.add_argument("--rate", type=float, default=200.0, help="serving: Poisson arrival rate (jobs/s)")
+    ap.add_argument("--trace", default=None,
+                    help="serving: write one JSON line per job (kind, R, C, estimated cost, arrival, start, "
+                         "finish) to this file")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -690,20 +693,24 @@ def serving_block(args):
             rowmap = np.full(R, max_leaves, dtype=np.int32)
             rowmap[leaf] = np.arange(int(leaf.sum()), dtype=np.int32)
             off = int(np.random.default_rng(d['seed']).integers(0, POOL_C - C + 1))
-            aln = serve.HostRows(base=pools[A], col0=off, rowmap=torch.from_numpy(rowmap).cuda(), R=R, C=C)
+            aln = serve.HostRows(base=pools[A], col0=off, rowmap=rowmap, R=R, C=C)
             out.append(serve.Job(id=d['id'], alignment=aln, tree=tree, model=model,
                                  f81=(d['kind'] == 'f81'), want=("counts",), arrival=d['arrival']))
         return out
 
     jobs, warm = build(desc), build(wdesc)
-    srv = serve.Server(max_inflight=8, device_budget=64 << 30)
-    srv.prewarm(host_bytes=4 << 30, device_bytes=48 << 30)
+    # the library's engine (C++ thread): Python only submits and collects
+    srv = serve.NativeServer(max_inflight=8, device_budget=64 << 30, pinned_prewarm=4 << 30)
     # the consumer takes each result as it lands and hands its buffers back
     srv.run(warm, realtime=False, on_done=lambda j: j.release())
-    srv.completed = []
-    srv.host_s = {k: 0.0 for k in srv.host_s}
+    eng0 = srv.stats()
     with ClockSampler(torch.cuda.current_device()) as clk:
+        t_run = time.perf_counter()
         done = srv.run(jobs, realtime=True, on_done=lambda j: j.release())
+        t_run = time.perf_counter() - t_run
+    engine = srv.stats()
+    for k in ("engine_busy_s", "packed_jobs", "packed_launches"):
+        engine[k] -= eng0[k]
     st = serve.latency_stats(done)
     kind_of = {d['id']: f"A={d['A']} {d['kind']}" for d in desc}
     by_kind = {}
@@ -714,6 +721,15 @@ def serving_block(args):
             by_kind[k] = {"jobs": s2['jobs'], "p50_ms": s2['p50_ms'], "p99_ms": s2['p99_ms'],
                           "queue_p99_ms": s2['queue_p99_ms'], "service_p99_ms": s2['service_p99_ms'],
                           "columns": s2['columns']}
+    if getattr(args, "trace", None):
+        dmap = {d['id']: d for d in desc}
+        with open(args.trace, "w") as f:
+            for j in done:
+                d = dmap[j.id]
+                R, C = j.RC
+                f.write(json.dumps({"id": j.id, "A": d['A'], "kind": d['kind'], "R": R, "C": C,
+                                    "cost_ms": serve.job_cost_ms(R, C, d['A'], d['kind'] == 'f81'),
+                                    "arrival": j.arrival, "start": j.start, "finish": j.finish}) + "\n")
     failed = sum(1 for j in done if j.error)
     h2d = sum(j.alignment.nbytes for j in done)
     d2h = sum(4 * j.RC[1] * len(j.model.pi) ** 2 for j in done)
@@ -728,7 +744,11 @@ def serving_block(args):
             "service_p50_ms": st['service_p50_ms'], "service_p99_ms": st['service_p99_ms'],
             "columns_per_s": st['columns_per_s'], "span_s": st['span_s'], "rate_jobs_per_s": args.rate,
             "h2d_bytes": h2d, "d2h_bytes": d2h, "by_kind": by_kind,
-            "host_s": {k: round(v, 3) for k, v in srv.host_s.items()},
+            "host": {"engine_busy_s": round(engine["engine_busy_s"], 3), "wall_s": round(t_run, 3),
+                     "plans_cached": engine["plans_cached"], "packed_jobs": engine["packed_jobs"],
+                     "packed_launches": engine["packed_launches"],
+                     "engine": "library serving engine (subby_server_*, one C++ thread); Python submits "
+                               "each job at its arrival time and collects results"},
             "latency": "arrival -> counts in pinned host memory; includes the upload of the job's alignment "
                        "from pinned host memory and the result copy",
             "data": "synthetic: per-job random tree and model; leaf tokens uniform with 5% gaps from a pinned "

@@ -269,6 +269,94 @@ int subby_counts_noalloc(const int32_t *alignment, const int32_t *parent_index,
                          const uint8_t *mask, float *counts, float *logLike,
                          void *stream);
 
+/*
+ * Serving engine: continuous batching of jobs of uneven R, C and A on the
+ * current device.  An engine thread admits submitted jobs as slots and the
+ * device-memory budget free up (shortest estimated job first, aged by its
+ * wait; two slots kept for short jobs), runs short A = 4 jobs that wait
+ * together as one launch of a persistent kernel over their flattened
+ * (job, column-tile) queue, keeps prepared plans resident in an LRU cache
+ * keyed by tree and model, gathers each job's alignment rows from host
+ * memory on the job's own stream, runs long jobs as column slices so that
+ * short ones are not held behind them, and copies results into pinned host
+ * blocks that the caller hands back with subby_server_release.  The
+ * reference has no server (its batching is jax.vmap over same-shaped trees,
+ * scripts/batch_eigensub_maf.py:527-532); the per-job computation is
+ * subby_plan_run's.  Reversible models only.
+ */
+typedef struct subby_server subby_server;
+
+#define SUBBY_WANT_LOGLIKE  1
+#define SUBBY_WANT_COUNTS   2
+#define SUBBY_WANT_ROOTPROB 4
+
+typedef struct subby_job {
+  /* tree and model, host memory, copied by subby_server_submit */
+  const int32_t *parent_index;
+  const double *distances;
+  int R;
+  const double *eigenvalues, *eigenvectors, *pi;
+  int A;
+  /* alignment: row r of the job is alignment + map(r) * pitch (C int32
+   * tokens), map(r) = row_map[r] (host, R entries, copied) or r.  Pinned
+   * host memory (read by the GPU over the host link) or device memory; it
+   * must stay valid until the job completes. */
+  const int32_t *alignment;
+  int64_t pitch;
+  const int32_t *row_map;
+  int C;
+  int want;          /* SUBBY_WANT_* bits */
+  int counts_kind;   /* SUBBY_COUNTS_EIGEN / SUBBY_COUNTS_F81 */
+  int mask_mode;     /* SUBBY_MASK_NONE / SUBBY_MASK_AUTO */
+  double arrival;    /* arrival time on the server clock, or < 0 for now */
+  int64_t tag;       /* caller's identifier, returned with the result */
+} subby_job;
+
+typedef struct subby_job_result {
+  int64_t tag, handle;
+  int status;        /* SUBBY_OK, SUBBY_ERR_TIMEOUT (a bounded device wait gave up), ... */
+  const float *logLike, *counts, *rootProb;  /* pinned host, (C,), (A,A,C), (A,C) or NULL */
+  double t_arrival, t_start, t_finish;       /* server clock, seconds */
+} subby_job_result;
+
+/* Create an engine on the current device with max_inflight slots (2..64),
+ * a device-memory budget for admitted jobs, and pinned result blocks
+ * allocated up front (two of every power-of-two size up to
+ * pinned_prewarm_bytes). */
+int subby_server_create(int max_inflight, size_t device_budget, size_t pinned_prewarm_bytes,
+                        subby_server **out);
+/* Queue a job (thread-safe; returns at once). */
+int subby_server_submit(subby_server *server, const subby_job *job);
+/* Collect up to max completed jobs, waiting up to timeout_ms for the first;
+ * *n receives how many.  Each result's buffers stay valid until
+ * subby_server_release(handle). */
+int subby_server_wait(subby_server *server, subby_job_result *out, int max, int timeout_ms, int *n);
+int subby_server_release(subby_server *server, int64_t handle);
+/* Scheduling parameters, before the first submission: "short_ms" (jobs up
+ * to this estimated device time take the high-priority streams and the
+ * reserved slots; 5), "slice_ms" (long jobs run as column slices of about
+ * this device time; 8), "wave_cols" (slice granularity in columns; 0 = one
+ * wave of the kernels' grids), "aging" (ms of estimated cost forgiven per ms
+ * waited; 0.2), "short_slots" (2), "plan_cache" (resident plans; 64),
+ * "pack" (1: short A = 4 jobs waiting together run as one launch of the
+ * persistent packed kernel over their (job, column-tile) queue; 0: one
+ * launch per job), "pack_max_jobs" (64). */
+int subby_server_set(subby_server *server, const char *key, double value);
+/* Seconds since the engine was created (the clock of arrival / finish). */
+double subby_server_clock(subby_server *server);
+/* Engine-thread busy time, cached plans, in-flight runs, waiting jobs, and
+ * the jobs / launches of the packed A = 4 kernel so far (any may be NULL). */
+int subby_server_stats(subby_server *server, double *engine_busy_s, int *plans_cached, int *inflight,
+                       int *waiting, long long *packed_jobs, long long *packed_launches);
+/* Finish every queued job, then free the engine and everything it holds. */
+int subby_server_destroy(subby_server *server);
+/* Test hook of the packed kernel's bounded queue wait: launches it on `grid`
+ * CTAs over an open queue with nothing published; every CTA's claim waits
+ * `polls` polls, gives up and counts itself in the status word (*gave_up).
+ * Returns SUBBY_ERR_TIMEOUT when any wait gave up.  Synchronous; no
+ * reference counterpart. */
+int subby_debug_packed_queue_wait(int polls, int grid, int *gave_up);
+
 /* Test hook selecting the kernel so that every code path can be checked
  * against the oracle: 0 automatic (A = 4 tree kernel with tensor-memory
  * slots when it fits; A = 64 tree walk on the tensor cores), 1

@@ -24,8 +24,27 @@ EXPORTS = (
     "subby_plan_posteriors", "subby_plan_status", "subby_plan_run", "subby_plan_grad",
     "subby_loglike", "subby_counts", "subby_rootprob", "subby_last_launch_count",
     "subby_debug_set_kernel", "subby_debug_fail_waits", "subby_counts_noalloc", "subby_mixture_posterior",
-    "subby_tokenize", "subby_gather_rows",
+    "subby_tokenize", "subby_gather_rows", "subby_server_create", "subby_server_submit", "subby_server_wait",
+    "subby_server_release", "subby_server_set", "subby_server_clock", "subby_server_stats",
+    "subby_server_destroy", "subby_debug_packed_queue_wait",
 )
+WANT_LOGLIKE, WANT_COUNTS, WANT_ROOTPROB = 1, 2, 4
+
+
+class Job(ct.Structure):
+    """struct subby_job of include/subby_gb300.h."""
+    _fields_ = [("parent_index", ct.c_void_p), ("distances", ct.c_void_p), ("R", ct.c_int),
+                ("eigenvalues", ct.c_void_p), ("eigenvectors", ct.c_void_p), ("pi", ct.c_void_p), ("A", ct.c_int),
+                ("alignment", ct.c_void_p), ("pitch", ct.c_int64), ("row_map", ct.c_void_p), ("C", ct.c_int),
+                ("want", ct.c_int), ("counts_kind", ct.c_int), ("mask_mode", ct.c_int), ("arrival", ct.c_double),
+                ("tag", ct.c_int64)]
+
+
+class JobResult(ct.Structure):
+    """struct subby_job_result of include/subby_gb300.h."""
+    _fields_ = [("tag", ct.c_int64), ("handle", ct.c_int64), ("status", ct.c_int),
+                ("logLike", ct.c_void_p), ("counts", ct.c_void_p), ("rootProb", ct.c_void_p),
+                ("t_arrival", ct.c_double), ("t_start", ct.c_double), ("t_finish", ct.c_double)]
 
 _lock = threading.Lock()
 _lib = None
@@ -77,6 +96,25 @@ def _declare(lib):
     lib.subby_tokenize.restype = ct.c_int
     lib.subby_tokenize.argtypes = [_p, ct.c_int64, _p, _p, _p, _p]
     lib.subby_gather_rows.restype = ct.c_int
+    lib.subby_server_create.restype = ct.c_int
+    lib.subby_server_create.argtypes = [ct.c_int, ct.c_size_t, ct.c_size_t, ct.POINTER(ct.c_void_p)]
+    lib.subby_server_submit.restype = ct.c_int
+    lib.subby_server_submit.argtypes = [_p, ct.POINTER(Job)]
+    lib.subby_server_wait.restype = ct.c_int
+    lib.subby_server_wait.argtypes = [_p, ct.POINTER(JobResult), ct.c_int, ct.c_int, ct.POINTER(ct.c_int)]
+    lib.subby_server_release.restype = ct.c_int
+    lib.subby_server_release.argtypes = [_p, ct.c_int64]
+    lib.subby_server_set.restype = ct.c_int
+    lib.subby_server_set.argtypes = [_p, ct.c_char_p, ct.c_double]
+    lib.subby_server_clock.restype = ct.c_double
+    lib.subby_server_clock.argtypes = [_p]
+    lib.subby_server_stats.restype = ct.c_int
+    lib.subby_server_stats.argtypes = [_p, ct.POINTER(ct.c_double), ct.POINTER(ct.c_int), ct.POINTER(ct.c_int),
+                                       ct.POINTER(ct.c_int), ct.POINTER(ct.c_longlong), ct.POINTER(ct.c_longlong)]
+    lib.subby_server_destroy.restype = ct.c_int
+    lib.subby_server_destroy.argtypes = [_p]
+    lib.subby_debug_packed_queue_wait.restype = ct.c_int
+    lib.subby_debug_packed_queue_wait.argtypes = [ct.c_int, ct.c_int, ct.POINTER(ct.c_int)]
     lib.subby_gather_rows.argtypes = [_p, ct.c_int64, _p, ct.c_int, ct.c_int, _p, _p]
     lib.subby_mixture_posterior.restype = ct.c_int
     lib.subby_mixture_posterior.argtypes = [_p, _p, ct.c_int, ct.c_int, _p, ct.c_int, _p]

@@ -149,6 +149,23 @@ int launch_acc(const KParams &p, int A, bool f81, bool tc, const float *sa, cons
                int c_count, int grid, cudaStream_t s);
 int launch_tree4(const KParams &p, bool f81, int mask_mode, int grid, int block, size_t smem,
                  cudaStream_t s);
+// Packed queue of (job, column tile) work items of the A = 4 serving kernel
+// (k_tree4_packed): jobs[j] are the tree-kernel parameters of job j, items
+// are (job, first column of a tile of blockDim.x columns).  CTAs claim items
+// with an atomic counter; an item at or past *published is waited for (at
+// most wait_polls polls) until *closed is set, and a wait that gives up
+// increments *err and ends the CTA.
+struct T4Queue {
+  const KParams *jobs;
+  const int2 *items;
+  int *head;
+  const int *published;
+  const int *closed;
+  int wait_polls;
+  int *err;
+};
+int launch_tree4_packed(const T4Queue &q, bool f81, int mask_mode, int grid, int block, size_t smem,
+                        cudaStream_t s);
 // Load the counts variants of the A = 4 kernel into the current context
 // (cudaFuncGetAttributes), so that a later launch needs no module loading.
 int preload_tree4();

@@ -910,6 +910,27 @@ int subby_plan_trim(subby_plan *P) {
   return SUBBY_OK;
 }
 
+}  // extern "C"
+
+namespace subby {
+// Serving support (server.cu): enqueue on `s` a copy of the plan's device
+// status word into the pinned host word *h (valid once `s` passes this
+// point) followed by clearing the device word, so a completed job's status
+// is known without a blocking copy.
+int plan_status_async(subby_plan *P, int *h, cudaStream_t s) {
+  if (!P || !h) return SUBBY_ERR_ARG;
+  if (!P->d_err) {
+    *h = 0;
+    return SUBBY_OK;
+  }
+  cudaError_t e = cudaMemcpyAsync(h, P->d_err, sizeof(int), cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(P->d_err, 0, sizeof(int), s);
+  return e == cudaSuccess ? SUBBY_OK : SUBBY_ERR_CUDA;
+}
+}  // namespace subby
+
+extern "C" {
+
 size_t subby_plan_device_bytes(const subby_plan *P) {
   if (!P) return 0;
   return P->tab_bytes + P->work.bytes + P->io.bytes + sizeof(int4) * 2 * P->nInt;
@@ -1623,6 +1644,62 @@ int run_common(subby_plan *P, const int32_t *d_aln, int C, float *d_logL, float 
 }
 
 }  // namespace
+
+namespace subby {
+// Packed serving (server.cu): the A = 4 tree kernel's parameters of a
+// device-pointer run of plan P over d_aln (R, C), without launching.  On
+// success `stream` waits for the plan's tables and *smem / *block are the
+// launch's dynamic shared memory and CTA size; the caller launches the
+// packed kernel on `stream` and then calls plan_mark_used.  Returns nonzero
+// (nothing enqueued) when the plan does not take the A = 4 tree kernel with
+// 256 threads per CTA, or the kernel selector is not automatic.
+int plan_tree4_params(subby_plan *P, const int32_t *d_aln, int C, float *d_logL, float *d_counts,
+                      float *d_root, int counts_kind, int mask_mode, KParams *out, size_t *smem, int *block,
+                      cudaStream_t stream) {
+  if (!P || P->irrev || P->rows || P->A != 4 || P->R < 2 || C < 1 || !out) return SUBBY_ERR_UNSUPPORTED;
+  if (mask_mode != SUBBY_MASK_NONE && mask_mode != SUBBY_MASK_AUTO) return SUBBY_ERR_UNSUPPORTED;
+  int mode = kModeBT64;
+  if (d_logL) mode |= kModeLogLike;
+  if (d_root) mode |= kModeRootProb;
+  if (d_counts) mode |= kModeCounts;
+  if (d_counts && counts_kind == SUBBY_COUNTS_F81) mode |= kModeF81;
+  if (!d_counts) mask_mode = SUBBY_MASK_NONE;
+  std::lock_guard<std::mutex> g(P->lock);
+  Launch L;
+  if (plan_tree4(P, mode, C, L) != 0 || L.block != 256) return SUBBY_ERR_UNSUPPORTED;
+  KParams &k = L.kp;
+  k.aln = d_aln;
+  k.C = C;
+  k.R = P->R;
+  k.A = P->A;
+  k.nInt = P->nInt;
+  k.mode = mode;
+  k.mask_mode = mask_mode;
+  k.mask = nullptr;
+  k.tab = P->d_tab;
+  k.tab64 = P->d_tab64;
+  k.off = P->off;
+  k.steps = P->d_steps;
+  k.slots = P->d_slots;
+  k.root_is_leaf = P->root_is_leaf;
+  k.f81_mu = P->f81_mu;
+  k.nworkers = L.nworkers;
+  k.logL = d_logL;
+  k.counts = d_counts;
+  k.rootp = d_root;
+  if (cudaStreamWaitEvent(stream, P->ready, 0) != cudaSuccess) return SUBBY_ERR_CUDA;
+  *out = k;
+  *smem = L.smem;
+  *block = L.block;
+  return SUBBY_OK;
+}
+
+// The plan's tables were read by work enqueued on `stream` up to here.
+int plan_mark_used(subby_plan *P, cudaStream_t stream) {
+  std::lock_guard<std::mutex> g(P->lock);
+  return mark_use(P, stream);
+}
+}  // namespace subby
 
 extern "C" {
 

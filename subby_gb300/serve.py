@@ -56,7 +56,8 @@ class HostRows:
     job's stream, the SMs reading the host rows over the host link."""
     base: object          # pinned CPU torch int32 tensor (rows, pitch)
     col0: int
-    rowmap: object        # CUDA int32 tensor (R,) or None
+    rowmap: object        # int32 row indices (R,): a CUDA tensor for Server,
+    #                       a host array for NativeServer; or None
     R: int
     C: int
 
@@ -453,3 +454,151 @@ def latency_stats(jobs):
             "queue_p50_ms": float(np.percentile(wait, 50)), "queue_p99_ms": float(np.percentile(wait, 99)),
             "service_p50_ms": float(np.percentile(serv, 50)), "service_p99_ms": float(np.percentile(serv, 99)),
             "max_ms": float(lat.max()), "columns": int(cols), "columns_per_s": cols / span, "span_s": span}
+
+
+class NativeServer:
+    """The library's serving engine (subby_server_*): continuous batching run
+    by a C++ engine thread, so the Python side only submits descriptors and
+    collects results.  Short A = 4 jobs that wait together run as one launch
+    of the persistent packed kernel over their (job, column-tile) queue.
+
+    ``submit(job)`` takes a ``Job`` with a reversible model whose alignment
+    is ``HostRows`` (rows of a pinned host buffer) or a pinned / device int32
+    torch tensor (R, C); ``collect(timeout_ms)`` returns the jobs completed
+    since the last call, with ``start`` / ``finish`` on the arrival clock and
+    ``result`` numpy views of pinned blocks that ``Job.release()`` hands back
+    to the engine.
+    """
+
+    def __init__(self, max_inflight: int = 8, device_budget: int = 64 << 30, pinned_prewarm: int = 0,
+                 **settings):
+        """``settings``: scheduling parameters of subby_server_set (short_ms,
+        slice_ms, wave_cols, aging, short_slots, plan_cache, pack,
+        pack_max_jobs)."""
+        self._lib = _lib.load()
+        h = ct.c_void_p()
+        _lib.check(self._lib.subby_server_create(max_inflight, device_budget, pinned_prewarm, ct.byref(h)),
+                   "subby_server_create")
+        self._h = h
+        for k, v in settings.items():
+            _lib.check(self._lib.subby_server_set(h, k.encode(), float(v)), f"subby_server_set({k})")
+        self._jobs = {}
+        self._next = 0
+        self._res = (_lib.JobResult * 256)()
+        self.t0 = 0.0   # server-clock time of arrival 0
+
+    def clock(self) -> float:
+        return float(self._lib.subby_server_clock(self._h))
+
+    def start_clock(self):
+        """Arrival times of submitted jobs count from now."""
+        self.t0 = self.clock()
+
+    def submit(self, job: Job, arrival: float = None):
+        m = ensure_diag(job.model)
+        if np.iscomplexobj(np.asarray(m.eigenvalues)) or hasattr(m, "eigenvectors_inv"):
+            raise ValueError("NativeServer takes reversible models; irreversible jobs run on Server")
+        par = np.ascontiguousarray(job.tree.parentIndex, dtype=np.int32)
+        dist = np.ascontiguousarray(job.tree.distanceToParent, dtype=np.float64)
+        ev, V, pi = (np.ascontiguousarray(np.asarray(x), dtype=np.float64) for x in (m.eigenvalues, m.eigenvectors, m.pi))
+        a = job.alignment
+        rowmap = None
+        if isinstance(a, HostRows):
+            R, C = a.R, a.C
+            ptr = a.base.data_ptr() + 4 * int(a.col0)
+            pitch = int(a.base.stride(0))
+            if a.rowmap is not None:
+                rm = a.rowmap
+                rowmap = np.ascontiguousarray(rm.cpu().numpy() if hasattr(rm, "cpu") else rm, dtype=np.int32)
+        else:
+            import torch
+            if not isinstance(a, torch.Tensor) or not (a.is_cuda or a.is_pinned()) or a.dtype != torch.int32 \
+                    or a.dim() != 2 or a.stride(1) != 1:
+                raise ValueError("NativeServer jobs take HostRows or a pinned / CUDA int32 (R, C) tensor")
+            R, C = int(a.shape[0]), int(a.shape[1])
+            ptr, pitch = a.data_ptr(), int(a.stride(0))
+        want = sum(bit for k, bit in (("logLike", _lib.WANT_LOGLIKE), ("counts", _lib.WANT_COUNTS),
+                                      ("rootProb", _lib.WANT_ROOTPROB)) if k in job.want)
+        if isinstance(job.branch_mask, str):
+            mask_mode = _lib.MASK_AUTO
+        elif job.branch_mask is None:
+            mask_mode = _lib.MASK_NONE
+        else:
+            raise ValueError("NativeServer: branch_mask must be 'auto' or None")
+        tag = self._next
+        self._next += 1
+        d = _lib.Job(par.ctypes.data, dist.ctypes.data, len(par), ev.ctypes.data, V.ctypes.data, pi.ctypes.data,
+                     len(pi), ptr, pitch, None if rowmap is None else rowmap.ctypes.data, C, want,
+                     _lib.COUNTS_F81 if job.f81 else _lib.COUNTS_EIGEN, mask_mode,
+                     -1.0 if arrival is None else self.t0 + float(arrival), tag)
+        _lib.check(self._lib.subby_server_submit(self._h, ct.byref(d)), "subby_server_submit")
+        job._A, job._C = len(pi), C
+        self._jobs[tag] = job
+
+    def collect(self, timeout_ms: int = 0):
+        n = ct.c_int(0)
+        _lib.check(self._lib.subby_server_wait(self._h, self._res, len(self._res), int(timeout_ms), ct.byref(n)),
+                   "subby_server_wait")
+        out = []
+        for i in range(n.value):
+            r = self._res[i]
+            job = self._jobs.pop(r.tag)
+            A, C = job._A, job._C
+            job.start = r.t_start - self.t0
+            job.finish = r.t_finish - self.t0
+            if r.status != _lib.OK:
+                job.error = f"{self._lib.subby_strerror(r.status).decode()} ({r.status})"
+            res = {}
+            for key, p, shape in (("logLike", r.logLike, (C,)), ("counts", r.counts, (A, A, C)),
+                                  ("rootProb", r.rootProb, (A, C))):
+                if p:
+                    n_el = int(np.prod(shape))
+                    res[key] = np.ctypeslib.as_array((ct.c_float * n_el).from_address(p)).reshape(shape)
+            job.result = res
+            handle = int(r.handle)
+            job._give_back = lambda blocks, h=handle: self._lib.subby_server_release(self._h, h)
+            job._pinned = [handle]
+            out.append(job)
+        return out
+
+    def stats(self):
+        b, p, i, w = ct.c_double(), ct.c_int(), ct.c_int(), ct.c_int()
+        pj, pl = ct.c_longlong(), ct.c_longlong()
+        self._lib.subby_server_stats(self._h, ct.byref(b), ct.byref(p), ct.byref(i), ct.byref(w), ct.byref(pj),
+                                     ct.byref(pl))
+        return {"engine_busy_s": b.value, "plans_cached": p.value, "inflight": i.value, "waiting": w.value,
+                "packed_jobs": pj.value, "packed_launches": pl.value}
+
+    def run(self, jobs, realtime: bool = True, on_done=None):
+        """Submit ``jobs`` at their arrival times (all at once when not
+        realtime), collect them as they complete; returns the completed jobs."""
+        pending = collections.deque(sorted(jobs, key=lambda j: j.arrival))
+        self.start_clock()
+        t0 = time.perf_counter()
+        done, outstanding = [], 0
+        while pending or outstanding:
+            now = time.perf_counter() - t0
+            while pending and (not realtime or pending[0].arrival <= now):
+                j = pending.popleft()
+                self.submit(j, arrival=j.arrival if realtime else None)
+                if not realtime:
+                    j.arrival = self.clock() - self.t0
+                outstanding += 1
+            wait_ms = 0 if pending and realtime and pending[0].arrival - now < 0.002 else 1
+            for j in self.collect(timeout_ms=wait_ms):
+                outstanding -= 1
+                done.append(j)
+                if on_done is not None:
+                    on_done(j)
+        return done
+
+    def close(self):
+        if getattr(self, "_h", None) and self._h.value:
+            self._lib.subby_server_destroy(self._h)
+            self._h = ct.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:  # noqa: BLE001
+            pass

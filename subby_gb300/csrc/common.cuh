@@ -166,6 +166,10 @@ struct T4Queue {
 };
 int launch_tree4_packed(const T4Queue &q, bool f81, int mask_mode, int grid, int block, size_t smem,
                         cudaStream_t s);
+// Row-strided copy by the SMs (k_token.cu): rows x width bytes (width a
+// multiple of 4), e.g. device results into pinned host memory.
+int launch_copy_rows(void *dst, size_t dpitch, const void *src, size_t spitch, size_t width, int rows,
+                     cudaStream_t s);
 // Load the counts variants of the A = 4 kernel into the current context
 // (cudaFuncGetAttributes), so that a later launch needs no module loading.
 int preload_tree4();

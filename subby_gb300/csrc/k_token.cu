@@ -106,3 +106,45 @@ extern "C" int subby_gather_rows(const int32_t *src, int64_t pitch, const int32_
   subby::k_gather_rows<<<dim3(gx, R), block, 0, (cudaStream_t)stream_>>>(src, pitch, rowmap, C, dst);
   return cudaGetLastError() == cudaSuccess ? SUBBY_OK : SUBBY_ERR_CUDA;
 }
+
+// Row-strided copy run by the SMs (device memory to pinned host memory in
+// the serving engine): dst[r * dpitch + i] = src[r * spitch + i] for byte i
+// < width.  Unlike a copy-engine transfer, whose queue is served in order,
+// its CTAs are scheduled like any kernel's, so the result copies of short
+// jobs (on high-priority streams) are not held behind multi-gigabyte copies
+// of long ones.  Rows whose addresses and width are 16-byte aligned move as
+// 16-byte vectors, others as 4-byte words (all uses copy float32 arrays).
+namespace subby {
+namespace {
+
+__global__ void k_copy_rows(char *__restrict__ dst, size_t dpitch, const char *__restrict__ src, size_t spitch,
+                            size_t width) {
+  char *d = dst + (size_t)blockIdx.y * dpitch;
+  const char *s = src + (size_t)blockIdx.y * spitch;
+  const size_t step = (size_t)gridDim.x * blockDim.x;
+  if (((reinterpret_cast<uintptr_t>(d) | reinterpret_cast<uintptr_t>(s) | width) & 15) == 0) {
+    const size_t nv = width >> 4;
+    for (size_t v = (size_t)blockIdx.x * blockDim.x + threadIdx.x; v < nv; v += step)
+      reinterpret_cast<int4 *>(d)[v] = reinterpret_cast<const int4 *>(s)[v];
+  } else {
+    const size_t nw = width >> 2;
+    for (size_t v = (size_t)blockIdx.x * blockDim.x + threadIdx.x; v < nw; v += step)
+      reinterpret_cast<int *>(d)[v] = reinterpret_cast<const int *>(s)[v];
+  }
+}
+
+}  // namespace
+
+int launch_copy_rows(void *dst, size_t dpitch, const void *src, size_t spitch, size_t width, int rows,
+                     cudaStream_t s) {
+  if (rows <= 0 || width == 0) return 0;
+  if ((width & 3) || rows > 65535) return (int)cudaErrorInvalidValue;
+  const int block = 256;
+  const size_t per_cta = (size_t)block * 16 * 4;  // four 16-byte vectors per thread
+  const int gx = (int)std::max<size_t>(1, std::min<size_t>(1024, (width + per_cta - 1) / per_cta));
+  k_copy_rows<<<dim3(gx, rows), block, 0, s>>>(static_cast<char *>(dst), dpitch, static_cast<const char *>(src),
+                                               spitch, width);
+  return (int)cudaGetLastError();
+}
+
+}  // namespace subby

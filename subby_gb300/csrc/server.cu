@@ -68,12 +68,23 @@ namespace {
 
 using Clock = std::chrono::steady_clock;
 
-// Device time per (column x tree node), ns, of Counts by path on GB300; used
-// only to order and slice work, never to skip any.
+// Kernel time per (column x tree node), ns, of Counts by path on GB300
+// (measured: A = 4 R = 255, A = 20 R = 399, A = 64 R = 127 workloads), plus
+// the host-link time of the job's tokens and results; used only to order
+// and slice work, never to skip any.
 double ns_per_col_node(int A, bool f81) {
   if (A <= 8) return f81 ? 0.011 : 0.012;
-  if (A <= 20) return f81 ? 0.05 : 0.20;
-  return f81 ? 0.30 : 1.6;
+  if (A <= 20) return f81 ? 0.10 : 0.30;
+  return f81 ? 0.70 : 1.6;
+}
+double job_cost_ms(const subby_job &d) {
+  const bool f81 = d.counts_kind == SUBBY_COUNTS_F81 && (d.want & SUBBY_WANT_COUNTS);
+  const double kern = ns_per_col_node(d.A, f81) * d.R * (double)d.C * 1e-6;
+  const double out_b = 4.0 * d.C * (((d.want & SUBBY_WANT_LOGLIKE) ? 1 : 0) +
+                                    ((d.want & SUBBY_WANT_COUNTS) ? d.A * d.A : 0) +
+                                    ((d.want & SUBBY_WANT_ROOTPROB) ? d.A : 0));
+  const double in_b = 4.0 * d.R * (double)d.C;
+  return kern + out_b / 1.7e8 + in_b / 2.0e8;  // ~170 GB/s out, ~200 GB/s in
 }
 
 uint64_t fnv(uint64_t h, const void *p, size_t n) {
@@ -376,17 +387,17 @@ int launch(subby_server *S, SJob *j) {
     rc = subby_plan_run(plan, s_aln, cc, s_ll, s_ct, s_rp, d.counts_kind, d.mask_mode, nullptr,
                         SUBBY_DEVICE_PTRS, st);
     if (rc) return bail(rc);
-    // this slice's outputs into columns [c0, c0 + cc) of the host outputs
-    cudaError_t e = cudaSuccess;
-    if (wl)
-      e = cudaMemcpyAsync(static_cast<float *>(j->out[0]) + c0, s_ll, (size_t)4 * cc, cudaMemcpyDeviceToHost, st);
-    if (e == cudaSuccess && wc)
-      e = cudaMemcpy2DAsync(static_cast<float *>(j->out[1]) + c0, (size_t)4 * C, s_ct, (size_t)4 * cc,
-                            (size_t)4 * cc, (size_t)A * A, cudaMemcpyDeviceToHost, st);
-    if (e == cudaSuccess && wr)
-      e = cudaMemcpy2DAsync(static_cast<float *>(j->out[2]) + c0, (size_t)4 * C, s_rp, (size_t)4 * cc,
-                            (size_t)4 * cc, (size_t)A, cudaMemcpyDeviceToHost, st);
-    if (e != cudaSuccess) return bail(SUBBY_ERR_CUDA);
+    // this slice's outputs into columns [c0, c0 + cc) of the host outputs,
+    // copied by the SMs so that other jobs' copies interleave with them
+    int e = 0;
+    if (wl) e = subby::launch_copy_rows(static_cast<float *>(j->out[0]) + c0, 0, s_ll, 0, (size_t)4 * cc, 1, st);
+    if (!e && wc)
+      e = subby::launch_copy_rows(static_cast<float *>(j->out[1]) + c0, (size_t)4 * C, s_ct, (size_t)4 * cc,
+                                  (size_t)4 * cc, A * A, st);
+    if (!e && wr)
+      e = subby::launch_copy_rows(static_cast<float *>(j->out[2]) + c0, (size_t)4 * C, s_rp, (size_t)4 * cc,
+                                  (size_t)4 * cc, A, st);
+    if (e) return bail(SUBBY_ERR_CUDA);
   }
   if (subby::plan_status_async(plan, sl.h_err, st)) return bail(SUBBY_ERR_CUDA);
   if (cudaEventRecord(sl.done, st) != cudaSuccess) return bail(SUBBY_ERR_CUDA);
@@ -523,13 +534,12 @@ int launch_batch(subby_server *S, std::vector<SJob *> &batch) {
     SJob *j = taken[i];
     const KParams &k = hkp[i];
     const subby_job &d = j->d;
-    if (k.logL) e = cudaMemcpyAsync(j->out[0], k.logL, (size_t)4 * d.C, cudaMemcpyDeviceToHost, st);
-    if (e == cudaSuccess && k.counts)
-      e = cudaMemcpyAsync(j->out[1], k.counts, (size_t)64 * d.C, cudaMemcpyDeviceToHost, st);
-    if (e == cudaSuccess && k.rootp)
-      e = cudaMemcpyAsync(j->out[2], k.rootp, (size_t)16 * d.C, cudaMemcpyDeviceToHost, st);
-    if (e == cudaSuccess && subby::plan_mark_used(taken_plans[i], st) != 0) e = cudaErrorUnknown;
-    if (e != cudaSuccess) return bail(SUBBY_ERR_CUDA);
+    int ce = 0;
+    if (k.logL) ce = subby::launch_copy_rows(j->out[0], 0, k.logL, 0, (size_t)4 * d.C, 1, st);
+    if (!ce && k.counts) ce = subby::launch_copy_rows(j->out[1], 0, k.counts, 0, (size_t)64 * d.C, 1, st);
+    if (!ce && k.rootp) ce = subby::launch_copy_rows(j->out[2], 0, k.rootp, 0, (size_t)16 * d.C, 1, st);
+    if (!ce && subby::plan_mark_used(taken_plans[i], st) != 0) ce = 1;
+    if (ce) return bail(SUBBY_ERR_CUDA);
   }
   if (cudaMemcpyAsync(sl.h_err, d_q + 3, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
       cudaEventRecord(sl.done, st) != cudaSuccess)
@@ -746,7 +756,7 @@ int subby_server_submit(subby_server *S, const subby_job *d) {
   j->d.distances = j->d.eigenvalues = j->d.eigenvectors = j->d.pi = nullptr;
   j->d.row_map = nullptr;
   j->key = job_key(*j);
-  j->cost_ms = ns_per_col_node(A, d->counts_kind == SUBBY_COUNTS_F81) * R * (double)d->C * 1e-6;
+  j->cost_ms = job_cost_ms(*d);
   j->bytes = job_bytes(R, d->C, A);
   {
     std::lock_guard<std::mutex> g(S->mu);

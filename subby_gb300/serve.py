@@ -120,14 +120,15 @@ STAGE_CAP = 4 << 30   # per-plan staging cap of the large-alphabet path (bytes)
 
 # Device time per (column x tree node), ns, by path (GB300, Counts): used only
 # to order and slice work, never to skip any.
-_NS_PER_COL_NODE = {("4", False): 0.012, ("4", True): 0.011, ("16", False): 0.20, ("16", True): 0.05,
-                    ("64", False): 1.6, ("64", True): 0.30}
+_NS_PER_COL_NODE = {("4", False): 0.012, ("4", True): 0.011, ("16", False): 0.30, ("16", True): 0.10,
+                    ("64", False): 1.6, ("64", True): 0.70}
 
 
 def job_cost_ms(R: int, C: int, A: int, f81: bool = False) -> float:
-    """Estimated device time of one job's Counts call (ms)."""
+    """Estimated device time of one job's Counts call (ms): kernels, plus
+    the host-link time of its tokens (~200 GB/s) and counts (~170 GB/s)."""
     key = ("4" if A <= 8 else "16" if A <= 20 else "64", bool(f81))
-    return _NS_PER_COL_NODE[key] * R * C * 1e-6
+    return _NS_PER_COL_NODE[key] * R * C * 1e-6 + 4.0 * C * A * A / 1.7e8 + 4.0 * R * C / 2.0e8
 
 
 def job_device_bytes(R: int, C: int, A: int) -> int:

@@ -153,3 +153,23 @@ def test_c3_full_size_run_vs_oracle_subsample(precision64, sel, mask):
     assert_loglike(r['logLike'][ii].cpu().numpy(), ref["ll"])
     assert_cols(r['counts'][:, :, ii].cpu().numpy(), ref[mask], COUNTS_RTOL, f"c3 counts mask={mask}")
     assert_cols(r['rootProb'][:, ii].cpu().numpy(), ref["rp"], ROOTPROB_RTOL, "c3 rootProb")
+
+
+def test_c4_gradient_device_memory_is_bounded_in_the_column_count(grad20):
+    """The adjoint's per-branch staging runs in column chunks of at most
+    4 GiB, so past that cap the plan's device memory grows with C only by
+    the uploaded tokens: 2 x 10^5 columns hold the 10^5-column workspace plus
+    the extra alignment (and the gradient of the doubled alignment is twice
+    the gradient)."""
+    w = grad20
+    aln = w['alignment']
+    plan = sg.Plan(w['tree'], w['model'])
+    _, t1, G1 = plan.grad(aln)
+    b1 = plan.device_bytes()
+    _, t2, G2 = plan.grad(np.ascontiguousarray(np.concatenate([aln, aln], axis=1)))
+    b2 = plan.device_bytes()
+    plan.close()
+    assert b2 - b1 <= 1.5 * aln.nbytes + (64 << 20), (b1, b2, aln.nbytes)
+    assert b1 < (5 << 30)
+    _close(t2, 2 * t1, "d/dt of the doubled alignment", rtol=1e-4)
+    _close(G2, 2 * G1, "d/dS of the doubled alignment", rtol=1e-4)

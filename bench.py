@@ -699,8 +699,18 @@ def serving_block(args):
         return out
 
     jobs, warm = build(desc), build(wdesc)
+    # work-item shape of the packed A = 4 kernel, tuned on this device
+    fd, tune_path = tempfile.mkstemp(suffix=".json")
+    os.close(fd)
+    t_tune = time.perf_counter()
+    tuned = serve.autotune_packed(cache=tune_path)
+    t_tune = time.perf_counter() - t_tune
+    with open(tune_path) as f:
+        tune_record = json.load(f)
     # the library's engine (C++ thread): Python only submits and collects
-    srv = serve.NativeServer(max_inflight=8, device_budget=64 << 30, pinned_prewarm=4 << 30)
+    srv = serve.NativeServer(max_inflight=8, device_budget=64 << 30, pinned_prewarm=4 << 30,
+                             autotune_cache=tune_path)
+    os.unlink(tune_path)
     # the consumer takes each result as it lands and hands its buffers back
     srv.run(warm, realtime=False, on_done=lambda j: j.release())
     eng0 = srv.stats()
@@ -744,6 +754,7 @@ def serving_block(args):
             "service_p50_ms": st['service_p50_ms'], "service_p99_ms": st['service_p99_ms'],
             "columns_per_s": st['columns_per_s'], "span_s": st['span_s'], "rate_jobs_per_s": args.rate,
             "h2d_bytes": h2d, "d2h_bytes": d2h, "by_kind": by_kind,
+            "autotune": {"settings": tuned, "wall_ms": tune_record.get("wall_ms"), "seconds": round(t_tune, 2)},
             "host": {"engine_busy_s": round(engine["engine_busy_s"], 3), "wall_s": round(t_run, 3),
                      "plans_cached": engine["plans_cached"], "packed_jobs": engine["packed_jobs"],
                      "packed_launches": engine["packed_launches"],

@@ -340,7 +340,10 @@ int subby_server_release(subby_server *server, int64_t handle);
  * waited; 0.2), "short_slots" (2), "plan_cache" (resident plans; 64),
  * "pack" (1: short A = 4 jobs waiting together run as one launch of the
  * persistent packed kernel over their (job, column-tile) queue; 0: one
- * launch per job), "pack_max_jobs" (64). */
+ * launch per job), "pack_max_jobs" (64), "pack_tiles_r64",
+ * "pack_tiles_r256", "pack_tiles_big" (256-column tiles per packed work item
+ * for trees of up to 64, up to 256 and more nodes; 1; the shape
+ * subby_gb300.serve.autotune_packed chooses). */
 int subby_server_set(subby_server *server, const char *key, double value);
 /* Seconds since the engine was created (the clock of arrival / finish). */
 double subby_server_clock(subby_server *server);

@@ -149,15 +149,16 @@ int launch_acc(const KParams &p, int A, bool f81, bool tc, const float *sa, cons
                int c_count, int grid, cudaStream_t s);
 int launch_tree4(const KParams &p, bool f81, int mask_mode, int grid, int block, size_t smem,
                  cudaStream_t s);
-// Packed queue of (job, column tile) work items of the A = 4 serving kernel
-// (k_tree4_packed): jobs[j] are the tree-kernel parameters of job j, items
-// are (job, first column of a tile of blockDim.x columns).  CTAs claim items
-// with an atomic counter; an item at or past *published is waited for (at
-// most wait_polls polls) until *closed is set, and a wait that gives up
-// increments *err and ends the CTA.
+// Packed queue of (job, column range) work items of the A = 4 serving
+// kernel (k_tree4_packed): jobs[j] are the tree-kernel parameters of job j,
+// items are (job, first column, end column) of a run of whole tiles of
+// blockDim.x columns (how many tiles an item spans is the work-item shape
+// the serving autotuner picks).  CTAs claim items with an atomic counter; an
+// item at or past *published is waited for (at most wait_polls polls) until
+// *closed is set, and a wait that gives up increments *err and ends the CTA.
 struct T4Queue {
   const KParams *jobs;
-  const int2 *items;
+  const int4 *items;
   int *head;
   const int *published;
   const int *closed;

@@ -687,7 +687,7 @@ __global__ void __launch_bounds__(256, 1) k_tree4_packed(const T4Queue Q) {
     __syncthreads();
     const int it = s_item;
     if (it < 0) break;
-    const int2 w = Q.items[it];
+    const int4 w = Q.items[it];
     const KParams &P = Q.jobs[w.x];
     if (w.x != loaded) {
       // every thread is past the previous item (barrier above)
@@ -697,7 +697,7 @@ __global__ void __launch_bounds__(256, 1) k_tree4_packed(const T4Queue Q) {
       __syncthreads();
       loaded = w.x;
     }
-    t4_cols<F81, MASK, kOutSum>(P, sm, tb, w.y + (int)threadIdx.x - lane);
+    for (int c0 = w.y; c0 < w.z; c0 += nb) t4_cols<F81, MASK, kOutSum>(P, sm, tb, c0 + (int)threadIdx.x - lane);
     __syncthreads();  // s_item and, on a job change, the tables are rewritten next
   }
   asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");

@@ -192,6 +192,9 @@ struct subby_server {
   int wave_cols = 0;   // slice granularity in columns (0: one wave of the kernels' grids)
   bool pack = true;    // short A = 4 jobs waiting together share one packed launch
   int pack_max_jobs = 64;
+  // tiles of 256 columns per packed work item, by tree size (R <= 64, <= 256,
+  // larger): the item shape the serving autotuner picks
+  int pack_tiles_r[3] = {1, 1, 1};
   long long pack_max_cols = 152LL * 256 * 16;
   Clock::time_point t0;
   cudaMemPool_t pool = nullptr;
@@ -405,6 +408,8 @@ int launch(subby_server *S, SJob *j) {
   return SUBBY_OK;
 }
 
+int pack_tiles(const subby_server *S, int R) { return S->pack_tiles_r[R <= 64 ? 0 : R <= 256 ? 1 : 2]; }
+
 bool packable(const subby_server *S, const SJob *j) {
   return S->pack && !j->nopack && j->d.A == 4 && j->d.R >= 2 && j->cost_ms <= S->short_ms;
 }
@@ -457,7 +462,7 @@ int launch_batch(subby_server *S, std::vector<SJob *> &batch) {
   const size_t o_kp = off;
   off += align256(sizeof(KParams) * n);
   const size_t o_items = off;
-  off += align256(sizeof(int2) * ntiles);
+  off += align256(sizeof(int4) * ntiles);
   const size_t o_ints = off;
   off += 256;
   if (grow_arena(S, sl, off, st)) return bail(SUBBY_ERR_NOMEM);
@@ -475,7 +480,7 @@ int launch_batch(subby_server *S, std::vector<SJob *> &batch) {
   }
   char *hs = static_cast<char *>(sl.h_stage);
   KParams *hkp = reinterpret_cast<KParams *>(hs);
-  int2 *hit = reinterpret_cast<int2 *>(hs + (o_items - o_kp));
+  int4 *hit = reinterpret_cast<int4 *>(hs + (o_items - o_kp));
   int *hq = reinterpret_cast<int *>(hs + (o_ints - o_kp));
   char *hrm = hs + (o_ints + 256 - o_kp);
   size_t smem = 0;
@@ -509,7 +514,8 @@ int launch_batch(subby_server *S, std::vector<SJob *> &batch) {
     }
     const int rc = subby_gather_rows(d.alignment, d.pitch, rowmap, d.R, d.C, d_tok, st);
     if (rc) return bail(rc);
-    for (int c0 = 0; c0 < d.C; c0 += 256) hit[nit++] = make_int2(njobs, c0);
+    const int span = 256 * pack_tiles(S, d.R);
+    for (int c0 = 0; c0 < d.C; c0 += span) hit[nit++] = make_int4(njobs, c0, std::min(d.C, c0 + span), 0);
     const bool want_k[3] = {d_ll != nullptr, d_ct != nullptr, d_rp != nullptr};
     const size_t n_out[3] = {(size_t)4 * d.C, (size_t)64 * d.C, (size_t)16 * d.C};
     for (int k = 0; k < 3; ++k)
@@ -526,7 +532,7 @@ int launch_batch(subby_server *S, std::vector<SJob *> &batch) {
   cudaError_t e = cudaMemcpyAsync(base + o_kp, hs, o_ints + 256 - o_kp, cudaMemcpyHostToDevice, st);
   if (e != cudaSuccess) return bail(SUBBY_ERR_CUDA);
   int *d_q = reinterpret_cast<int *>(base + o_ints);
-  const T4Queue q{reinterpret_cast<const KParams *>(base + o_kp), reinterpret_cast<const int2 *>(base + o_items),
+  const T4Queue q{reinterpret_cast<const KParams *>(base + o_kp), reinterpret_cast<const int4 *>(base + o_items),
                   d_q, d_q + 1, d_q + 2, 1, d_q + 3};
   const int grid = (int)std::min<long long>(nit, S->nsm);
   if (subby::launch_tree4_packed(q, f81, mask, grid, 256, smem, st) != 0) return bail(SUBBY_ERR_CUDA);
@@ -821,6 +827,9 @@ int subby_server_set(subby_server *S, const char *key, double value) {
   else if (k == "plan_cache" && value >= 1) S->plan_cache = (int)value;
   else if (k == "pack") S->pack = value != 0;
   else if (k == "pack_max_jobs" && value >= 1 && value <= 4096) S->pack_max_jobs = (int)value;
+  else if (k == "pack_tiles_r64" && value >= 1 && value <= 64) S->pack_tiles_r[0] = (int)value;
+  else if (k == "pack_tiles_r256" && value >= 1 && value <= 64) S->pack_tiles_r[1] = (int)value;
+  else if (k == "pack_tiles_big" && value >= 1 && value <= 64) S->pack_tiles_r[2] = (int)value;
   else return SUBBY_ERR_ARG;
   return SUBBY_OK;
 }

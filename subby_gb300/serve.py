@@ -472,10 +472,14 @@ class NativeServer:
     """
 
     def __init__(self, max_inflight: int = 8, device_budget: int = 64 << 30, pinned_prewarm: int = 0,
-                 **settings):
+                 autotune_cache: str = None, **settings):
         """``settings``: scheduling parameters of subby_server_set (short_ms,
         slice_ms, wave_cols, aging, short_slots, plan_cache, pack,
-        pack_max_jobs)."""
+        pack_max_jobs, pack_tiles_*).  ``autotune_cache``: a file written by
+        ``autotune_packed`` whose work-item shapes apply unless ``settings``
+        gives them."""
+        if autotune_cache is not None:
+            settings = {**load_autotune(autotune_cache), **settings}
         self._lib = _lib.load()
         h = ct.c_void_p()
         _lib.check(self._lib.subby_server_create(max_inflight, device_budget, pinned_prewarm, ct.byref(h)),
@@ -603,3 +607,79 @@ class NativeServer:
             self.close()
         except Exception:  # noqa: BLE001
             pass
+
+
+# ---------------------------------------------------------------------------
+# autotuner of the packed kernel's work-item shape
+# ---------------------------------------------------------------------------
+
+PACK_TILE_KEYS = (("pack_tiles_r64", 24), ("pack_tiles_r256", 96), ("pack_tiles_big", 300))
+
+
+def default_autotune_cache() -> str:
+    import os
+    return os.environ.get("SUBBY_AUTOTUNE_CACHE",
+                          os.path.join(os.path.expanduser("~"), ".cache", "subby_gb300", "autotune.json"))
+
+
+def autotune_packed(cache: str = None, candidates=(1, 2, 4, 8), n_jobs: int = 48, trials: int = 3,
+                    seed: int = 0) -> dict:
+    """Choose the packed A = 4 kernel's work-item shape — how many 256-column
+    tiles one claimed item spans — for small, medium and large trees, by
+    timing each candidate on the device, and write the choice to ``cache``
+    (JSON; default ``$SUBBY_AUTOTUNE_CACHE`` or ~/.cache/subby_gb300/
+    autotune.json).  Larger items amortise the per-item claim and table
+    reload; smaller ones balance the CTAs better.  Per bucket: ``n_jobs``
+    HKY85 jobs on random trees of about the bucket's size, C log-uniform in
+    100..20000, uniform tokens with 5% gaps, submitted together so they run
+    as packed batches; the median wall time over ``trials`` runs of one
+    engine per candidate decides.  Returns the settings dict."""
+    import json
+    import os
+    import torch
+    from . import synth, models
+    rng = np.random.default_rng(seed)
+    out, measured = {}, {}
+    for key, leaves in PACK_TILE_KEYS:
+        jobs = []
+        for i in range(n_jobs):
+            tree = synth.random_tree(int(leaves * rng.uniform(0.7, 1.3)), 0.1, rng)
+            model = models.hky85_diag(2.0, rng.dirichlet(np.ones(4)))
+            C = int(np.exp(rng.uniform(np.log(100), np.log(20000))))
+            tok = rng.integers(0, 80, size=(len(tree.parentIndex), C))
+            aln = torch.from_numpy(np.where(tok < 76, tok % 4, 5).astype(np.int32)).pin_memory()
+            jobs.append((tree, model, aln))
+        times = {}
+        for k in candidates:
+            srv = NativeServer(max_inflight=2, device_budget=16 << 30, **{key: k})
+            ts = []
+            for t in range(trials + 1):
+                batch = [Job(id=i, alignment=a, tree=tr, model=m, want=("counts",)) for i, (tr, m, a) in
+                         enumerate(jobs)]
+                t0 = time.perf_counter()
+                done = srv.run(batch, realtime=False, on_done=lambda j: j.release())
+                dt = time.perf_counter() - t0
+                if any(j.error for j in done):
+                    raise RuntimeError("autotune run failed: " + next(j.error for j in done if j.error))
+                if t > 0:          # the first run builds the plans
+                    ts.append(dt)
+            srv.close()
+            times[k] = float(np.median(ts))
+        out[key] = int(min(times, key=times.get))
+        measured[key] = {str(k): round(v * 1e3, 3) for k, v in times.items()}
+    cache = cache or default_autotune_cache()
+    os.makedirs(os.path.dirname(os.path.abspath(cache)), exist_ok=True)
+    with open(cache, "w") as f:
+        json.dump({"settings": out, "wall_ms": measured, "device": torch.cuda.get_device_name()}, f, indent=1)
+    return out
+
+
+def load_autotune(cache: str = None) -> dict:
+    """Settings of a previous autotune_packed run ({} when there is none)."""
+    import json
+    import os
+    cache = cache or default_autotune_cache()
+    if not os.path.exists(cache):
+        return {}
+    with open(cache) as f:
+        return dict(json.load(f).get("settings", {}))

@@ -313,3 +313,45 @@ def test_packed_kernel_queue_wait_gives_up_and_reports_timeout():
     assert not d[0].error
     np.testing.assert_array_equal(d[0].result['counts'], _alone(j)['counts'])
     srv.close()
+
+
+def test_packed_work_item_shapes_give_identical_results():
+    """Items spanning 1 or 3 tiles of 256 columns (the autotuned shape): each
+    job's results equal its single call bit for bit."""
+    rng = np.random.default_rng(13)
+    jobs = []
+    for i in range(12):
+        tree = synth.random_tree(int(rng.integers(3, 200)), 0.1, rng)
+        model = sg.models.hky85_diag(2.0, rng.dirichlet(np.ones(4)))
+        aln = synth.simulated_alignment(tree, model, int(rng.integers(1, 5000)), 0.1, rng)
+        jobs.append((tree, model, aln))
+    for tiles in (1, 3):
+        srv = serve.NativeServer(max_inflight=2, device_budget=1 << 30, pack_tiles_r64=tiles,
+                                 pack_tiles_r256=tiles, pack_tiles_big=tiles)
+        batch = []
+        for i, (tree, model, aln) in enumerate(jobs):
+            j = serve.Job(id=i, alignment=_pinned(aln), tree=tree, model=model, want=("logLike", "counts"))
+            j.host = aln
+            batch.append(j)
+        done = srv.run(batch, realtime=False)
+        assert srv.stats()["packed_jobs"] == len(jobs)
+        for j in done:
+            assert not j.error
+            ref = _alone(j)
+            for k in ("logLike", "counts"):
+                np.testing.assert_array_equal(j.result[k], ref[k])
+            j.release()
+        srv.close()
+
+
+def test_autotune_packed_writes_and_applies_its_choice(tmp_path):
+    cache = str(tmp_path / "autotune.json")
+    got = serve.autotune_packed(cache=cache, candidates=(1, 4), n_jobs=6, trials=1)
+    assert set(got) == {k for k, _ in serve.PACK_TILE_KEYS} and set(got.values()) <= {1, 4}
+    assert serve.load_autotune(cache) == got
+    j = _native_jobs(n=1, seed=3)[0]
+    srv = serve.NativeServer(max_inflight=2, device_budget=1 << 30, autotune_cache=cache)
+    d = srv.run([j], realtime=False)
+    assert not d[0].error
+    np.testing.assert_array_equal(d[0].result['counts'], _alone(j)['counts'])
+    srv.close()

@@ -321,7 +321,9 @@ def test_packed_work_item_shapes_give_identical_results():
     rng = np.random.default_rng(13)
     jobs = []
     for i in range(12):
-        tree = synth.random_tree(int(rng.integers(3, 200)), 0.1, rng)
+        # trees whose tables fit the A = 4 kernel's shared memory (larger
+        # ones take the one-job path)
+        tree = synth.random_tree(int(rng.integers(3, 70)), 0.1, rng)
         model = sg.models.hky85_diag(2.0, rng.dirichlet(np.ones(4)))
         aln = synth.simulated_alignment(tree, model, int(rng.integers(1, 5000)), 0.1, rng)
         jobs.append((tree, model, aln))

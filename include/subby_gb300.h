@@ -186,6 +186,13 @@ int subby_gather_rows(const int32_t *src, int64_t pitch, const int32_t *rowmap, 
  * (device-pointer runs return before their kernels finish, so they report
  * it here); clears the record.  No counterpart in the reference. */
 int subby_plan_status(subby_plan *plan);
+/* Replace the root prior (A positive values, host FP64) of a reversible
+ * plan; the model's pi still defines M(t) and the eigenbasis.  This is the
+ * root prior of subby.jax InsideOutside over a per-column model list, which
+ * takes the first model's pi for every column (subby/jax/__init__.py:
+ * 721-731, rootProb = stacked.pi[0]); the posteriors, LogLike and RootProb
+ * of later runs use it.  Ordered after the plan's enqueued work. */
+int subby_plan_set_root_prior(subby_plan *plan, const double *root_prior);
 /* Release the plan's workspace (staging, scratch, host-call buffers) in
  * stream order after its last enqueued kernel; the tables stay.  The next
  * run allocates again (from the library pool).  For servers that keep many

@@ -563,13 +563,16 @@ def _sub_matrices(model, distances):
     return compute_sub_matrices(model, distances)
 
 
-def _inside_outside(alignment, tree, model):
+def _inside_outside(alignment, tree, model, root_prob=None):
     """U, D, scales and M with the root's outside vector set to pi / max(pi),
-    as InsideOutside.__init__ does (oracle.py:1631-1661)."""
+    as InsideOutside.__init__ does (oracle.py:1631-1661).  ``root_prob``
+    replaces the model's pi at the root (subby/jax/__init__.py:721-731: a
+    per-column model list takes the first model's pi for every column)."""
     M = _sub_matrices(model, tree.distanceToParent)
-    U, lnU, lnL = upward_pass(alignment, tree, M, model['pi'])
-    D, lnD = downward_pass(U, lnU, tree, M, model['pi'], alignment)
-    pi = np.asarray(model['pi'], dtype=np.float64)
+    rp = model['pi'] if root_prob is None else root_prob
+    U, lnU, lnL = upward_pass(alignment, tree, M, rp)
+    D, lnD = downward_pass(U, lnU, tree, M, rp, alignment)
+    pi = np.asarray(rp, dtype=np.float64)
     mx = max(float(np.max(pi)), RESCALE_FLOOR)
     D[0] = pi[None, :] / mx
     lnD[0] = np.log(mx)
@@ -582,14 +585,14 @@ def _normalise(x, axes):
     return np.where(tot > 0, x / np.where(tot > 0, tot, 1.0), x)
 
 
-def NodePosterior(alignment, tree, model, node=None):
+def NodePosterior(alignment, tree, model, node=None, root_prob=None):
     """Posterior state distribution of node(s); InsideOutside.node_posterior,
     oracle.py:1755-1831 (subby/jax/__init__.py:868-946).
 
     Root: pi_a U_0a; node n > 0: (sum_a D_na M_n[a, j]) U_nj; times
     exp(logNormU + logNormD - logLike), normalised over the states.
     Returns (A, C) for one node, (R, A, C) for node=None."""
-    M, U, lnU, lnL, D, lnD = _inside_outside(alignment, tree, model)
+    M, U, lnU, lnL, D, lnD = _inside_outside(alignment, tree, model, root_prob)
     scale = np.exp(lnU + lnD - lnL[None, :])                       # (R, C)
     Dt = np.einsum('rca,raj->rcj', D, M)
     Dt[0] = D[0]
@@ -598,13 +601,13 @@ def NodePosterior(alignment, tree, model, node=None):
     return post if node is None else post[node]
 
 
-def BranchPosterior(alignment, tree, model, node=None):
+def BranchPosterior(alignment, tree, model, node=None, root_prob=None):
     """Joint posterior of (parent state i, child state j) on branch(es);
     InsideOutside.branch_posterior, oracle.py:1833-1905
     (subby/jax/__init__.py:948-1040): D_ni M_n[i, j] U_nj exp(logNormD +
     logNormU - logLike), normalised over (i, j).  Returns (A, A, C) for one
     node (> 0), (R, A, A, C) with branch 0 zero for node=None."""
-    M, U, lnU, lnL, D, lnD = _inside_outside(alignment, tree, model)
+    M, U, lnU, lnL, D, lnD = _inside_outside(alignment, tree, model, root_prob)
     scale = np.exp(lnU + lnD - lnL[None, :])
     joint = D[:, :, :, None] * M[:, None, :, :] * U[:, :, None, :] * scale[:, :, None, None]  # (R, C, A, A)
     joint = _normalise(joint, (-2, -1))

@@ -21,7 +21,7 @@ COUNTS_EIGEN, COUNTS_F81 = 0, 1
 EXPORTS = (
     "subby_version", "subby_strerror", "subby_last_error", "subby_plan_create", "subby_plan_create_irrev", "subby_plan_create_rows",
     "subby_plan_destroy", "subby_plan_device_bytes", "subby_plan_trim", "subby_plan_branch_counts",
-    "subby_plan_posteriors", "subby_plan_status", "subby_plan_run", "subby_plan_grad",
+    "subby_plan_posteriors", "subby_plan_status", "subby_plan_set_root_prior", "subby_plan_run", "subby_plan_grad",
     "subby_loglike", "subby_counts", "subby_rootprob", "subby_last_launch_count",
     "subby_debug_set_kernel", "subby_debug_fail_waits", "subby_counts_noalloc", "subby_mixture_posterior",
     "subby_tokenize", "subby_gather_rows", "subby_server_create", "subby_server_submit", "subby_server_wait",
@@ -89,6 +89,8 @@ def _declare(lib):
     lib.subby_plan_device_bytes.argtypes = [_p]
     lib.subby_plan_trim.restype = ct.c_int
     lib.subby_plan_trim.argtypes = [_p]
+    lib.subby_plan_set_root_prior.restype = ct.c_int
+    lib.subby_plan_set_root_prior.argtypes = [_p, _p]
     lib.subby_plan_status.restype = ct.c_int
     lib.subby_plan_status.argtypes = [_p]
     lib.subby_plan_branch_counts.restype = ct.c_int

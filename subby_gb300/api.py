@@ -343,6 +343,17 @@ class Plan:
     def device_bytes(self) -> int:
         return int(_lib.load().subby_plan_device_bytes(self._handle))
 
+    def set_root_prior(self, root_prior):
+        """Use ``root_prior`` (A positive values) instead of the model's pi at
+        the root: the root prior of subby.jax InsideOutside over a
+        per-column model list, the first model's pi for every column
+        (subby/jax/__init__.py:721-731)."""
+        rp = np.ascontiguousarray(root_prior, dtype=np.float64)
+        if rp.shape != (self.A,):
+            raise ValueError(f"root prior must have shape ({self.A},)")
+        with self._lock:
+            _lib.check(_lib.load().subby_plan_set_root_prior(self._handle, _ptr(rp)), "subby_plan_set_root_prior")
+
     def status(self):
         """Raise SubbyError if a bounded device wait of this plan's kernels
         gave up since the last check (waits for the plan's enqueued work)."""
@@ -656,16 +667,42 @@ class InsideOutside:
             return self._each(lambda p, a: p.posteriors(a, node=node, want_node=want_node,
                                                         want_branch=want_branch)[key])
         ms, groups = batch._groups(self._alignment, self._model)
+        # the inside and outside passes of every column take the first
+        # model's pi at the root (subby/jax/__init__.py:721-731: rootProb =
+        # stacked.pi[0]); the root's own posterior row takes the column's own
+        # pi (its outside vector is set from the stacked pis, :763-774)
         pi0 = np.asarray(ms[0].pi, np.float64)
-        if any(not np.array_equal(np.asarray(m.pi, np.float64), pi0) for m, _ in groups):
-            raise NotImplementedError("posteriors of per-column models with different pi are not supported")
         R, A, C = int(self._alignment.shape[0]), len(pi0), int(self._alignment.shape[1])
         lead = (R,) if node is None else ()
         shape = lead + ((A,) if key == 'node' else (A, A)) + (C,)
         out = batch._new(self._alignment, shape)
         for m, idx in groups:
-            r = self._one(m).posteriors(batch._take(self._alignment, idx), node=node, want_node=want_node,
-                                        want_branch=want_branch)[key]
+            same = np.array_equal(np.asarray(m.pi, np.float64), pi0)
+            # a group whose own pi differs runs on a plan of its own with the
+            # shared root prior (cached plans keep their model's pi)
+            plan = self._one(m) if same else Plan(self._tree, ensure_diag(m), _device_of(self._alignment))
+            try:
+                if not same:
+                    plan.set_root_prior(pi0)
+                r = plan.posteriors(batch._take(self._alignment, idx), node=node, want_node=want_node,
+                                    want_branch=want_branch)[key]
+            finally:
+                if not same:
+                    plan.close()
+            if not same and key == 'node' and (node is None or int(node) == 0):
+                # root row: pi0 o U_0 normalised -> pi_g o U_0 normalised
+                # (U_0 does not depend on the root prior)
+                w = np.asarray(m.pi, np.float64) / pi0
+                if _is_torch(r):
+                    import torch
+                    w = torch.as_tensor(w, dtype=r.dtype, device=r.device)
+                row = r[0] if node is None else r
+                row = row * w[:, None]
+                row = row / row.sum(0, keepdims=True) if not _is_torch(row) else row / row.sum(0, keepdim=True)
+                if node is None:
+                    r[0] = row
+                else:
+                    r = row
             batch._put(out, idx, r)
         return out
 

@@ -38,6 +38,8 @@ struct TableOffsets {
   int Vu;    // A x A         : Vu[b][l] = sqrt(pi_b) V[b][l]
   int Vd;    // A x A         : Vd[a][k] = V[a][k] / sqrt(pi_a)
   int Ut;    // (A+1) x A     : Ut[tok][l] = Vu[tok][l], Ut[A][l] = sum_b Vu[b][l]
+  int pi0;   // A             : root prior (pi unless subby_plan_set_root_prior set another);
+             //                 follows V in the small block
   int pi;    // A
   int V;     // A x A         : V[i][k] (FP32 copy)
   int S;     // A x A         : S[i][j] = sum_k V_ik mu_k V_jk

@@ -109,7 +109,7 @@ struct N4 {
 };
 
 // Shared-memory table layout (float offsets), set by the host in KParams:
-//   stab[0] MT   R x 5 x 4      stab[1] small block (Vu, Vd, Ut, pi, S, V)
+//   stab[0] MT   R x 5 x 4      stab[1] small block (Vu, Vd, Ut, pi, S, V, root prior)
 //   stab[2] J    R x 16 (eigen) or F81 R x 4
 //   stab[3] K    R x 5 x 20 (eigen: K_n[code][k][l] = J_n[k][l] Ut[code][l], rows padded)
 //   stab[4] LV   5 x 4 (observation rows), followed by piL[5] (pi . L(code))
@@ -174,7 +174,8 @@ __device__ __forceinline__ void t4_cols(const KParams &P, float *sm, const uint3
   int *swd = reinterpret_cast<int *>(sm + P.smem_words) + threadIdx.x;
   const int C = P.C;
   const int lane = threadIdx.x & 31;
-  const F4 piv = ld4s(pis);
+  const F4 piv = ld4s(pis);           // the model's pi (F81 formulas)
+  const F4 pr0 = ld4s(V32 + 16);      // root prior (pi unless the plan sets another)
   const float mu81 = P.f81_mu;
   const bool valid = c0 + lane < C;
   const int col = valid ? c0 + lane : C - 1;
@@ -281,11 +282,11 @@ __device__ __forceinline__ void t4_cols(const KParams &P, float *sm, const uint3
 #pragma unroll
     for (int q = 0; q < 7; ++q) tk[q] = tn[q];
   }
-  const float Pp = dot4(piv, ur);
+  const float Pp = dot4(pr0, ur);
   if ((P.mode & kModeLogLike) && valid) P.logL[col] = (float)((double)eRoot * kLn2q + (double)logf(Pp));
   const float invP = 1.0f / Pp;
   if ((P.mode & kModeRootProb) && valid) {
-    const F4 q = scale4(mul4(piv, ur), invP);
+    const F4 q = scale4(mul4(pr0, ur), invP);
     P.rootp[col] = q.a.x;
     P.rootp[(size_t)C + col] = q.a.y;
     P.rootp[(size_t)2 * C + col] = q.b.x;
@@ -472,7 +473,7 @@ __device__ __forceinline__ void t4_cols(const KParams &P, float *sm, const uint3
     F4 O;
     int eO, stp;
     if (root) {
-      O = mul4(piv, Lp);
+      O = mul4(pr0, Lp);
       eO = 0;
       stp = iRoot;
     } else {

@@ -190,12 +190,13 @@ extern "C" int subby_counts_noalloc(const int32_t *d_aln, const int32_t *parent,
     return at;
   };
   o.MT = take(R * 20);
-  o.Vu = take(4 * 16 + 20 + 4);
+  o.Vu = take(4 * 16 + 20 + 4 + 4);
   o.Vd = o.Vu + 16;
   o.Ut = o.Vd + 16;
   o.pi = o.Ut + 20;
   o.S = o.pi + 4;
   o.V = o.S + 16;
+  o.pi0 = o.V + 16;
   o.J = take(R * 16);
   o.F81 = take(R * 4);
   o.K = take(R * 100);
@@ -230,7 +231,7 @@ extern "C" int subby_counts_noalloc(const int32_t *d_aln, const int32_t *parent,
     Ut64[16 + l] = s;
   }
   for (int i = 0; i < 20; ++i) T[o.Ut + i] = (float)Ut64[i];
-  for (int a = 0; a < 4; ++a) T[o.pi + a] = (float)pi[a];
+  for (int a = 0; a < 4; ++a) T[o.pi + a] = T[o.pi0 + a] = (float)pi[a];
   for (int n = 0; n < R; ++n) {
     const double t = dist[n];
     double E[4], M[16], J[16];
@@ -303,7 +304,7 @@ extern "C" int subby_counts_noalloc(const int32_t *d_aln, const int32_t *parent,
     sofs += align4(n);
   };
   add(o.MT, R * 20);
-  add(o.Vu, 16 * 4 + 20 + 4);
+  add(o.Vu, 16 * 4 + 20 + 4 + 4);
   if (f81) add(o.F81, R * 4);
   else add(o.J, R * 16);
   if (!f81) add(o.K, R * 100);

@@ -523,14 +523,15 @@ int plan_create(const int32_t *parent, const double *dist, const double *evals, 
     return at;
   };
   o.MT = take(R * (A + 1) * A);
-  // small block, contiguous in this order: Vu, Vd, Ut, pi, S, V
-  const int small_n = A * A + A * A + (A + 1) * A + A + A * A + A * A;
+  // small block, contiguous in this order: Vu, Vd, Ut, pi, S, V, root prior
+  const int small_n = A * A + A * A + (A + 1) * A + A + A * A + A * A + A;
   o.Vu = take(small_n);
   o.Vd = o.Vu + A * A;
   o.Ut = o.Vd + A * A;
   o.pi = o.Ut + (A + 1) * A;
   o.S = o.pi + A;
   o.V = o.S + A * A;
+  o.pi0 = o.V + A * A;
   o.MN = take(R * A * A);
   o.J = take(R * A * A);
   o.JT = take(R * A * A);
@@ -580,7 +581,7 @@ int plan_create(const int32_t *parent, const double *dist, const double *evals, 
     for (int b = 0; b < A; ++b) s += sp[b] * evecs[b * A + l];
     at(o.Ut + A * A + l) = (float)s;
   }
-  for (int a = 0; a < A; ++a) at(o.pi + a) = (float)pi[a];
+  for (int a = 0; a < A; ++a) at(o.pi + a) = at(o.pi0 + a) = (float)pi[a];
 
   // ---- device upload
   auto cleanup = [&](int rc) {
@@ -897,6 +898,31 @@ int subby_plan_status(subby_plan *P) {
   return SUBBY_OK;
 }
 
+int subby_plan_set_root_prior(subby_plan *P, const double *root_prior) {
+  clear_error();
+  if (!P || !root_prior) return fail(SUBBY_ERR_ARG, "null argument");
+  const int A = P->A;
+  std::vector<float> h(A);
+  for (int a = 0; a < A; ++a) {
+    if (!(root_prior[a] > 0.0) || !std::isfinite(root_prior[a]))
+      return fail(SUBBY_ERR_ARG, "root prior entries must be positive and finite");
+    h[a] = (float)root_prior[a];
+  }
+  std::lock_guard<std::mutex> g(P->lock);
+  int cur = 0;
+  cudaGetDevice(&cur);
+  if (cur != P->device) cudaSetDevice(P->device);
+  // after every enqueued use of the tables; later runs wait for `ready`
+  cudaError_t e = P->used ? cudaStreamWaitEvent(P->s_prep, P->last_use, 0) : cudaSuccess;
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(P->d_tab + P->off.pi0, h.data(), sizeof(float) * A, cudaMemcpyHostToDevice, P->s_prep);
+  if (e == cudaSuccess) e = cudaEventRecord(P->ready, P->s_prep);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(P->s_prep);
+  if (cur != P->device) cudaSetDevice(cur);
+  if (e != cudaSuccess) return cuda_fail(e, "root prior upload");
+  return SUBBY_OK;
+}
+
 int subby_plan_trim(subby_plan *P) {
   if (!P) return fail(SUBBY_ERR_ARG, "null plan");
   std::lock_guard<std::mutex> g(P->lock);
@@ -1103,7 +1129,7 @@ int plan_tree4(subby_plan *P, int mode, int C, Launch &L) {
   const TableOffsets &o = P->off;
   const bool f81 = (mode & kModeF81) != 0;
   add(o.MT, R * 20);
-  add(o.Vu, 16 * 4 + 20 + 4);
+  add(o.Vu, 16 * 4 + 20 + 4 + 4);
   if (f81) add(o.F81, R * 4);
   else add(o.J, R * 16);
   if (!f81) add(o.K, R * 100);

@@ -488,6 +488,7 @@ __global__ void __launch_bounds__(128 * Geo<A>::H, 1) k_walk(const KParams P, fl
   const float *Vd = P.tab + P.off.Vd;
   const float *Ut = P.tab + P.off.Ut;
   const float *pig = P.tab + P.off.pi;
+  const float *pr0g = P.tab + P.off.pi0;   // root prior
   const int4 *prog = P.prog;
   const int C = P.C;
   const size_t tile_slots = (size_t)P.nslots * kTile;
@@ -587,7 +588,7 @@ __global__ void __launch_bounds__(128 * Geo<A>::H, 1) k_walk(const KParams P, fl
     // P = pi . U_root (combined over the pair)
     float pp = 0.f;
 #pragma unroll
-    for (int q = 0; q < S; ++q) pp = fmaf(piv.v[q], ur.v[q], pp);
+    for (int q = 0; q < S; ++q) pp = fmaf(__ldg(pr0g + 32 * h + q), ur.v[q], pp);
     if constexpr (Geo<A>::H == 2) {
       s_xch[h * kTile + cl] = pp;
       pair_sync(wk.warp);
@@ -600,7 +601,7 @@ __global__ void __launch_bounds__(128 * Geo<A>::H, 1) k_walk(const KParams P, fl
     const float invP = 1.0f / Pp;
     if ((P.mode & kModeRootProb) && valid) {
 #pragma unroll
-      for (int q = 0; q < S; ++q) P.rootp[(size_t)(32 * h + q) * C + col] = piv.v[q] * ur.v[q] * invP;
+      for (int q = 0; q < S; ++q) P.rootp[(size_t)(32 * h + q) * C + col] = __ldg(pr0g + 32 * h + q) * ur.v[q] * invP;
     }
     if (MODE == 0 || P.nsteps == 0) continue;
 
@@ -724,7 +725,7 @@ __global__ void __launch_bounds__(128 * Geo<A>::H, 1) k_walk(const KParams P, fl
       BV<A> O;
       int eO, stp;
       if (s0.z) {
-        O = piv;
+        wk.ld(O, pr0g + 32 * h);
         wk.obs(O, codep);
         eO = 0;
         stp = iRoot;

@@ -171,3 +171,46 @@ def test_unsupported_alphabet_raises():
     with pytest.raises(_lib.SubbyError):
         plan.posteriors(aln)
     plan.close()
+
+
+@pytest.mark.parametrize("A,leaves,C", [(4, 14, 300), (16, 9, 160)])
+def test_inside_outside_over_per_column_models_with_different_pi(A, leaves, C):
+    """InsideOutside over a per-column model list whose pis differ
+    (subby/jax/__init__.py:721-774): the passes of every column take the
+    first model's pi at the root, the root's own posterior row the column's
+    own pi.  Each group runs on a plan with that root prior
+    (subby_plan_set_root_prior); compared with the oracle restated the same
+    way, node and branch posteriors, every node."""
+    rng = np.random.default_rng(70 + A)
+    if A == 4:
+        ms = [models.hky85_diag(2.0, rng.dirichlet(np.ones(4))) for _ in range(3)]
+    else:
+        ms = [models.random_reversible(A, rng, 0.5, 2.0)[0] for _ in range(3)]
+    tree = synth.random_tree(leaves, 0.1, rng)
+    aln = synth.simulated_alignment(tree, ms[0], C, 0.1, rng)
+    which = rng.integers(0, 3, size=C)
+    which[0] = 0
+    per_col = [ms[k] for k in which]
+    io = sg.InsideOutside(aln, tree, per_col)
+    node = np.asarray(io.node_posterior())
+    br = np.asarray(io.branch_posterior())
+    t = oracle.Tree(tree.parentIndex, tree.distanceToParent)
+    pi0 = np.asarray(ms[0].pi, np.float64)
+    ref_n = np.zeros_like(node, dtype=np.float64)
+    ref_b = np.zeros_like(br, dtype=np.float64)
+    for k in range(3):
+        idx = np.nonzero(which == k)[0]
+        if idx.size == 0:
+            continue
+        sub = np.ascontiguousarray(aln[:, idx])
+        md = ms[k]._asdict()
+        rn = oracle.NodePosterior(sub, t, md, root_prob=pi0)
+        rn[0] = oracle.NodePosterior(sub, t, md)[0]
+        ref_n[..., idx] = rn
+        ref_b[..., idx] = oracle.BranchPosterior(sub, t, md, root_prob=pi0)
+    _check(node, ref_n, f"A={A} node posteriors, per-column pis")
+    _check(br, ref_b, f"A={A} branch posteriors, per-column pis")
+    # the shared-pi columns equal the plain single-model run
+    one = np.nonzero(which == 0)[0]
+    _check(node[..., one], oracle.NodePosterior(np.ascontiguousarray(aln[:, one]), t, ms[0]._asdict()),
+           "first-model columns")

@@ -85,6 +85,7 @@ __global__ void __launch_bounds__(256, 1) k_acc_f81_tc(const KParams P, const fl
     }
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
+  __syncwarp();  // warp-aligned barriers below need warp 0 whole
   if (t < kA) pis[t] = __ldg(P.tab + P.off.pi + t);
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
@@ -99,6 +100,7 @@ __global__ void __launch_bounds__(256, 1) k_acc_f81_tc(const KParams P, const fl
     if (!mbar_wait_t(mbs[b], ph & 1)) s_err = 1;
     if (b) ++nph1;
     else ++nph0;
+    __syncwarp();
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   };
   // this thread's tile row r (state ii of column 2p + ci) and K half kh
@@ -197,6 +199,7 @@ __global__ void __launch_bounds__(256, 1) k_acc_f81_tc(const KParams P, const fl
         asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mbs[b])
                      : "memory");
       }
+      __syncwarp();
     }
     // the last two chunks' products
     if (NK >= 2) wait_buf((NK - 2) & 1);

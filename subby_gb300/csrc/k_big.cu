@@ -120,6 +120,7 @@ __global__ void __launch_bounds__(256, 1) k_acc(const KParams P, const float *__
     }
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
+  __syncwarp();  // warp-aligned barriers below need warp 0 whole
   // tensor-core back-transform: TMEM (T = C V^T in columns 0-127, V T in
   // 128-191), its mbarrier, and the static A operand [V ; V] (three BF16 terms)
   __shared__ uint32_t s_tm;
@@ -135,6 +136,7 @@ __global__ void __launch_bounds__(256, 1) k_acc(const KParams P, const float *__
                    : "memory");
       asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
+    __syncwarp();
     __syncthreads();   // Vs is loaded
     unsigned char *vv = reinterpret_cast<unsigned char *>(sm + acc_vv_offset<A>());
     for (int idx = t; idx < 128 * 64; idx += blockDim.x) {
@@ -215,11 +217,13 @@ __global__ void __launch_bounds__(256, 1) k_acc(const KParams P, const float *__
     };
     if (t == 0)
       for (int n = n_lo; n < n_lo + S - 1 && n < n_hi; ++n) load(n, it + (n - n_lo));
+    __syncwarp();
     float *scal = sm + Rg::SCAL;  // F81: piU, Dsum per column
     for (int n = n_lo; n < n_hi; ++n, ++it) {
       // every thread is done with the stage of branch n - 1: refill it
       __syncthreads();
       if (t == 0 && n + S - 1 < n_hi) load(n + S - 1, it + S - 1);
+      __syncwarp();
       const int st = (int)(it % S);
       const float *cur = sm + st * Rg::STAGE;
       if (!mbar_wait((uint32_t)__cvta_generic_to_shared(&mbar[st]), (it / S) & 1)) s_err = 1;
@@ -367,6 +371,7 @@ __global__ void __launch_bounds__(256, 1) k_acc(const KParams P, const float *__
                      ::"r"((uint32_t)__cvta_generic_to_shared(&mbT)) : "memory");
       };
       auto sync_tc = [&]() {
+        __syncwarp();
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
         __syncthreads();
@@ -375,6 +380,7 @@ __global__ void __launch_bounds__(256, 1) k_acc(const KParams P, const float *__
       auto wait_t = [&]() {
         if (!mbar_wait((uint32_t)__cvta_generic_to_shared(&mbT), nT & 1)) s_err = 1;
         ++nT;
+        __syncwarp();
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
       };
       auto ld32 = [&](uint32_t col, uint32_t (&r)[32]) {
@@ -420,6 +426,7 @@ __global__ void __launch_bounds__(256, 1) k_acc(const KParams P, const float *__
         }
         sync_tc();
         if (t == 0) mma6(tm, VV, B1, kIdesc128);
+        __syncwarp();
         wait_t();
         // (e) T_c^T rows (lane (cg, jj), k in [32 hh, 32 hh + 32)) into A2
         {
@@ -442,6 +449,7 @@ __global__ void __launch_bounds__(256, 1) k_acc(const KParams P, const float *__
         }
         sync_tc();
         if (t == 0) mma6(tm + 128, A2, VV, kIdesc);
+        __syncwarp();
         wait_t();
         // (i) V C V^T of (column cg, j = jj), i in [32 hh, 32 hh + 32)
         {

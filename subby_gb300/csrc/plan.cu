@@ -1235,7 +1235,7 @@ int run_big(subby_plan *P, const int32_t *d_aln, int C, float *d_logL, float *d_
   }
   const int walk_grid = std::max(1, std::min((chunk + tile - 1) / tile, P->nsm * (H == 2 ? 1 : 2)));
   const size_t slot_floats = (size_t)walk_grid * k.nslots * tile * A;
-  const size_t slot_ints = (size_t)walk_grid * k.nslots * tile;
+  const size_t slot_ints = (size_t)walk_grid * k.nslots * tile * 2;  // a word per column half
   const size_t stage_floats = counts ? (size_t)(R - 1) * chunk * A : 0;
   // A = 64 F81 counts on the tensor cores: per-branch scalars staged too
   const bool f81tc = counts && (mode & kModeF81) && tc && !(mode & kModeBranch);
@@ -1341,7 +1341,7 @@ int run_post(subby_plan *P, const int32_t *d_aln, int C, int node, float *d_node
   const int per_sm = A <= 8 ? 8 : (H == 2 ? 1 : 2);
   const int walk_grid = std::max(1, std::min((chunk + tile - 1) / tile, P->nsm * per_sm));
   const size_t slot_floats = (size_t)walk_grid * k.nslots * tile * A;
-  const size_t slot_ints = (size_t)walk_grid * k.nslots * tile;
+  const size_t slot_ints = (size_t)walk_grid * k.nslots * tile * 2;  // a word per column half
   const size_t stage_floats = stage ? (size_t)(R - 1) * chunk * A : 0;
   auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
   int rc;
@@ -1408,7 +1408,7 @@ int run_cx(subby_plan *P, const int32_t *d_aln, int C, float *d_logL, float *d_c
   const int per_sm = A <= 8 ? 8 : (H == 2 ? 1 : 2);
   const int walk_grid = std::max(1, std::min((chunk + tile - 1) / tile, P->nsm * per_sm));
   const size_t slot_floats = (size_t)walk_grid * k.nslots * tile * A;
-  const size_t slot_ints = (size_t)walk_grid * k.nslots * tile;
+  const size_t slot_ints = (size_t)walk_grid * k.nslots * tile * 2;  // a word per column half
   const size_t stage_floats = counts ? (size_t)(R - 1) * chunk * A : 0;
   const size_t cbuf_bytes = (counts && bt64) ? (size_t)chunk * A * A * sizeof(float2) : 0;
   auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
@@ -1490,7 +1490,7 @@ int run_big_grad(subby_plan *P, const int32_t *d_aln, int C, float *d_logL, cons
   }
   const int walk_grid = std::max(1, std::min((chunk + tile - 1) / tile, P->nsm * (H == 2 ? 1 : 2)));
   const size_t slot_floats = (size_t)walk_grid * k.nslots * tile * A;
-  const size_t slot_ints = (size_t)walk_grid * k.nslots * tile;
+  const size_t slot_ints = (size_t)walk_grid * k.nslots * tile * 2;  // a word per column half
   const size_t stage_floats = R > 1 ? (size_t)(R - 1) * chunk * A : 0;
   auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
   int rc;
@@ -1545,7 +1545,7 @@ int run_cx_grad(subby_plan *P, const int32_t *d_aln, int C, float *d_logL, const
   const int per_sm = A <= 8 ? 8 : (H == 2 ? 1 : 2);
   const int walk_grid = std::max(1, std::min((chunk + tile - 1) / tile, P->nsm * per_sm));
   const size_t slot_floats = (size_t)walk_grid * k.nslots * tile * A;
-  const size_t slot_ints = (size_t)walk_grid * k.nslots * tile;
+  const size_t slot_ints = (size_t)walk_grid * k.nslots * tile * 2;  // a word per column half
   const size_t stage_floats = R > 1 ? (size_t)(R - 1) * chunk * A : 0;
   auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
   int rc;

@@ -152,9 +152,13 @@ struct Walk {
         asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
                      ::"r"(T.sA + kSB2 + part * 16384), "l"(Bg + part * 4096), "r"(8192), "r"(T.mbB) : "memory");
     }
+    __syncwarp();  // warp 0 whole again before the next warp-collective step
   }
   // A-tile stores visible to the tensor cores, then every thread past the barrier
+  // (__syncwarp first: bar.sync is warp-aligned, and a warp that reaches it
+  // diverged may be counted as arrived before all its lanes stored)
   __device__ __forceinline__ void tc_sync() const {
+    __syncwarp();
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
@@ -225,6 +229,7 @@ struct Walk {
       asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(T.mbM)
                    : "memory");
     }
+    __syncwarp();
     T.nB += 1;
     mma_wait();
     tm_ld32(y, 32u * h);
@@ -253,6 +258,7 @@ struct Walk {
       asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(T.mbM)
                    : "memory");
     }
+    __syncwarp();
     if (wantO) T.nB += 1;
     mma_wait();
     {
@@ -428,6 +434,7 @@ __global__ void __launch_bounds__(128 * Geo<A>::H, 1) k_walk(const KParams P, fl
       }
       asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
+    __syncwarp();
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
@@ -460,6 +467,7 @@ __global__ void __launch_bounds__(128 * Geo<A>::H, 1) k_walk(const KParams P, fl
         s_tc.nB = 1;
       }
     }
+    __syncwarp();
     __syncthreads();
     wk.tcs = s_tc;
     if (s_skip) {
@@ -493,7 +501,9 @@ __global__ void __launch_bounds__(128 * Geo<A>::H, 1) k_walk(const KParams P, fl
   const int C = P.C;
   const size_t tile_slots = (size_t)P.nslots * kTile;
   float *svec = P.scrV + (size_t)blockIdx.x * tile_slots * A;  // [slot][c][A]
-  int *sword = P.scrW + (size_t)blockIdx.x * tile_slots;       // [slot][c]
+  // slot words (exponent, mask flags) [h][slot][c]: each half of a column
+  // keeps its own copy, so no word crosses warps between barriers
+  int *sword = P.scrW + (size_t)blockIdx.x * tile_slots * Geo<A>::H;
   BV<A> piv;
   wk.ld(piv, pig + 32 * h);
   const float *EF = P.tab + P.off.EF;
@@ -517,7 +527,7 @@ __global__ void __launch_bounds__(128 * Geo<A>::H, 1) k_walk(const KParams P, fl
     const int32_t *alnc = P.aln + col;
     auto tok = [&](int n) { return __ldg(alnc + (size_t)n * C); };
     auto slotv = [&](int s) { return svec + ((size_t)s * kTile + cl) * A + 32 * h; };
-    auto slotw = [&](int s) -> int & { return sword[(size_t)s * kTile + cl]; };
+    auto slotw = [&](int s) -> int & { return sword[(size_t)h * tile_slots + (size_t)s * kTile + cl]; };
     auto leaf = [&](BN<A> &o, int n) {
       const int t = tok(n);
       o.code = btcode(t, A);
@@ -582,7 +592,7 @@ __global__ void __launch_bounds__(128 * Geo<A>::H, 1) k_walk(const KParams P, fl
         BV<A> cc;
         mprod(cc, u, s0.x, false);
         wk.st(slotv(s0.y), cc);
-        if (h == 0) slotw(s0.y) = (eU << 2) | (hh << 1) | init;
+        slotw(s0.y) = (eU << 2) | (hh << 1) | init;
       }
     }
     // P = pi . U_root (combined over the pair)
@@ -781,7 +791,7 @@ __global__ void __launch_bounds__(128 * Geo<A>::H, 1) k_walk(const KParams P, fl
         } else if (sc.y >= 0) {
           __syncwarp();
           wk.st(slotv(sc.y), Dc);
-          if (h == 0) slotw(sc.y) = (eDc << 2) | (stc << 1) | actc;
+          slotw(sc.y) = (eDc << 2) | (stc << 1) | actc;
         } else {
           const int gks[2] = {side ? s3.z : s3.x, side ? s3.w : s3.y};
           const int gn[2] = {sc.z, sc.w};
@@ -830,7 +840,7 @@ __global__ void __launch_bounds__(128 * Geo<A>::H, 1) k_walk(const KParams P, fl
               }
             } else {
               wk.st(slotv(gks[gs]), Dg);
-              if (h == 0) slotw(gks[gs]) = (eDg << 2) | (stg << 1) | actg;
+              slotw(gks[gs]) = (eDg << 2) | (stg << 1) | actg;
             }
           }
         }

@@ -271,22 +271,35 @@ def test_fp32_vs_fp64_back_transform_both_within_tolerance():
         assert_cols(r['counts'], ref, COUNTS_RTOL, f"counts bt64={bt}")
 
 
-def test_tensor_core_walk_repeatable_small_tree():
+@pytest.mark.parametrize("sel", [0, 2], ids=["tensor_core_walk", "fp32_walk"])
+@pytest.mark.parametrize("mask", ["auto", None], ids=["masked", "unmasked"])
+def test_tensor_core_walk_repeatable_small_tree(sel, mask):
     """A=64 reversible model, 6-leaf tree, 314 columns (three 128-column
-    tiles, the last one ragged): 30 runs of the tensor-core path give
-    bit-identical counts (a walk variant once produced intermittently wrong
-    tiles on this shape)."""
+    tiles, the last one ragged), where a stored child's step directly
+    follows the step that writes its slot word: 30 runs agree bit for bit
+    and every run matches the oracle.  (Before each column half kept its own
+    slot word, the half in warp w + 4 could read the word before warp w wrote
+    it, and columns 0-31 of a tile came out wrong.)"""
     rng = np.random.default_rng(77)
     m = models.random_reversible(64, rng)[0]
     tree = sg.Tree(np.array([-1, 0, 1, 2, 2, 1, 5, 5, 7, 7, 0], dtype=np.int32),
                    rng.exponential(0.1, 11))
     aln = synth.simulated_alignment(tree, m, 314, 0.05, rng)
+    oref = oracle.Counts(aln, oracle.Tree(tree.parentIndex, tree.distanceToParent), _model_dict(m),
+                         branch_mask=mask)
+    lib = _lib.load()
     plan = sg.Plan(tree, m)
-    ref = plan.run(aln, loglike=True, counts=True)['counts']
-    assert np.isfinite(ref).all()
-    for _ in range(30):
-        np.testing.assert_array_equal(plan.run(aln, loglike=True, counts=True)['counts'], ref)
-    plan.close()
+    try:
+        lib.subby_debug_set_kernel(sel)
+        ref = plan.run(aln, loglike=True, counts=True, branch_mask=mask)['counts']
+        assert_cols(ref, oref, COUNTS_RTOL, "first run vs oracle")
+        for _ in range(30):
+            got = plan.run(aln, loglike=True, counts=True, branch_mask=mask)['counts']
+            assert_cols(got, oref, COUNTS_RTOL, "repeat vs oracle")
+            np.testing.assert_array_equal(got, ref)
+    finally:
+        lib.subby_debug_set_kernel(0)
+        plan.close()
 
 
 @pytest.mark.parametrize("A", [4, 20])

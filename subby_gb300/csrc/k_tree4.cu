@@ -148,27 +148,11 @@ __device__ __forceinline__ void t4_piL(const KParams &P, float *sm) {
   }
 }
 
-// The tree program as the kernel reads it: RunProg from shared memory
-// (loaded per plan); a generated policy with the same interface can give the
-// steps as compile-time constants, with the step loops fully unrolled.
-struct RunProg {
-  static __device__ __forceinline__ int4 at(const int4 *prog, int i) { return prog[i]; }
-  static __device__ __forceinline__ int steps(const KParams &P) { return P.nsteps; }
-  template <class F>
-  static __device__ __forceinline__ void up(int n, F &&f) {
-    for (int i = 0; i < n; ++i) f(i);
-  }
-  template <class F>
-  static __device__ __forceinline__ void down(int n, F &&f) {
-    for (int i = n - 1; i >= 0; --i) f(i);
-  }
-};
-
 // The columns [c0, c0 + 32) of one warp (lane = column): inside pass,
 // LogLike / root posterior, outside pass with the fused count accumulation
 // and the epilogue.  sm holds P's tables (t4_load); tb is this warp's
 // tensor-memory slot base.
-template <bool F81, int MASK, int OUT, class PG = RunProg>
+template <bool F81, int MASK, int OUT>
 __device__ __forceinline__ void t4_cols(const KParams &P, float *sm, const uint32_t tb, const int c0) {
   const float *LV = sm + P.stab[P.ntab - 1].sofs;
   const float *small = sm + P.stab[1].sofs;
@@ -199,7 +183,7 @@ __device__ __forceinline__ void t4_cols(const KParams &P, float *sm, const uint3
   auto tok = [&](int n) { return __ldg(alnc + (size_t)n * C); };
   int tk[7], tn[7];
   auto fetch = [&](int (&o)[7], int i) {
-    const int4 s0 = PG::at(prog, 4 * i), s1 = PG::at(prog, 4 * i + 1), s2 = PG::at(prog, 4 * i + 2);
+    const int4 s0 = prog[4 * i], s1 = prog[4 * i + 1], s2 = prog[4 * i + 2];
     o[0] = tok(s0.x);
     o[1] = tok(s1.x);
     o[2] = tok(s2.x);
@@ -274,11 +258,10 @@ __device__ __forceinline__ void t4_cols(const KParams &P, float *sm, const uint3
   F4 ur = F4{make_float2(1.f, 1.f), make_float2(1.f, 1.f)};
   int eRoot = 0, iRoot = 0;
   if (P.root_is_leaf) ur = ld4s(LV + tcode4(tok(0)) * 4);
-  const int nst = PG::steps(P);
+  const int nst = P.nsteps;
   if (nst > 0) fetch(tk, 0);
-  PG::up(nst, [&](const int i) {
-    const int4 s0 = PG::at(prog, 4 * i), s1 = PG::at(prog, 4 * i + 1), s2 = PG::at(prog, 4 * i + 2),
-               s3 = PG::at(prog, 4 * i + 3);
+  for (int i = 0; i < nst; ++i) {
+    const int4 s0 = prog[4 * i], s1 = prog[4 * i + 1], s2 = prog[4 * i + 2], s3 = prog[4 * i + 3];
     if (i + 1 < nst) fetch(tn, i + 1);
     asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
     N4 nl, nr;
@@ -299,7 +282,7 @@ __device__ __forceinline__ void t4_cols(const KParams &P, float *sm, const uint3
     }
 #pragma unroll
     for (int q = 0; q < 7; ++q) tk[q] = tn[q];
-  });
+  }
   const float Pp = dot4(pr0, ur);
   if ((P.mode & kModeLogLike) && valid) P.logL[col] = (float)((double)eRoot * kLn2q + (double)logf(Pp));
   const float invP = 1.0f / Pp;
@@ -477,9 +460,8 @@ __device__ __forceinline__ void t4_cols(const KParams &P, float *sm, const uint3
   };
 
   fetch(tk, nst - 1);
-  PG::down(nst, [&](const int i) {
-    const int4 s0 = PG::at(prog, 4 * i), s1 = PG::at(prog, 4 * i + 1), s2 = PG::at(prog, 4 * i + 2),
-               s3 = PG::at(prog, 4 * i + 3);
+  for (int i = nst - 1; i >= 0; --i) {
+    const int4 s0 = prog[4 * i], s1 = prog[4 * i + 1], s2 = prog[4 * i + 2], s3 = prog[4 * i + 3];
     if (i > 0) fetch(tn, i - 1);
     asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
     N4 nl, nr;
@@ -545,7 +527,7 @@ __device__ __forceinline__ void t4_cols(const KParams &P, float *sm, const uint3
     }
 #pragma unroll
     for (int q = 0; q < 7; ++q) tk[q] = tn[q];
-  });
+  }
   // ------------------------------------------------------------ epilogue
   if (OUT != kOutSum || !valid) return;
   float *out = P.counts + col;

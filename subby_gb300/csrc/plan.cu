@@ -247,10 +247,11 @@ struct subby_plan {
   int root_is_leaf = 0;
   std::vector<int4> steps, slots;
   int nslots = 0;
-  // tree program of k_tree (stored / derived node classification)
-  std::vector<int4> prog;
-  int prog_steps = 0, prog_slots = 0;
-  int4 *d_prog = nullptr;
+  // tree program of k_tree (stored / derived node classification), and the
+  // walk's program with every internal node stored
+  std::vector<int4> prog, prog_w;
+  int prog_steps = 0, prog_slots = 0, prog_w_steps = 0, prog_w_slots = 0;
+  int4 *d_prog = nullptr, *d_prog_w = nullptr;
   std::vector<double> V, mu, pi, t;   // FP64 model and branch lengths (host)
   float f81_mu = 0.f;
   int f81_model = 0;   // M(t) has the F81 / JC closed form (checked on the host)
@@ -445,9 +446,13 @@ int plan_create(const int32_t *parent, const double *dist, const double *evals, 
     P->slots.push_back(make_int4(slot[v], slot[l], slot[r], 0));
   }
 
-  // ---- tree program (k_tree): a node is DERIVED when both children are
-  // leaves or stored (its CC is recomputed from them), otherwise STORED.
-  {
+  // ---- tree program (k_tree, k_tree4): a node is DERIVED when both
+  // children are leaves or stored (its CC is recomputed from them),
+  // otherwise STORED.  The walk (k_walk, slots in global memory) takes the
+  // program in which every internal node is stored: a derived node costs
+  // the walk one more M product (a tensor-core round trip at A = 64) in the
+  // outside pass, a slot only 2 A floats per column.
+  auto build_prog = [&](bool store_all, std::vector<int4> &prog, int &prog_steps, int &prog_slots) {
     std::vector<int> kind(R, -1);  // -1 leaf, -2 derived, -3 root, >= 0 slot
     int nsl = 0;
     for (int v : order) {          // postorder of internal nodes
@@ -455,7 +460,7 @@ int plan_create(const int32_t *parent, const double *dist, const double *evals, 
         kind[v] = -3;
         continue;
       }
-      const bool ok = (kind[left[v]] == -1 || kind[left[v]] >= 0) &&
+      const bool ok = !store_all && (kind[left[v]] == -1 || kind[left[v]] >= 0) &&
                       (kind[right[v]] == -1 || kind[right[v]] >= 0);
       kind[v] = ok ? -2 : nsl++;
     }
@@ -472,14 +477,16 @@ int plan_create(const int32_t *parent, const double *dist, const double *evals, 
           gk[2 * side + 1] = kind[kr];
         }
       }
-      P->prog.push_back(make_int4(v, v == 0 ? -1 : kind[v], v == 0 ? 1 : 0, 0));
-      P->prog.push_back(c[0]);
-      P->prog.push_back(c[1]);
-      P->prog.push_back(make_int4(gk[0], gk[1], gk[2], gk[3]));
+      prog.push_back(make_int4(v, v == 0 ? -1 : kind[v], v == 0 ? 1 : 0, 0));
+      prog.push_back(c[0]);
+      prog.push_back(c[1]);
+      prog.push_back(make_int4(gk[0], gk[1], gk[2], gk[3]));
     }
-    P->prog_steps = (int)P->prog.size() / 4;
-    P->prog_slots = nsl;
-  }
+    prog_steps = (int)prog.size() / 4;
+    prog_slots = nsl;
+  };
+  build_prog(false, P->prog, P->prog_steps, P->prog_slots);
+  build_prog(true, P->prog_w, P->prog_w_steps, P->prog_w_slots);
 
   // ---- FP64 host tables
   P->t.assign(dist, dist + R);
@@ -621,6 +628,10 @@ int plan_create(const int32_t *parent, const double *dist, const double *evals, 
     e = pool_alloc((void **)&P->d_prog, sizeof(int4) * P->prog.size(), P->pool, qs);
     if (e == cudaSuccess)
       e = cudaMemcpyAsync(P->d_prog, P->prog.data(), sizeof(int4) * P->prog.size(), cudaMemcpyHostToDevice, qs);
+    if (e == cudaSuccess) e = pool_alloc((void **)&P->d_prog_w, sizeof(int4) * P->prog_w.size(), P->pool, qs);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(P->d_prog_w, P->prog_w.data(), sizeof(int4) * P->prog_w.size(), cudaMemcpyHostToDevice,
+                          qs);
     if (e != cudaSuccess) return cleanup(cuda_fail(e, "program upload"));
   }
   std::vector<float> hMT, hMN, hGQ;
@@ -858,8 +869,8 @@ int subby_plan_destroy(subby_plan *P) {
   if (s && P->used) cudaStreamWaitEvent(s, P->last_use, 0);
   if (P->s_in) cudaStreamSynchronize(P->s_in);
   if (P->s_out) cudaStreamSynchronize(P->s_out);
-  void *bufs[] = {P->d_tab, P->d_tab64, P->d_steps, P->d_slots, P->d_prog, P->d_tab16, P->d_err, P->d_cx,
-                  P->d_grp_br, P->d_gq};
+  void *bufs[] = {P->d_tab, P->d_tab64, P->d_steps, P->d_slots, P->d_prog, P->d_prog_w, P->d_tab16, P->d_err,
+                  P->d_cx, P->d_grp_br, P->d_gq};
   for (void *b : bufs)
     if (b) cudaFreeAsync(b, s);
   P->work.release(s);
@@ -1182,8 +1193,13 @@ int mark_use(subby_plan *P, cudaStream_t stream) {
 }
 
 // Parameters of the walk (k_walk) and the kernels that consume its staging.
+// A walk with an outside pass runs the program in which every internal node
+// is stored (its M product is not repeated in the outside pass); an
+// inside-only walk runs the derived-node program (no slot round trips
+// through global memory for nodes whose parent can recompute them).
 KParams walk_params(const subby_plan *P, const int32_t *d_aln, int C, int mode, int mask_mode,
-                    const uint8_t *d_mask, float *d_logL, float *d_counts, float *d_root) {
+                    const uint8_t *d_mask, float *d_logL, float *d_counts, float *d_root,
+                    bool outside = true) {
   KParams k{};
   k.aln = d_aln;
   k.C = C;
@@ -1202,9 +1218,9 @@ KParams walk_params(const subby_plan *P, const int32_t *d_aln, int C, int mode, 
   k.logL = d_logL;
   k.counts = d_counts;
   k.rootp = d_root;
-  k.prog = P->d_prog;
-  k.nsteps = P->prog_steps;
-  k.nslots = std::max(P->prog_slots, 1);
+  k.prog = outside ? P->d_prog_w : P->d_prog;
+  k.nsteps = outside ? P->prog_w_steps : P->prog_steps;
+  k.nslots = std::max(outside ? P->prog_w_slots : P->prog_slots, 1);
   k.tab16 = P->d_tab16;
   k.err = P->d_err;
   k.dbg_wait_polls = g_dbg_wait_polls.load();
@@ -1214,7 +1230,8 @@ KParams walk_params(const subby_plan *P, const int32_t *d_aln, int C, int mode, 
 int run_big(subby_plan *P, const int32_t *d_aln, int C, float *d_logL, float *d_counts, float *d_root,
             int mode, int mask_mode, const uint8_t *d_mask, cudaStream_t stream) {
   const int A = P->A, R = P->R;
-  KParams k = walk_params(P, d_aln, C, mode, mask_mode, d_mask, d_logL, d_counts, d_root);
+  KParams k = walk_params(P, d_aln, C, mode, mask_mode, d_mask, d_logL, d_counts, d_root,
+                          (mode & kModeCounts) != 0 && R > 1);
   // 5: tensor-core walk with the CUDA-core back-transform; 6: CUDA-core walk
   // with the tensor-core back-transform (test hooks)
   const bool tc = (A == 64) && P->d_tab16 && (g_kernel_sel == 0 || g_kernel_sel == 5);
@@ -1323,7 +1340,8 @@ int run_post(subby_plan *P, const int32_t *d_aln, int C, int node, float *d_node
   }
   const bool stage = outside && d_br;
   const int mode = (node <= 0 && d_node) ? kModeRootProb : 0;
-  KParams k = walk_params(P, d_aln, C, mode, SUBBY_MASK_NONE, nullptr, nullptr, nullptr, node <= 0 ? d_node : nullptr);
+  KParams k = walk_params(P, d_aln, C, mode, SUBBY_MASK_NONE, nullptr, nullptr, nullptr, node <= 0 ? d_node : nullptr,
+                          outside);
   k.npost = d_node;
   k.npost_node = node;
   const bool tc = (A == 64) && P->d_tab16 && (g_kernel_sel == 0 || g_kernel_sel == 5);

@@ -159,7 +159,10 @@ def test_c4_gradient_device_memory_is_bounded_in_the_column_count(grad20):
     """The adjoint's per-branch staging runs in column chunks of about 4 GiB
     at most, so once C passes the chunk size the plan's device memory grows
     only by the uploaded tokens: doubling 2 x 10^5 columns to 4 x 10^5 adds
-    the extra alignment and nothing else (and doubles the gradient)."""
+    the extra alignment and nothing else (and doubles the gradient).  The
+    absolute figure at 2 x 10^5 columns is the 4 GiB staging chunk, the
+    tokens and the walk's node slots (every internal node of the 399-node
+    tree stored, per column of the 304 resident 128-column tiles)."""
     w = grad20
     a2 = np.ascontiguousarray(np.concatenate([w['alignment']] * 2, axis=1))
     a4 = np.ascontiguousarray(np.concatenate([a2, a2], axis=1))
@@ -169,7 +172,7 @@ def test_c4_gradient_device_memory_is_bounded_in_the_column_count(grad20):
     _, t4, G4 = plan.grad(a4)
     b4 = plan.device_bytes()
     plan.close()
-    assert b2 < (6 << 30), b2
+    assert b2 < (7 << 30), b2
     assert b4 - b2 <= 1.5 * a2.nbytes + (64 << 20), (b2, b4, a2.nbytes)
     _close(t4, 2 * t2, "d/dt of the doubled alignment", rtol=1e-4)
     _close(G4, 2 * G2, "d/dS of the doubled alignment", rtol=1e-4)

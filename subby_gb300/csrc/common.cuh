@@ -98,6 +98,7 @@ struct KParams {
   // (4096 elements each), then [Vd^T 1|2|3 | Vu^T 1|2|3] at R*24576
   const uint16_t *tab16;
   int *err;               // device status: bounded waits that gave up (tensor-core walk)
+  int noderiv;            // the walk's program has no derived nodes (every internal node stored)
   int dbg_wait_polls;     // test hook: > 0 makes the tensor-core walk's prologue wait
                           // on an unarmed mbarrier for that many polls and give up
   // the model is F81 / JC: M_n = e_n I + (1 - e_n) 1 pi^T, so the walk's

@@ -1219,6 +1219,7 @@ KParams walk_params(const subby_plan *P, const int32_t *d_aln, int C, int mode, 
   k.counts = d_counts;
   k.rootp = d_root;
   k.prog = outside ? P->d_prog_w : P->d_prog;
+  k.noderiv = outside ? 1 : 0;
   k.nsteps = outside ? P->prog_w_steps : P->prog_steps;
   k.nslots = std::max(outside ? P->prog_w_slots : P->prog_slots, 1);
   k.tab16 = P->d_tab16;

@@ -403,8 +403,10 @@ struct BN {
 
 // MODE: 0 inside only, 1 eigen staging, 2 F81 (raw) staging, 3 node
 // posteriors (and raw staging when stage_a is given); F81M: the model is
-// F81 / JC and the M products take the closed form
-template <int A, int MODE, bool TC, bool F81M>
+// F81 / JC and the M products take the closed form; ND: the program has no
+// derived nodes (every internal node stored), so the derived-node paths are
+// not compiled (fewer live registers)
+template <int A, int MODE, bool TC, bool F81M, bool ND = false>
 __global__ void __launch_bounds__(128 * Geo<A>::H, 1) k_walk(const KParams P, float *__restrict__ stage_a,
                                                               float *__restrict__ stage_b, int c_base,
                                                               int c_count) {
@@ -573,9 +575,9 @@ __global__ void __launch_bounds__(128 * Geo<A>::H, 1) k_walk(const KParams P, fl
         BV<A> u;
         BN<A> k0, k1;
         int cd;
-        if (s1.y == -2) derive(nl, u, k0, k1, cd, s1.x, s1, s3.x, s3.y);
+        if (!ND && s1.y == -2) derive(nl, u, k0, k1, cd, s1.x, s1, s3.x, s3.y);
         else basic(nl, s1.x, s1.y);
-        if (s2.y == -2) derive(nr, u, k0, k1, cd, s2.x, s2, s3.z, s3.w);
+        if (!ND && s2.y == -2) derive(nr, u, k0, k1, cd, s2.x, s2, s3.z, s3.w);
         else basic(nr, s2.x, s2.y);
       }
       BV<A> u;
@@ -726,9 +728,9 @@ __global__ void __launch_bounds__(128 * Geo<A>::H, 1) k_walk(const KParams P, fl
         BV<A> u;
         BN<A> k0, k1;
         int cd;
-        if (s1.y == -2) derive(nl, u, k0, k1, cd, s1.x, s1, s3.x, s3.y);
+        if (!ND && s1.y == -2) derive(nl, u, k0, k1, cd, s1.x, s1, s3.x, s3.y);
         else basic(nl, s1.x, s1.y);
-        if (s2.y == -2) derive(nr, u, k0, k1, cd, s2.x, s2, s3.z, s3.w);
+        if (!ND && s2.y == -2) derive(nr, u, k0, k1, cd, s2.x, s2, s3.z, s3.w);
         else basic(nr, s2.x, s2.y);
       }
       const int codep = btcode(tok(s0.x), A);
@@ -788,7 +790,7 @@ __global__ void __launch_bounds__(128 * Geo<A>::H, 1) k_walk(const KParams P, fl
             wk.obs(U, me.code);
             emit(sc.x, Dc, U, me.code, eDc, actc);
           }
-        } else if (sc.y >= 0) {
+        } else if (ND || sc.y >= 0) {
           __syncwarp();
           wk.st(slotv(sc.y), Dc);
           slotw(sc.y) = (eDc << 2) | (stc << 1) | actc;
@@ -858,17 +860,26 @@ __global__ void __launch_bounds__(128 * Geo<A>::H, 1) k_walk(const KParams P, fl
 }
 
 
-template <int A, int MODE, bool TC, bool F81M>
-int walk_launch1(const KParams &p, float *sa, float *sb, int c_base, int c_count, int grid, cudaStream_t s) {
+template <int A, int MODE, bool TC, bool F81M, bool ND>
+int walk_launch_nd(const KParams &p, float *sa, float *sb, int c_base, int c_count, int grid, cudaStream_t s) {
   const int threads = 128 * Geo<A>::H;
   const size_t dyn = TC ? kTcDyn + 1024 : 0;
   if (TC) {
-    cudaError_t e =
-        cudaFuncSetAttribute(k_walk<A, MODE, TC, F81M>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
+    cudaError_t e = cudaFuncSetAttribute(k_walk<A, MODE, TC, F81M, ND>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)dyn);
     if (e != cudaSuccess) return (int)e;
   }
-  k_walk<A, MODE, TC, F81M><<<grid, threads, dyn, s>>>(p, sa, sb, c_base, c_count);
+  k_walk<A, MODE, TC, F81M, ND><<<grid, threads, dyn, s>>>(p, sa, sb, c_base, c_count);
   return (int)cudaGetLastError();
+}
+// the eigen-staging walk (Counts, gradients) in its derived-node-free form
+// when the program has no derived nodes
+template <int A, int MODE, bool TC, bool F81M>
+int walk_launch1(const KParams &p, float *sa, float *sb, int c_base, int c_count, int grid, cudaStream_t s) {
+  if constexpr (MODE == 1) {
+    if (p.noderiv) return walk_launch_nd<A, MODE, TC, F81M, true>(p, sa, sb, c_base, c_count, grid, s);
+  }
+  return walk_launch_nd<A, MODE, TC, F81M, false>(p, sa, sb, c_base, c_count, grid, s);
 }
 
 }  // namespace

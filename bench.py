@@ -437,7 +437,7 @@ def precision64_block(args):
     import subby_gb300 as sg
     from subby_gb300 import synth, _lib
     from tests._tol import colwise_err, loglike_err
-    C = 65536
+    C = args.columns if args.columns != (1 << 20) else 65536
     w = synth.precision64(seed=3, C=C)
     R = len(w['tree'].parentIndex)
     A = 64
@@ -498,7 +498,7 @@ def precision64_block(args):
     tc, fp = res["split_bf16_tensor_core"], res["fp32_cuda_core"]
     return {"workload": "precision64: A=64 random reversible (exchangeabilities LogNormal(0,1), "
                         "pi ~ Dir(1^64), ~5% of eigenvalue pairs within 1e-7), R=127 (64 leaves), "
-                        "C=65536 simulated columns, Counts (unmasked) + LogLike",
+                        f"C={C} simulated columns, Counts (unmasked) + LogLike",
             "unit": UNIT, "steps": steps, "warmup": args.warmup,
             "forced_near_degenerate_pairs": w['forced_pairs'],
             "tensor_core_vs_fp32_speedup": tc["columns_per_s"] / fp["columns_per_s"],
@@ -514,7 +514,8 @@ def precision64_block(args):
 def precision64_bench(args):
     """Prints the precision64 block as its own line."""
     b = precision64_block(args)
-    b.update({"metric": "Counts columns/s (A=64 reversible, R=127, C=65536)",
+    C = args.columns if args.columns != (1 << 20) else 65536
+    b.update({"metric": f"Counts columns/s (A=64 reversible, R=127, C={C})",
               "value": b["variants"]["split_bf16_tensor_core"]["columns_per_s"], "higher_is_better": True,
               "dtype": "fp32 (split-bf16 tensor-core products)"})
     print(json.dumps(b))

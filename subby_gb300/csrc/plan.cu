@@ -1193,10 +1193,11 @@ int mark_use(subby_plan *P, cudaStream_t stream) {
 }
 
 // Parameters of the walk (k_walk) and the kernels that consume its staging.
-// A walk with an outside pass runs the program in which every internal node
-// is stored (its M product is not repeated in the outside pass); an
-// inside-only walk runs the derived-node program (no slot round trips
-// through global memory for nodes whose parent can recompute them).
+// A walk with an outside pass and costly M products (A >= 16, not the F81
+// closed form) runs the program in which every internal node is stored (its
+// M product is not repeated in the outside pass); other walks run the
+// derived-node program (no slot round trips through global memory for nodes
+// whose parent can recompute them cheaply).
 KParams walk_params(const subby_plan *P, const int32_t *d_aln, int C, int mode, int mask_mode,
                     const uint8_t *d_mask, float *d_logL, float *d_counts, float *d_root,
                     bool outside = true) {
@@ -1218,10 +1219,11 @@ KParams walk_params(const subby_plan *P, const int32_t *d_aln, int C, int mode, 
   k.logL = d_logL;
   k.counts = d_counts;
   k.rootp = d_root;
-  k.prog = outside ? P->d_prog_w : P->d_prog;
-  k.noderiv = outside ? 1 : 0;
-  k.nsteps = outside ? P->prog_w_steps : P->prog_steps;
-  k.nslots = std::max(outside ? P->prog_w_slots : P->prog_slots, 1);
+  const bool all = outside && P->A >= 16 && !P->f81_model;
+  k.prog = all ? P->d_prog_w : P->d_prog;
+  k.noderiv = all ? 1 : 0;
+  k.nsteps = all ? P->prog_w_steps : P->prog_steps;
+  k.nslots = std::max(all ? P->prog_w_slots : P->prog_slots, 1);
   k.tab16 = P->d_tab16;
   k.err = P->d_err;
   k.dbg_wait_polls = g_dbg_wait_polls.load();

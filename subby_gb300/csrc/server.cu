@@ -75,7 +75,7 @@ using Clock = std::chrono::steady_clock;
 double ns_per_col_node(int A, bool f81) {
   if (A <= 8) return f81 ? 0.011 : 0.012;
   if (A <= 20) return f81 ? 0.10 : 0.30;
-  return f81 ? 0.70 : 1.6;
+  return f81 ? 0.70 : 1.2;
 }
 double job_cost_ms(const subby_job &d) {
   const bool f81 = d.counts_kind == SUBBY_COUNTS_F81 && (d.want & SUBBY_WANT_COUNTS);

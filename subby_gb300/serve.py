@@ -121,7 +121,7 @@ STAGE_CAP = 4 << 30   # per-plan staging cap of the large-alphabet path (bytes)
 # Device time per (column x tree node), ns, by path (GB300, Counts): used only
 # to order and slice work, never to skip any.
 _NS_PER_COL_NODE = {("4", False): 0.012, ("4", True): 0.011, ("16", False): 0.30, ("16", True): 0.10,
-                    ("64", False): 1.6, ("64", True): 0.70}
+                    ("64", False): 1.2, ("64", True): 0.70}
 
 
 def job_cost_ms(R: int, C: int, A: int, f81: bool = False) -> float:

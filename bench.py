@@ -137,6 +137,12 @@ class ClockSampler:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", f"--id={self.idx}", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
                  "-lms", "100"], stdout=self.f, stderr=subprocess.DEVNULL)
+            # the sampler's start-up (driver queries) must not fall inside a
+            # short timed region: wait for its first sample (at most 2 s)
+            t0 = time.perf_counter()
+            while (self.proc.poll() is None and os.path.getsize(self.path) == 0
+                   and time.perf_counter() - t0 < 2.0):
+                time.sleep(0.02)
         except Exception:  # noqa: BLE001
             self.proc = None
         return self

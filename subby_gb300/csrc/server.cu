@@ -587,8 +587,11 @@ void engine(subby_server *S) {
       rel.swap(S->to_release);
     }
     for (void *p : rel) S->pinned.put(p);
-    // short A = 4 jobs waiting together: one packed launch per batch
-    while (S->pack && !S->free_slots.empty()) {
+    // short A = 4 jobs waiting together: one packed launch per batch.  (The
+    // settings are read only while jobs wait: subby_server_set changes them
+    // only before the first submission, under the lock the engine took to
+    // move that job here.)
+    while (!S->waiting.empty() && S->pack && !S->free_slots.empty()) {
       std::vector<SJob *> cand;
       long long cols = 0;
       size_t bytes = 0;

@@ -124,7 +124,7 @@ __global__ void __launch_bounds__(256, 1) k_acc(const KParams P, const float *__
   // tensor-core back-transform: TMEM (T = C V^T in columns 0-127, V T in
   // 128-191), its mbarrier, and the static A operand [V ; V] (three BF16 terms)
   __shared__ uint32_t s_tm;
-  __shared__ __align__(8) uint64_t mbT;
+  __shared__ __align__(8) uint64_t mbT[2];   // D1 products, D2 products
   if constexpr (TCB) {
     if ((t >> 5) == 0) {
       asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;"
@@ -132,8 +132,9 @@ __global__ void __launch_bounds__(256, 1) k_acc(const KParams P, const float *__
       asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     }
     if (t == 0) {
-      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"((uint32_t)__cvta_generic_to_shared(&mbT))
-                   : "memory");
+      for (int i = 0; i < 2; ++i)
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"((uint32_t)__cvta_generic_to_shared(&mbT[i]))
+                     : "memory");
       asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     __syncwarp();
@@ -156,7 +157,7 @@ __global__ void __launch_bounds__(256, 1) k_acc(const KParams P, const float *__
   }
   __syncthreads();
   if constexpr (TCB) asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-  uint32_t nT = 0;  // completed phases of mbT
+  uint32_t nT[2] = {0, 0};  // completed phases of mbT[0] (D1) and mbT[1] (D2)
   uint32_t it = 0;  // ring position of the next branch to consume (all groups)
 
   for (int wi = blockIdx.x; wi < nitems; wi += gridDim.x) {
@@ -355,7 +356,10 @@ __global__ void __launch_bounds__(256, 1) k_acc(const KParams P, const float *__
       const uint32_t tm = s_tm;
       const int warp = t >> 5, lane = t & 31, sub = warp & 3, hh = warp >> 2;
       const int m = 32 * sub + lane, cg = m >> 6, jj = m & 63;
-      auto mma6 = [&](uint32_t d, uint32_t a, uint32_t b, uint32_t idesc) {
+      // each kind of product commits to its own mbarrier, so a wait never
+      // has two phases of one barrier outstanding (a parity wait cannot tell
+      // them apart)
+      auto mma6 = [&](uint32_t d, uint32_t a, uint32_t b, uint32_t idesc, int kind) {
         constexpr int pa[6] = {0, 0, 1, 0, 1, 2}, pb[6] = {0, 1, 0, 2, 1, 0};
 #pragma unroll
         for (int ks = 0; ks < 4; ++ks)
@@ -368,7 +372,7 @@ __global__ void __launch_bounds__(256, 1) k_acc(const KParams P, const float *__
                          "l"(umma_desc(b + pb[prod] * 16384 + ks * 256)), "r"(idesc), "r"(accum) : "memory");
           }
         asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
-                     ::"r"((uint32_t)__cvta_generic_to_shared(&mbT)) : "memory");
+                     ::"r"((uint32_t)__cvta_generic_to_shared(&mbT[kind])) : "memory");
       };
       auto sync_tc = [&]() {
         __syncwarp();
@@ -377,9 +381,9 @@ __global__ void __launch_bounds__(256, 1) k_acc(const KParams P, const float *__
         __syncthreads();
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
       };
-      auto wait_t = [&]() {
-        if (!mbar_wait((uint32_t)__cvta_generic_to_shared(&mbT), nT & 1)) s_err = 1;
-        ++nT;
+      auto wait_t = [&](int kind) {
+        if (!mbar_wait((uint32_t)__cvta_generic_to_shared(&mbT[kind]), nT[kind] & 1)) s_err = 1;
+        ++nT[kind];
         __syncwarp();
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
       };
@@ -407,9 +411,8 @@ __global__ void __launch_bounds__(256, 1) k_acc(const KParams P, const float *__
         t3 = *reinterpret_cast<const uint32_t *>(&b3);
       };
       const bool vec2 = (C & 1) == 0 && (c_base & 1) == 0;
-#pragma unroll
-      for (int p = 0; p < 4; ++p) {
-        // (a) B1 rows of this thread's 4 x 4 block for the two columns
+      // (a) B1 rows of this thread's 4 x 4 block for the columns 2p, 2p+1
+      auto build_B1 = [&](const int p) {
 #pragma unroll
         for (int h2 = 0; h2 < 2; ++h2) {
           const int q = 2 * p + h2;
@@ -424,34 +427,49 @@ __global__ void __launch_bounds__(256, 1) k_acc(const KParams P, const float *__
             asm volatile("st.shared.v2.b32 [%0], {%1, %2};" ::"r"(o + 32768), "r"(u3[0]), "r"(u3[1]) : "memory");
           }
         }
-        sync_tc();
-        if (t == 0) mma6(tm, VV, B1, kIdesc128);
-        __syncwarp();
-        wait_t();
-        // (e) T_c^T rows (lane (cg, jj), k in [32 hh, 32 hh + 32)) into A2
-        {
-          uint32_t r[32];
-          ld32(64u * cg + 32u * hh, r);
+      };
+      // (e) T_c^T rows (lane (cg, jj), k in [32 hh, 32 hh + 32)) into A2
+      auto build_A2 = [&]() {
+        uint32_t r[32];
+        ld32(64u * cg + 32u * hh, r);
 #pragma unroll
-          for (int q = 0; q < 4; ++q) {
-            uint32_t w1[4], w2[4], w3[4];
+        for (int q = 0; q < 4; ++q) {
+          uint32_t w1[4], w2[4], w3[4];
 #pragma unroll
-            for (int pp = 0; pp < 4; ++pp)
-              split3(__uint_as_float(r[8 * q + 2 * pp]), __uint_as_float(r[8 * q + 2 * pp + 1]), w1[pp], w2[pp], w3[pp]);
-            const uint32_t o = A2 + kmaj_off(m, 32 * hh + 8 * q);
-            asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};" ::"r"(o), "r"(w1[0]), "r"(w1[1]), "r"(w1[2]),
-                         "r"(w1[3]) : "memory");
-            asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};" ::"r"(o + 16384), "r"(w2[0]), "r"(w2[1]),
-                         "r"(w2[2]), "r"(w2[3]) : "memory");
-            asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};" ::"r"(o + 32768), "r"(w3[0]), "r"(w3[1]),
-                         "r"(w3[2]), "r"(w3[3]) : "memory");
-          }
+          for (int pp = 0; pp < 4; ++pp)
+            split3(__uint_as_float(r[8 * q + 2 * pp]), __uint_as_float(r[8 * q + 2 * pp + 1]), w1[pp], w2[pp], w3[pp]);
+          const uint32_t o = A2 + kmaj_off(m, 32 * hh + 8 * q);
+          asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};" ::"r"(o), "r"(w1[0]), "r"(w1[1]), "r"(w1[2]),
+                       "r"(w1[3]) : "memory");
+          asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};" ::"r"(o + 16384), "r"(w2[0]), "r"(w2[1]),
+                       "r"(w2[2]), "r"(w2[3]) : "memory");
+          asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};" ::"r"(o + 32768), "r"(w3[0]), "r"(w3[1]),
+                       "r"(w3[2]), "r"(w3[3]) : "memory");
         }
+      };
+      // Pair p's products in issue order D1(p) -> D2(p) -> D1(p+1) -> D2(p+1):
+      // D2(p) runs while B1(p+1) is built and D1(p+1) issued, and the counts
+      // of pair p are staged and stored while D1(p+1) runs (D1 in tensor-
+      // memory columns 0-127, D2 in 128-191, as before).
+      build_B1(0);
+      sync_tc();
+      if (t == 0) mma6(tm, VV, B1, kIdesc128, 0);
+      __syncwarp();
+      wait_t(0);
+#pragma unroll
+      for (int p = 0; p < 4; ++p) {
+        build_A2();   // from D1(p); A2 is free: D2(p-1) has completed
         sync_tc();
-        if (t == 0) mma6(tm + 128, A2, VV, kIdesc);
+        if (t == 0) mma6(tm + 128, A2, VV, kIdesc, 1);
         __syncwarp();
-        wait_t();
-        // (i) V C V^T of (column cg, j = jj), i in [32 hh, 32 hh + 32)
+        if (p < 3) {
+          build_B1(p + 1);   // B1 is free: D1(p) has completed
+          sync_tc();
+          if (t == 0) mma6(tm, VV, B1, kIdesc128, 0);   // D1(p) has been read into A2
+          __syncwarp();
+        }
+        wait_t(1);   // D2(p)
+        // (i) V C V^T of (column 2p + cg, j = jj), i in [32 hh, 32 hh + 32)
         {
           uint32_t r[32];
           ld32(128u + 32u * hh, r);
@@ -479,6 +497,7 @@ __global__ void __launch_bounds__(256, 1) k_acc(const KParams P, const float *__
               }
             }
         }
+        if (p < 3) wait_t(0);   // D1(p+1)
       }
       __syncthreads();
       continue;

@@ -1,6 +1,6 @@
 """FP64 CPU oracle for the eigensubstitution hot path (TEST INFRASTRUCTURE ONLY).
 
-This module is the checker, never the product: only ``tests/``,
+This module checks the product and is never part of it: only ``tests/``,
 ``__graft_entry__.smoke()`` and the CPU-baseline / reference arm of
 ``bench.py`` may import it.  The shipped path (``subby_gb300``) never calls it
 and has no CPU fallback.

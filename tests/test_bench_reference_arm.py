@@ -1,5 +1,5 @@
 """The bench's reference arm (the reference's CPU algorithm on the host
-cores) runs without a GPU and prints the JSON line the driver parses: the
+cores) runs without a GPU and prints the bench's one JSON line: the
 headline metric and unit, impl = reference, its cpu_baseline record and an
 e2e entry with no host-device copies."""
 import json

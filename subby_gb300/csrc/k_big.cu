@@ -450,7 +450,9 @@ __global__ void __launch_bounds__(256, 1) k_acc(const KParams P, const float *__
       // Pair p's products in issue order D1(p) -> D2(p) -> D1(p+1) -> D2(p+1):
       // D2(p) runs while B1(p+1) is built and D1(p+1) issued, and the counts
       // of pair p are staged and stored while D1(p+1) runs (D1 in tensor-
-      // memory columns 0-127, D2 in 128-191, as before).
+      // memory columns 0-127, D2 in 128-191).  Each buffer is rewritten
+      // only after the product that reads it has completed (B1, A2) or its
+      // tensor-memory loads have finished before a block barrier (D1, D2).
       build_B1(0);
       sync_tc();
       if (t == 0) mma6(tm, VV, B1, kIdesc128, 0);

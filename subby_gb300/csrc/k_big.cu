@@ -121,14 +121,15 @@ __global__ void __launch_bounds__(256, 1) k_acc(const KParams P, const float *__
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   __syncwarp();  // warp-aligned barriers below need warp 0 whole
-  // tensor-core back-transform: TMEM (T = C V^T in columns 0-127, V T in
-  // 128-191), its mbarrier, and the static A operand [V ; V] (three BF16 terms)
+  // tensor-core back-transform: TMEM (the four pairs' V C V^T in columns
+  // 0-255, T = C V^T in 256-383), one mbarrier per product kind, and the
+  // static A operand [V ; V] (three BF16 terms)
   __shared__ uint32_t s_tm;
   __shared__ __align__(8) uint64_t mbT[2];   // D1 products, D2 products
   if constexpr (TCB) {
     if ((t >> 5) == 0) {
       asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;"
-                   ::"r"((uint32_t)__cvta_generic_to_shared(&s_tm)), "r"(256) : "memory");
+                   ::"r"((uint32_t)__cvta_generic_to_shared(&s_tm)), "r"(512) : "memory");
       asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     }
     if (t == 0) {
@@ -345,15 +346,18 @@ __global__ void __launch_bounds__(256, 1) k_acc(const KParams P, const float *__
       continue;
     }
     if constexpr (TCB) {
-      // Per column pair (2p, 2p+1): B1 = [C_2p ; C_2p+1] (rows (c, k), K = l);
+      // Per column pair (p, p+4): B1 = [C_p ; C_p+4] (rows (c, k), K = l);
       // D1 = [V ; V] B1^T holds T_c^T (lane (c, j), column k) in its
       // diagonal blocks; A2 = those rows (K = k); D2 = A2 V^T holds
-      // (V C V^T)_c[i][j] at lane (c, j), column i.
+      // (V C V^T)_c[i][j] at lane (c, j), column i.  D1 sits in tensor-memory
+      // columns 256-383; each pair's D2 stays in columns 64p.. until all four
+      // are formed, so a pair's D2 product runs while the next pair's B1 is
+      // built and its D1 issued, and the eight columns go out together:
+      // lane (c, j) holds columns 4c .. 4c+3 of the group, one 16-byte store.
       const uint32_t base = (uint32_t)__cvta_generic_to_shared(sm);
       const uint32_t B1 = base, A2 = base + 49152;
-      float *Pst = sm + (98304 / 4);                 // [i][j][2] staging of one pair
       const uint32_t VV = base + 4u * acc_vv_offset<A>();
-      const uint32_t tm = s_tm;
+      const uint32_t tm = s_tm, tmD1 = s_tm + 256u;
       const int warp = t >> 5, lane = t & 31, sub = warp & 3, hh = warp >> 2;
       const int m = 32 * sub + lane, cg = m >> 6, jj = m & 63;
       // each kind of product commits to its own mbarrier, so a wait never
@@ -390,13 +394,13 @@ __global__ void __launch_bounds__(256, 1) k_acc(const KParams P, const float *__
       auto ld32 = [&](uint32_t col, uint32_t (&r)[32]) {
         asm volatile("tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,"
                      "%15,%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];\n"
-                 "tcgen05.wait::ld.sync.aligned;"
+                     "tcgen05.wait::ld.sync.aligned;"
                      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
                        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
                        "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]),
                        "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]),
                        "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
-                     : "r"(tm + ((uint32_t)(32 * sub) << 16) + col)
+                     : "r"(col + ((uint32_t)(32 * sub) << 16))
                      : "memory");
       };
       auto split3 = [](float x0, float x1, uint32_t &t1, uint32_t &t2, uint32_t &t3) {
@@ -410,12 +414,13 @@ __global__ void __launch_bounds__(256, 1) k_acc(const KParams P, const float *__
         t2 = *reinterpret_cast<const uint32_t *>(&b2);
         t3 = *reinterpret_cast<const uint32_t *>(&b3);
       };
-      const bool vec2 = (C & 1) == 0 && (c_base & 1) == 0;
-      // (a) B1 rows of this thread's 4 x 4 block for the columns 2p, 2p+1
-      auto build_B1 = [&](const int p) {
+#pragma unroll
+      for (int p = 0; p < 4; ++p) {
+        // (a) B1 rows of this thread's 4 x 4 block for columns p and p + 4
+        // (B1 is free: the previous pair's D1 has completed)
 #pragma unroll
         for (int h2 = 0; h2 < 2; ++h2) {
-          const int q = 2 * p + h2;
+          const int q = p + 4 * h2;
 #pragma unroll
           for (int a = 0; a < 4; ++a) {
             uint32_t u1[2], u2[2], u3[2];
@@ -427,80 +432,78 @@ __global__ void __launch_bounds__(256, 1) k_acc(const KParams P, const float *__
             asm volatile("st.shared.v2.b32 [%0], {%1, %2};" ::"r"(o + 32768), "r"(u3[0]), "r"(u3[1]) : "memory");
           }
         }
-      };
-      // (e) T_c^T rows (lane (cg, jj), k in [32 hh, 32 hh + 32)) into A2
-      auto build_A2 = [&]() {
-        uint32_t r[32];
-        ld32(64u * cg + 32u * hh, r);
-#pragma unroll
-        for (int q = 0; q < 4; ++q) {
-          uint32_t w1[4], w2[4], w3[4];
-#pragma unroll
-          for (int pp = 0; pp < 4; ++pp)
-            split3(__uint_as_float(r[8 * q + 2 * pp]), __uint_as_float(r[8 * q + 2 * pp + 1]), w1[pp], w2[pp], w3[pp]);
-          const uint32_t o = A2 + kmaj_off(m, 32 * hh + 8 * q);
-          asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};" ::"r"(o), "r"(w1[0]), "r"(w1[1]), "r"(w1[2]),
-                       "r"(w1[3]) : "memory");
-          asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};" ::"r"(o + 16384), "r"(w2[0]), "r"(w2[1]),
-                       "r"(w2[2]), "r"(w2[3]) : "memory");
-          asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};" ::"r"(o + 32768), "r"(w3[0]), "r"(w3[1]),
-                       "r"(w3[2]), "r"(w3[3]) : "memory");
-        }
-      };
-      // Pair p's products in issue order D1(p) -> D2(p) -> D1(p+1) -> D2(p+1):
-      // D2(p) runs while B1(p+1) is built and D1(p+1) issued, and the counts
-      // of pair p are staged and stored while D1(p+1) runs (D1 in tensor-
-      // memory columns 0-127, D2 in 128-191).  Each buffer is rewritten
-      // only after the product that reads it has completed (B1, A2) or its
-      // tensor-memory loads have finished before a block barrier (D1, D2).
-      build_B1(0);
-      sync_tc();
-      if (t == 0) mma6(tm, VV, B1, kIdesc128, 0);
-      __syncwarp();
-      wait_t(0);
-#pragma unroll
-      for (int p = 0; p < 4; ++p) {
-        build_A2();   // from D1(p); A2 is free: D2(p-1) has completed
         sync_tc();
-        if (t == 0) mma6(tm + 128, A2, VV, kIdesc, 1);
+        if (t == 0) mma6(tmD1, VV, B1, kIdesc128, 0);
         __syncwarp();
-        if (p < 3) {
-          build_B1(p + 1);   // B1 is free: D1(p) has completed
-          sync_tc();
-          if (t == 0) mma6(tm, VV, B1, kIdesc128, 0);   // D1(p) has been read into A2
-          __syncwarp();
-        }
-        wait_t(1);   // D2(p)
-        // (i) V C V^T of (column 2p + cg, j = jj), i in [32 hh, 32 hh + 32)
+        if (p > 0) wait_t(1);   // the previous pair's D2
+        wait_t(0);              // this pair's D1
+        // (e) T_c^T rows (lane (cg, jj), k in [32 hh, 32 hh + 32)) into A2
+        // (A2 is free: the previous pair's D2 has completed)
         {
           uint32_t r[32];
-          ld32(128u + 32u * hh, r);
+          ld32(tmD1 + 64u * cg + 32u * hh, r);
 #pragma unroll
-          for (int i = 0; i < 32; ++i) Pst[((32 * hh + i) * 64 + jj) * 2 + cg] = __uint_as_float(r[i]);
+          for (int q = 0; q < 4; ++q) {
+            uint32_t w1[4], w2[4], w3[4];
+#pragma unroll
+            for (int pp = 0; pp < 4; ++pp)
+              split3(__uint_as_float(r[8 * q + 2 * pp]), __uint_as_float(r[8 * q + 2 * pp + 1]), w1[pp], w2[pp], w3[pp]);
+            const uint32_t o = A2 + kmaj_off(m, 32 * hh + 8 * q);
+            asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};" ::"r"(o), "r"(w1[0]), "r"(w1[1]), "r"(w1[2]),
+                         "r"(w1[3]) : "memory");
+            asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};" ::"r"(o + 16384), "r"(w2[0]), "r"(w2[1]),
+                         "r"(w2[2]), "r"(w2[3]) : "memory");
+            asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};" ::"r"(o + 32768), "r"(w3[0]), "r"(w3[1]),
+                         "r"(w3[2]), "r"(w3[3]) : "memory");
+          }
         }
-        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-        __syncthreads();
-        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        // (k) counts rows (i, j) of the two columns
-        {
-          const int cp = c_base + g0 + 2 * p;
-          const int nc = gcols - 2 * p;
-          if (nc > 0)
-            for (int e = t; e < 64 * 64; e += 256) {
-              const int i = e >> 6, j = e & 63;
-              const float f = (i == j) ? 1.f : Ss[e];
-              const float2 v = *reinterpret_cast<const float2 *>(Pst + 2 * e);
-              float *o = P.counts + (size_t)e * C + cp;
-              if (vec2 && nc >= 2) {
-                *reinterpret_cast<float2 *>(o) = make_float2(f * v.x, f * v.y);
+        sync_tc();   // D1's tensor-memory loads are done before the next pair's D1 overwrites it
+        if (t == 0) mma6(tm + 64u * p, A2, VV, kIdesc, 1);
+        __syncwarp();
+      }
+      wait_t(1);   // the last pair's D2
+      // (k) counts rows (i, j = jj) of columns 4 cg .. 4 cg + 3, i in [32 hh, 32 hh + 32)
+      {
+        const int col0 = c_base + g0 + 4 * cg;
+        const int ncol = min(4, gcols - 4 * cg);
+        const bool vec4 = (C & 3) == 0 && (col0 & 3) == 0 && ncol == 4;
+        if (ncol > 0) {
+#pragma unroll 1
+          for (int h16 = 0; h16 < 2; ++h16) {
+            const int i0 = 32 * hh + 16 * h16;
+            uint32_t v[4][16];
+#pragma unroll
+            for (int p = 0; p < 4; ++p)
+              asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,"
+                           "%14,%15}, [%16];\n"
+                           "tcgen05.wait::ld.sync.aligned;"
+                           : "=r"(v[p][0]), "=r"(v[p][1]), "=r"(v[p][2]), "=r"(v[p][3]), "=r"(v[p][4]),
+                             "=r"(v[p][5]), "=r"(v[p][6]), "=r"(v[p][7]), "=r"(v[p][8]), "=r"(v[p][9]),
+                             "=r"(v[p][10]), "=r"(v[p][11]), "=r"(v[p][12]), "=r"(v[p][13]), "=r"(v[p][14]),
+                             "=r"(v[p][15])
+                           : "r"(tm + ((uint32_t)(32 * sub) << 16) + 64u * p + (uint32_t)i0)
+                           : "memory");
+#pragma unroll
+            for (int i2 = 0; i2 < 16; ++i2) {
+              const int i = i0 + i2;
+              const float f = (i == jj) ? 1.f : Ss[i * A + jj];
+              const float4 o4 = make_float4(f * __uint_as_float(v[0][i2]), f * __uint_as_float(v[1][i2]),
+                                            f * __uint_as_float(v[2][i2]), f * __uint_as_float(v[3][i2]));
+              float *o = P.counts + (size_t)(i * A + jj) * C + col0;
+              if (vec4) {
+                *reinterpret_cast<float4 *>(o) = o4;
               } else {
-                o[0] = f * v.x;
-                if (nc >= 2) o[1] = f * v.y;
+                o[0] = o4.x;
+                if (ncol > 1) o[1] = o4.y;
+                if (ncol > 2) o[2] = o4.z;
+                if (ncol > 3) o[3] = o4.w;
               }
             }
+          }
         }
-        if (p < 3) wait_t(0);   // D1(p+1)
       }
+      // every tensor-memory read done before the next group's products
+      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
       __syncthreads();
       continue;
     }
@@ -613,7 +616,7 @@ __global__ void __launch_bounds__(256, 1) k_acc(const KParams P, const float *__
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     if ((t >> 5) == 0)
-      asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(s_tm), "r"(256) : "memory");
+      asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(s_tm), "r"(512) : "memory");
   }
   if (t == 0 && s_err && P.err) atomicAdd(P.err, 1);
 }
